@@ -1,0 +1,166 @@
+/* modal_gb300.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * Modal-CMB mode-space hot path: Gauss-Legendre quadrature, the P_l(mu)
+ * table, the l-contraction M/A(mu), the Gamma matrix of inner products of
+ * symmetrised separable modes, its orthogonalisation, the projection of
+ * bispectrum shapes onto the modes and the alpha solve.
+ *
+ * Plain C: pointers, sizes and status codes; no CUDA or torch types.  Host
+ * pointers are caller-owned; device buffers are owned by the context.  Each
+ * context owns one CUDA stream; calls on one context are stream-ordered and
+ * blocking unless stated; a context is not thread-safe (like the reference's
+ * module-static state).  Layouts are the reference's: row-major FP64 arrays
+ * exactly as its fwrite'd files (arrays.c:6-21).
+ *
+ * Each entry point names the reference function it replaces (file:line in
+ * the Modal-CMB sources).
+ */
+#ifndef MODAL_GB300_H
+#define MODAL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MODAL_OK = 0,
+    MODAL_ERR_ARG = 1,      /* bad size, NULL pointer, mode index out of range */
+    MODAL_ERR_CUDA = 2,     /* CUDA runtime failure; text in modal_last_error() */
+    MODAL_ERR_NOT_PD = 3,   /* Cholesky met a non-positive pivot; *info = pivot row */
+    MODAL_ERR_TIMEOUT = 4,  /* a bounded device wait gave up */
+    MODAL_ERR_NOMEM = 5,    /* device allocation failed */
+    MODAL_ERR_STATE = 6,    /* a prerequisite call is missing (basis, modes, ...) */
+    MODAL_ERR_NOCONV = 7    /* iterative eigensolver did not converge */
+} modal_status;
+
+typedef enum {
+    MODAL_PREC_FP64 = 0,    /* plain form: FP64 throughout */
+    MODAL_PREC_SPLIT = 1    /* split-precision tensor-core form, FP64 accumulation */
+} modal_prec;
+
+typedef enum {
+    MODAL_SHAPE_SEPARABLE = 0, /* S = sum_t (1/6) sum_perm f_t(l1) g_t(l2) h_t(l3) */
+    MODAL_SHAPE_BUMP = 1       /* S = exp(-|(l1,l2,l3)/(l1+l2+l3) - c|^2 / (2 sigma^2)) */
+} modal_shape_kind;
+
+/* One bispectrum shape, evaluated on the device at each tetrapyd point
+ * (replaces the per-point callback calculate_3D_bispectrum,
+ * calculate_mode_3D.c:266-281). */
+typedef struct {
+    int kind;            /* modal_shape_kind */
+    int nterms;          /* SEPARABLE: number of terms T */
+    const double *tab;   /* SEPARABLE: host [T][3][lmax+1]: f_t, g_t, h_t over l = 0..lmax */
+    double c[3];         /* BUMP: centre */
+    double sigma;        /* BUMP: width */
+} modal_shape;
+
+typedef struct modal_ctx modal_ctx;
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device` with its own stream. */
+modal_status modal_ctx_create(int device, modal_ctx **out);
+void modal_ctx_destroy(modal_ctx *ctx);
+/* Text of the last failure on the calling thread ("" if none). */
+const char *modal_last_error(void);
+/* The context's cudaStream_t, as an opaque pointer (for event timing). */
+void *modal_ctx_stream(modal_ctx *ctx);
+/* Number of CUDA kernels this context has launched so far. */
+long modal_ctx_launches(const modal_ctx *ctx);
+/* Block until all work on the context's stream is done. */
+modal_status modal_ctx_sync(modal_ctx *ctx);
+
+/* ------------------------------------------------- stand-alone primitives */
+
+/* Gauss-Legendre nodes and weights on [-1,1], ascending, computed on the GPU.
+ * Replaces asy() (gl_integration.c:46-168; global.h:421).  Same layout:
+ * symmetric pairs, exact 0 middle node for odd n. */
+modal_status modal_gl_nodes(int n, double *nodes, double *weights);
+
+/* out[k][l] = (2l+1)^{2/3} P_l(mu[k]), l = 0..lmax, FP64 three-term
+ * recurrence on the GPU.  Replaces the gl_Pl loop with gsl_sf_legendre_Pl
+ * (orthogonalisation_late.c:47-54). */
+modal_status modal_legendre_table(int nmu, int lmax, const double *mu, double *out);
+
+/* Shifted Legendre basis out[i][j] = P_j(2(values[i]-min)/(max-min) - 1),
+ * j = 0..pmax.  Replaces basis_functions_legendre (basis_functions.c:88-107;
+ * global.h:361). */
+modal_status modal_basis_legendre(int size, int pmax, double min, double max,
+                                  const double *values, double *out);
+
+/* Asymptotic geometric factor h~^2(l1,l2,l3) at npts points pts[n][3].
+ * Replaces calculate_geometric (calculate_geometric.c:59-92; global.h:370). */
+modal_status modal_geometric(long npts, const int *pts, double *out);
+
+/* Number of tetrapyd points lmin <= i <= j <= k <= lmax, k <= i+j, i+j+k even,
+ * as counted by decompose_tetrapyd_XXX (tetrapyd_tools.c:31-51). */
+modal_status modal_tetrapyd_count(int lmin, int lmax, long *count);
+
+/* ------------------------------------------------------------- pipeline */
+
+/* Install the 1D basis q[L][P] (L = lmax-lmin+1; layout of basis_late_T,
+ * fixed_data.c:1764) for l = lmin..lmax.  Resets everything derived from it.
+ * Replaces the basis reads of init_orthol_glint (orthogonalisation_late.c:56-64). */
+modal_status modal_set_basis(modal_ctx *ctx, int lmin, int lmax, int P, const double *q);
+
+/* Install the mode list triples[N][3] (order_late_TTT layout,
+ * set_terms_late fixed_data.c:272-467 / find_perm_late_TTT :983-990). */
+modal_status modal_set_modes(modal_ctx *ctx, int N, const int *triples);
+
+/* Optional: use caller-supplied quadrature (e.g. the output of the
+ * reference's asy()) instead of the GPU nodes.  nodes/weights[nmu]. */
+modal_status modal_set_gl(modal_ctx *ctx, int nmu, const double *nodes, const double *weights);
+
+/* GL nodes (n_mu = 3 lmax/2 + 1 unless set), P_l table and the l-contraction
+ * M[i][j][k] for all P^2 (i,j) in FP64.  Replaces init_orthol_glint
+ * (orthogonalisation_late.c:23-97) + calculate_orthoMij_T for all pairs
+ * (:99-129, ortho_late_mpi.c:170-225) + sync_orthoMij (:159-237). */
+modal_status modal_init_glint(modal_ctx *ctx);
+
+/* Download M as Mij_T[P][P][n_mu] (orthogonalisation_late.c:76). */
+modal_status modal_get_mij(modal_ctx *ctx, double *out);
+/* Download the quadrature in use (n_mu values each). */
+modal_status modal_get_gl(modal_ctx *ctx, int *nmu, double *nodes, double *weights);
+
+/* Gamma[N][N] = <Q_m, Q_n> with the 1/(48 pi) GL weight, full symmetric
+ * matrix, same scale as calculate_orthol (orthogonalisation_late.c:239-336)
+ * filled over all pairs and symmetrised (ortho_late_mpi.c:231-363).
+ * gamma may be NULL: the result stays on the device for the next steps. */
+modal_status modal_gamma(modal_ctx *ctx, modal_prec prec, double *gamma);
+
+/* result[0] = Gamma_mn, the per-pair interface of calculate_orthol
+ * (orthogonalisation_late.c:239; global.h:211).  Computes the whole matrix
+ * on first use and answers later pairs from it. */
+modal_status modal_orthol_pair(modal_ctx *ctx, int m, int n, double *result);
+
+/* Orthogonalise Gamma (ortho_late_mpi.c:724-876): normalise by sqrt(diag),
+ * then either Cholesky (orthol = D^{1/2} L, lambdal = L^{-1} D^{-1/2}) or,
+ * when pca_flag == 0 or the normalised Gamma is not positive definite, the
+ * PCA branch on its eigen-decomposition.  gamma: host [N][N] or NULL for
+ * the device result of modal_gamma.  orthol/lambdal: host [N][N] or NULL
+ * (kept on the device).  *branch = 0 Cholesky, 1 PCA; *rank = number of
+ * retained eigenvalues (N for Cholesky).  FP64 on the GPU. */
+modal_status modal_orthogonalise(modal_ctx *ctx, const double *gamma, int pca_flag,
+                                 double *orthol, double *lambdal, int *branch, int *rank);
+
+/* Install C_l + N_l/b_l^2 for l = 0..lmax (get_cl_TT etc., used for the
+ * per-leg weight w_l = (2l+1)^{1/6}/sqrt(.) of calculate_mode_3D.c:53-62). */
+modal_status modal_set_spectrum(modal_ctx *ctx, const double *cl);
+
+/* beta[s][r] = sum over the tetrapyd of permsix h~^2 prod(2l+1)^{-1/3}
+ * S_s(l1,l2,l3) w_l1 w_l2 w_l3 Q_r(l1,l2,l3) for S shapes in one call.
+ * Replaces calculate_mode_3D (calculate_mode_3D.c:217-264) driven over
+ * decompose_tetrapyd_XXX blocks (eigenmodetoday_mpi.c:235-273).  beta may be
+ * NULL (kept on the device for modal_alpha). */
+modal_status modal_project(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec,
+                           double *beta);
+
+/* alpha = lambdal^T lambdal beta and modesR = orthol^T alpha
+ * (eigenmodetoday_mpi.c:148-162, 286-316) for S shapes, FP64 on the GPU.
+ * beta: host [S][N] or NULL for the device result of modal_project.
+ * alpha/modesR: host [S][N] or NULL. */
+modal_status modal_alpha(modal_ctx *ctx, int S, const double *beta, double *alpha, double *modesR);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MODAL_GB300_H */

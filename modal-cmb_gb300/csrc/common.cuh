@@ -1,0 +1,119 @@
+// common.cuh -- context state and helpers shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include "../../include/modal_gb300.h"
+
+namespace modal {
+
+// Last error text (thread-local), returned by modal_last_error().
+void set_error(const char *fmt, ...);
+
+// Device buffer that grows on demand; contents are not preserved on growth.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    template <typename T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+}  // namespace modal
+
+struct modal_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    long launches = 0;
+
+    // problem description
+    int lmin = 0, lmax = 0, L = 0, P = 0, N = 0, nmu = 0;
+    bool have_basis = false, have_modes = false, have_user_gl = false;
+    bool have_glint = false, have_gamma = false, have_spec = false, have_ortho = false;
+    bool have_beta = false;
+    int ortho_branch = 0, ortho_rank = 0;
+    int beta_S = 0;
+
+    // device state
+    modal::DevBuf q;        // [L][P] basis
+    modal::DevBuf triples;  // [N][3]
+    modal::DevBuf mu, w;    // [nmu] quadrature
+    modal::DevBuf pl;       // [lmax+1][nmu] (2l+1)^{2/3} P_l(mu_k), l-major
+    modal::DevBuf mt;       // [nmu][P][P] l-contraction, mu-major
+    modal::DevBuf gamma;    // [N][N]
+    modal::DevBuf chol;     // [N][N] work: normalised Gamma -> L
+    modal::DevBuf linv;     // [N][N] work: L^{-1}
+    modal::DevBuf orthol;   // [N][N]
+    modal::DevBuf lambdal;  // [N][N]
+    modal::DevBuf norm;     // [N]
+    modal::DevBuf info;     // [4] int status words
+    modal::DevBuf cl;       // [lmax+1] C_l + N_l/b_l^2
+    modal::DevBuf vl;       // [lmax+1] (2l+1)^{-1/3} w_l
+    modal::DevBuf beta;     // [S][N]
+    modal::DevBuf alpha;    // [S][N]
+    modal::DevBuf modesr;   // [S][N]
+    modal::DevBuf scratch;  // general work area
+    modal::DevBuf scratch2;
+    modal::DevBuf shape_tab;   // separable tables
+    modal::DevBuf shape_desc;  // device shape descriptors
+    modal::DevBuf slab_order;  // projection slab schedule
+    double *h_info = nullptr;  // pinned readback
+};
+
+namespace modal {
+
+modal_status ensure(DevBuf &b, size_t bytes);
+void release(DevBuf &b);
+
+#define MODAL_CUDA(call)                                                                  \
+    do {                                                                                  \
+        cudaError_t err__ = (call);                                                       \
+        if (err__ != cudaSuccess) {                                                       \
+            ::modal::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call,                 \
+                               cudaGetErrorString(err__));                                \
+            return MODAL_ERR_CUDA;                                                        \
+        }                                                                                 \
+    } while (0)
+
+#define MODAL_TRY(expr)                                                                   \
+    do {                                                                                  \
+        modal_status st__ = (expr);                                                       \
+        if (st__ != MODAL_OK) return st__;                                                \
+    } while (0)
+
+// Check the last launch; counts it on the context.
+inline modal_status launched(modal_ctx *ctx, const char *what)
+{
+    ctx->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("launch %s: %s", what, cudaGetErrorString(e));
+        return MODAL_ERR_CUDA;
+    }
+    return MODAL_OK;
+}
+
+inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+
+// ---- entry points implemented per translation unit (internal) ----
+modal_status gl_nodes_dev(modal_ctx *ctx, int n, double *d_mu, double *d_w);
+modal_status legendre_table_dev(modal_ctx *ctx, int nmu, int lmax, const double *d_mu, double *d_pl);
+modal_status mij_dev(modal_ctx *ctx);
+modal_status gamma_fp64_dev(modal_ctx *ctx);
+modal_status gamma_split_dev(modal_ctx *ctx);
+modal_status ortho_dev(modal_ctx *ctx, int pca_flag);
+modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec);
+modal_status alpha_dev(modal_ctx *ctx, int S);
+modal_status transpose_dev(modal_ctx *ctx, const double *in, double *out, int R, int C);
+modal_status basis_legendre_dev(modal_ctx *ctx, int size, int pmax, double min, double max, const double *d_values,
+                                double *d_out);
+modal_status geometric_dev(modal_ctx *ctx, long npts, const int *d_pts, double *d_out);
+
+// FP64 tiled GEMM on the context stream:
+//   C[m][n] = beta*C[m][n] + alpha * sum_k opA(m,k) opB(k,n)
+//   opA(m,k) = transA ? A[k*lda+m] : A[m*lda+k];  opB(k,n) = transB ? B[n*ldb+k] : B[k*ldb+n]
+//   lower != 0: only entries with n <= m (tiles above the diagonal skipped).
+modal_status dgemm(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, int lda, bool transA,
+                   const double *B, int ldb, bool transB, double beta, double *C, int ldc, int lower);
+
+}  // namespace modal

@@ -1,0 +1,92 @@
+// eig.cu -- PCA branch of the orthogonalisation (ortho_late_mpi.c:775-805),
+// taken when pca_flag == 0 or the normalised Gamma is not positive definite.
+//
+// The symmetric eigen-decomposition of the normalised Gamma (the reference's
+// gsl_eigen_symmv + gsl_eigen_symmv_sort descending, :775-776) is the
+// cuSOLVER library routine cusolverDnDsyevd in FP64 on the GPU.  The outputs
+// follow the reference exactly, with eigenvalues e_i in descending order and
+// r = the number of leading positive eigenvalues:
+//   lambda[i][j]    = V[j][i] / (norm_j sqrt(e_i))   for i < r, else 0
+//   lambdainv[i][j] = norm_i V[i][j] sqrt(e_j)        for j < r, else 0
+// stored as lambdal and orthol.  Eigenvector signs are those of the solver.
+#include <cusolverDn.h>
+#include "common.cuh"
+
+namespace modal {
+
+// Count leading positive eigenvalues in descending order (W is ascending).
+__global__ void k_pca_rank(int N, const double *__restrict__ W, int *rank)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int r = 0;
+    for (int i = 0; i < N && W[N - 1 - i] > 0.0; i++) r = i + 1;
+    *rank = r;
+}
+
+// V_rm: row-major buffer whose row a holds the eigenvector of ascending index a.
+__global__ void k_pca_outputs(int N, const double *__restrict__ V_rm, const double *__restrict__ W,
+                              const double *__restrict__ norm, const int *__restrict__ rank,
+                              double *__restrict__ orthol, double *__restrict__ lambdal)
+{
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * N) return;
+    const int r = *rank;
+    int i = (int)(e / N), j = (int)(e % N);
+    // lambda[i][j] = V[j][desc i] / (norm_j sqrt(e_desc i))
+    double lam = 0.0;
+    if (i < r) {
+        int a = N - 1 - i;
+        lam = V_rm[(size_t)a * N + j] / (norm[j] * sqrt(W[a]));
+    }
+    double inv = 0.0;
+    if (j < r) {
+        int a = N - 1 - j;
+        inv = norm[i] * V_rm[(size_t)a * N + i] * sqrt(W[a]);
+    }
+    lambdal[e] = lam;
+    orthol[e] = inv;
+}
+
+modal_status eig_pca_dev(modal_ctx *ctx)
+{
+    const int N = ctx->N;
+    cusolverDnHandle_t h = nullptr;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return MODAL_ERR_CUDA; }
+    cusolverDnSetStream(h, ctx->stream);
+    modal_status st = MODAL_OK;
+    int lwork = 0;
+    double *A = ctx->chol.as<double>();  // symmetric: row-major == column-major
+    if (ensure(ctx->scratch2, sizeof(double) * (size_t)N) != MODAL_OK) { cusolverDnDestroy(h); return MODAL_ERR_NOMEM; }
+    double *W = ctx->scratch2.as<double>();
+    if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N, W, &lwork) !=
+        CUSOLVER_STATUS_SUCCESS) {
+        set_error("syevd_bufferSize failed");
+        cusolverDnDestroy(h);
+        return MODAL_ERR_CUDA;
+    }
+    st = ensure(ctx->scratch, sizeof(double) * (size_t)lwork + 64);
+    if (st != MODAL_OK) { cusolverDnDestroy(h); return st; }
+    int *devinfo = ctx->info.as<int>() + 1;
+    int *rank = ctx->info.as<int>() + 2;
+    cusolverStatus_t cs = cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N, W,
+                                           ctx->scratch.as<double>(), lwork, devinfo);
+    cusolverDnDestroy(h);
+    if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return MODAL_ERR_CUDA; }
+    int hinfo = 0;
+    MODAL_CUDA(cudaMemcpyAsync(&hinfo, devinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (hinfo != 0) { set_error("syevd info=%d", hinfo); return MODAL_ERR_NOCONV; }
+    k_pca_rank<<<1, 1, 0, ctx->stream>>>(N, W, rank);
+    MODAL_TRY(launched(ctx, "pca_rank"));
+    size_t NN = (size_t)N * N;
+    k_pca_outputs<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, A, W, ctx->norm.as<double>(), rank,
+                                                                       ctx->orthol.as<double>(), ctx->lambdal.as<double>());
+    MODAL_TRY(launched(ctx, "pca_outputs"));
+    int hr = 0;
+    MODAL_CUDA(cudaMemcpyAsync(&hr, rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->ortho_rank = hr;
+    return MODAL_OK;
+}
+
+}  // namespace modal

@@ -1,0 +1,373 @@
+// ortho.cu -- FP64 orthogonalisation of Gamma and the alpha solve on the GPU.
+//
+// Cholesky branch of ortho_late_mpi.c:759-843:
+//   norm_i = sqrt(gamma_ii), ghat = gamma_ij / (norm_i norm_j)
+//   ghat = L L^T                      (blocked right-looking Cholesky, lower)
+//   orthol[i][j]  = norm_i L_ij       (i >= j, 0 above)
+//   lambdal[i][j] = (L^{-1})_ij / norm_j
+// The reference builds lambdal from gsl_linalg_LU_invert of the upper factor
+// L^T with the identity permutation and transposes it (:821-841); that is
+// (L^{-1})^T transposed back, i.e. L^{-1}.  Here L^{-1} comes from a blocked
+// forward substitution L X = I.
+//
+// A non-positive pivot (ghat not positive definite) is recorded as the
+// smallest failing row in a device status word; the host then reports
+// MODAL_ERR_NOT_PD or takes the PCA branch (eig.cu).
+//
+// Alpha solve (eigenmodetoday_mpi.c:148-162, 286-316):
+//   alpha = lambdal^T (lambdal beta),  modesR = lambdainv^T alpha with
+//   lambdainv the lower triangle of orthol (or the PCA lambdainv).
+#include <climits>
+#include "common.cuh"
+
+namespace modal {
+
+// --------------------------------------------------------------------------
+// FP64 tiled GEMM (64x64 tile, K step 16, 4x4 outputs per thread).
+// --------------------------------------------------------------------------
+constexpr int GT = 64, GK = 16;
+
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, const double *__restrict__ A, int lda,
+                                               const double *__restrict__ B, int ldb, double beta, double *C, int ldc,
+                                               int lower)
+{
+    const int bm = blockIdx.y * GT, bn = blockIdx.x * GT;
+    if (lower && bn > bm + GT - 1) return;
+    __shared__ double As[GK][GT + 1];
+    __shared__ double Bs[GK][GT + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
+
+    for (int k0 = 0; k0 < K; k0 += GK) {
+#pragma unroll
+        for (int t = 0; t < (GK * GT) / 256; t++) {
+            int e = tid + 256 * t;
+            int kk, mm;
+            if (TA) { mm = e % GT; kk = e / GT; }
+            else { kk = e % GK; mm = e / GK; }
+            int m = bm + mm, k = k0 + kk;
+            double v = 0.0;
+            if (m < M && k < K) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+            As[kk][mm] = v;
+        }
+#pragma unroll
+        for (int t = 0; t < (GK * GT) / 256; t++) {
+            int e = tid + 256 * t;
+            int kk, nn;
+            if (TB) { kk = e % GK; nn = e / GK; }
+            else { nn = e % GT; kk = e / GT; }
+            int n = bn + nn, k = k0 + kk;
+            double v = 0.0;
+            if (n < N && k < K) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
+            Bs[kk][nn] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GK; kk++) {
+            double a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        int m = bm + ty + 16 * i;
+        if (m >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            int n = bn + tx + 16 * j;
+            if (n >= N || (lower && n > m)) continue;
+            double *c = C + (size_t)m * ldc + n;
+            *c = (beta == 0.0) ? alpha * acc[i][j] : fma(alpha, acc[i][j], beta * *c);
+        }
+    }
+}
+
+modal_status dgemm(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, int lda, bool transA,
+                   const double *B, int ldb, bool transB, double beta, double *C, int ldc, int lower)
+{
+    if (M <= 0 || N <= 0) return MODAL_OK;
+    dim3 grid(ceil_div(N, GT), ceil_div(M, GT));
+    if (!transA && !transB) k_dgemm<false, false><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    else if (!transA && transB) k_dgemm<false, true><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    else if (transA && !transB) k_dgemm<true, false><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    else k_dgemm<true, true><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
+    return launched(ctx, "dgemm");
+}
+
+// --------------------------------------------------------------------------
+// Normalisation (ortho_late_mpi.c:759-773).
+// --------------------------------------------------------------------------
+__global__ void k_norm(int N, const double *__restrict__ g, double *__restrict__ norm)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) norm[i] = sqrt(g[(size_t)i * N + i]);
+}
+
+__global__ void k_normalise(int N, const double *__restrict__ g, const double *__restrict__ norm, double *__restrict__ a)
+{
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * N) return;
+    int i = (int)(e / N), j = (int)(e % N);
+    a[e] = g[e] / (norm[i] * norm[j]);
+}
+
+// --------------------------------------------------------------------------
+// Cholesky of one nb x nb diagonal block in shared memory (right-looking).
+// info[0] = smallest failing pivot row (INT_MAX when none).
+// --------------------------------------------------------------------------
+constexpr int NB = 64;
+constexpr size_t TRI_SMEM = sizeof(double) * 2 * NB * (NB + 1);  // two 64 x 65 FP64 tiles
+
+__global__ void __launch_bounds__(256) k_potrf_diag(double *A, int N, int kb, int nb, int *info)
+{
+    __shared__ double s[NB][NB + 1];
+    __shared__ int bad;
+    const int tid = threadIdx.x;
+    if (tid == 0) bad = 0;
+    for (int e = tid; e < nb * nb; e += 256) {
+        int i = e / nb, j = e % nb;
+        s[i][j] = A[(size_t)(kb + i) * N + kb + j];
+    }
+    __syncthreads();
+    for (int j = 0; j < nb; j++) {
+        if (tid == 0) {
+            double d = s[j][j];
+            if (!(d > 0.0)) {
+                if (!bad) atomicMin(info, kb + j);
+                bad = 1;
+            }
+            s[j][j] = sqrt(d);
+        }
+        __syncthreads();
+        const double ljj = s[j][j];
+        for (int i = j + 1 + tid; i < nb; i += 256) s[i][j] /= ljj;
+        __syncthreads();
+        const int m = nb - j - 1;  // trailing size
+        for (int e = tid; e < m * m; e += 256) {
+            int i = j + 1 + e / m, c = j + 1 + e % m;
+            if (c <= i) s[i][c] -= s[i][j] * s[c][j];
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < nb * nb; e += 256) {
+        int i = e / nb, j = e % nb;
+        if (j <= i) A[(size_t)(kb + i) * N + kb + j] = s[i][j];
+    }
+}
+
+// Panel below the diagonal block: row r of A21 := row r of A21 * L11^{-T}.
+// One thread per row; 64 rows per CTA; rows staged in shared memory.
+__global__ void __launch_bounds__(64) k_trsm_panel(double *A, int N, int kb, int nb)
+{
+    extern __shared__ double dsm[];
+    double (*L11)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm);
+    double (*R)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm + NB * (NB + 1));
+    const int tid = threadIdx.x;
+    const int r0 = kb + nb + blockIdx.x * 64;
+    for (int e = tid; e < nb * nb; e += 64) {
+        int i = e / nb, j = e % nb;
+        L11[i][j] = A[(size_t)(kb + i) * N + kb + j];
+    }
+    for (int e = tid; e < 64 * nb; e += 64) {
+        int rr = e / nb, c = e % nb;
+        int r = r0 + rr;
+        R[rr][c] = (r < N) ? A[(size_t)r * N + kb + c] : 0.0;
+    }
+    __syncthreads();
+    if (r0 + tid < N) {
+        for (int c = 0; c < nb; c++) {
+            double s = R[tid][c];
+            for (int t = 0; t < c; t++) s -= R[tid][t] * L11[c][t];
+            R[tid][c] = s / L11[c][c];
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < 64 * nb; e += 64) {
+        int rr = e / nb, c = e % nb;
+        int r = r0 + rr;
+        if (r < N) A[(size_t)r * N + kb + c] = R[rr][c];
+    }
+}
+
+// --------------------------------------------------------------------------
+// X = L^{-1} by blocked forward substitution on L X = I.
+// Step for row block r: X[rb:rb+nb, 0:rb+nb] = L_rr^{-1} B[rb:rb+nb, 0:rb+nb]
+// (one thread per column), then B[rb+nb:, 0:rb+nb] -= L[rb+nb:, rb:rb+nb] X[rb:rb+nb, 0:rb+nb].
+// --------------------------------------------------------------------------
+__global__ void k_eye(int N, double *X)
+{
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * N) return;
+    X[e] = ((e / N) == (e % N)) ? 1.0 : 0.0;
+}
+
+__global__ void __launch_bounds__(64) k_trsv_diag(const double *L, double *X, int N, int rb, int nb, int ncols)
+{
+    extern __shared__ double dsm[];
+    double (*Ld)[NB + 1] = reinterpret_cast<double (*)[NB + 1]>(dsm);
+    double (*Xs)[64 + 1] = reinterpret_cast<double (*)[64 + 1]>(dsm + NB * (NB + 1));
+    const int tid = threadIdx.x;
+    const int c0 = blockIdx.x * 64;
+    for (int e = tid; e < nb * nb; e += 64) {
+        int i = e / nb, j = e % nb;
+        Ld[i][j] = L[(size_t)(rb + i) * N + rb + j];
+    }
+    for (int e = tid; e < nb * 64; e += 64) {
+        int i = e / 64, cc = e % 64;
+        int c = c0 + cc;
+        Xs[i][cc] = (c < ncols) ? X[(size_t)(rb + i) * N + c] : 0.0;
+    }
+    __syncthreads();
+    if (c0 + tid < ncols) {
+        for (int i = 0; i < nb; i++) {
+            double s = Xs[i][tid];
+            for (int t = 0; t < i; t++) s -= Ld[i][t] * Xs[t][tid];
+            Xs[i][tid] = s / Ld[i][i];
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < nb * 64; e += 64) {
+        int i = e / 64, cc = e % 64;
+        int c = c0 + cc;
+        if (c < ncols) X[(size_t)(rb + i) * N + c] = Xs[i][cc];
+    }
+}
+
+// orthol = D^{1/2} L (lower), lambdal = X D^{-1/2} (lower).
+__global__ void k_chol_outputs(int N, const double *__restrict__ Lm, const double *__restrict__ X,
+                               const double *__restrict__ norm, double *__restrict__ orthol, double *__restrict__ lambdal)
+{
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * N) return;
+    int i = (int)(e / N), j = (int)(e % N);
+    orthol[e] = (i >= j) ? norm[i] * Lm[e] : 0e0;
+    lambdal[e] = (i >= j) ? X[e] / norm[j] : 0.0;
+}
+
+modal_status eig_pca_dev(modal_ctx *ctx);  // eig.cu
+
+modal_status cholesky_dev(modal_ctx *ctx, int *fail_row)
+{
+    const int N = ctx->N;
+    double *A = ctx->chol.as<double>();
+    int *info = ctx->info.as<int>();
+    const int big = INT_MAX;
+    MODAL_CUDA(cudaFuncSetAttribute(k_trsm_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRI_SMEM));
+    MODAL_CUDA(cudaMemcpyAsync(info, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    for (int kb = 0; kb < N; kb += NB) {
+        int nb = (N - kb < NB) ? (N - kb) : NB;
+        k_potrf_diag<<<1, 256, 0, ctx->stream>>>(A, N, kb, nb, info);
+        MODAL_TRY(launched(ctx, "potrf_diag"));
+        int rest = N - kb - nb;
+        if (rest > 0) {
+            k_trsm_panel<<<ceil_div(rest, 64), 64, TRI_SMEM, ctx->stream>>>(A, N, kb, nb);
+            MODAL_TRY(launched(ctx, "trsm_panel"));
+            double *A21 = A + (size_t)(kb + nb) * N + kb;
+            double *A22 = A + (size_t)(kb + nb) * N + kb + nb;
+            MODAL_TRY(dgemm(ctx, rest, rest, nb, -1.0, A21, N, false, A21, N, true, 1.0, A22, N, 1));
+        }
+    }
+    int h = 0;
+    MODAL_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
+    *fail_row = (h == INT_MAX) ? -1 : h;
+    return MODAL_OK;
+}
+
+modal_status trtri_dev(modal_ctx *ctx)
+{
+    const int N = ctx->N;
+    const double *Lm = ctx->chol.as<double>();
+    double *X = ctx->linv.as<double>();
+    size_t NN = (size_t)N * N;
+    MODAL_CUDA(cudaFuncSetAttribute(k_trsv_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRI_SMEM));
+    k_eye<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, X);
+    MODAL_TRY(launched(ctx, "eye"));
+    for (int rb = 0; rb < N; rb += NB) {
+        int nb = (N - rb < NB) ? (N - rb) : NB;
+        int ncols = rb + nb;
+        k_trsv_diag<<<ceil_div(ncols, 64), 64, TRI_SMEM, ctx->stream>>>(Lm, X, N, rb, nb, ncols);
+        MODAL_TRY(launched(ctx, "trsv_diag"));
+        int rest = N - rb - nb;
+        if (rest > 0)
+            MODAL_TRY(dgemm(ctx, rest, ncols, nb, -1.0, Lm + (size_t)(rb + nb) * N + rb, N, false,
+                            X + (size_t)rb * N, N, false, 1.0, X + (size_t)(rb + nb) * N, N, 0));
+    }
+    return MODAL_OK;
+}
+
+modal_status ortho_dev(modal_ctx *ctx, int pca_flag)
+{
+    const int N = ctx->N;
+    size_t NN = (size_t)N * N;
+    MODAL_TRY(ensure(ctx->norm, sizeof(double) * N));
+    MODAL_TRY(ensure(ctx->chol, sizeof(double) * NN));
+    MODAL_TRY(ensure(ctx->orthol, sizeof(double) * NN));
+    MODAL_TRY(ensure(ctx->lambdal, sizeof(double) * NN));
+    MODAL_TRY(ensure(ctx->info, 4 * sizeof(int)));
+    k_norm<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(N, ctx->gamma.as<double>(), ctx->norm.as<double>());
+    MODAL_TRY(launched(ctx, "norm"));
+    k_normalise<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, ctx->gamma.as<double>(), ctx->norm.as<double>(),
+                                                                     ctx->chol.as<double>());
+    MODAL_TRY(launched(ctx, "normalise"));
+    ctx->have_ortho = false;
+    if (pca_flag != 0) {
+        int fail = -1;
+        MODAL_TRY(cholesky_dev(ctx, &fail));
+        if (fail < 0) {
+            MODAL_TRY(ensure(ctx->linv, sizeof(double) * NN));
+            MODAL_TRY(trtri_dev(ctx));
+            k_chol_outputs<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(
+                N, ctx->chol.as<double>(), ctx->linv.as<double>(), ctx->norm.as<double>(), ctx->orthol.as<double>(),
+                ctx->lambdal.as<double>());
+            MODAL_TRY(launched(ctx, "chol_outputs"));
+            ctx->ortho_branch = 0;
+            ctx->ortho_rank = N;
+            ctx->have_ortho = true;
+            return MODAL_OK;
+        }
+        // not positive definite: re-normalise (the factorisation overwrote it) and take the PCA branch
+        k_normalise<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, ctx->gamma.as<double>(),
+                                                                         ctx->norm.as<double>(), ctx->chol.as<double>());
+        MODAL_TRY(launched(ctx, "normalise"));
+        ctx->ortho_rank = fail;  // first failing pivot, reported if PCA is unavailable
+    }
+    MODAL_TRY(eig_pca_dev(ctx));
+    ctx->ortho_branch = 1;
+    ctx->have_ortho = true;
+    return MODAL_OK;
+}
+
+// --------------------------------------------------------------------------
+// Alpha solve for S shapes: y = beta lambdal^T, alpha = y lambdal,
+// modesR = alpha lambdainv with lambdainv = orthol (rows j, cols i).
+// --------------------------------------------------------------------------
+modal_status alpha_dev(modal_ctx *ctx, int S)
+{
+    const int N = ctx->N;
+    MODAL_TRY(ensure(ctx->alpha, sizeof(double) * (size_t)S * N));
+    MODAL_TRY(ensure(ctx->modesr, sizeof(double) * (size_t)S * N));
+    MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)S * N));
+    double *y = ctx->scratch2.as<double>();
+    const double *lam = ctx->lambdal.as<double>();
+    MODAL_TRY(dgemm(ctx, S, N, N, 1.0, ctx->beta.as<double>(), N, false, lam, N, true, 0.0, y, N, 0));
+    MODAL_TRY(dgemm(ctx, S, N, N, 1.0, y, N, false, lam, N, false, 0.0, ctx->alpha.as<double>(), N, 0));
+    MODAL_TRY(dgemm(ctx, S, N, N, 1.0, ctx->alpha.as<double>(), N, false, ctx->orthol.as<double>(), N, false, 0.0,
+                    ctx->modesr.as<double>(), N, 0));
+    return MODAL_OK;
+}
+
+}  // namespace modal

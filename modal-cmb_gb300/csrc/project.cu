@@ -1,0 +1,271 @@
+// project.cu -- projection of bispectrum shapes onto the modes.
+//
+// Reference (calculate_mode_3D, calculate_mode_3D.c:217-264, over the walk of
+// get_ijk_next_XXX, tetrapyd_tools.c:104-142):
+//   beta_r = sum_{i<=j<=k<=lmax, k<=i+j, i+j+k even}
+//            permsix(i,j,k) h~^2(i,j,k) prod (2l+1)^{-1/3} S(i,j,k) w_i w_j w_k
+//            * plijk_TTT(r,i,j,k)
+// with plijk_TTT the 1/6 sum of the six q-products (orthogonalisation_late.c:620-644).
+//
+// Sum factorisation: with f(i,j,k) the scalar weight above,
+//   B[a][b][c] = sum_i q_a(i) sum_j q_b(j) sum_k f(i,j,k) q_c(k)
+//   beta_r     = (1/6) sum over the six orderings s of B[p_s1][p_s2][p_s3]
+// for mode r = (p1,p2,p3).  That is O(points * P) instead of O(points * N).
+// One CTA per slab l1 = i; the tetrapyd rows j are processed JC at a time:
+//   phase 1: f(i,j,k) for the JC rows into shared memory (shape evaluated here)
+//   phase 2: H[j][c] = sum_k f(i,j,k) q_c(k)
+//   phase 3: F_i[b][c] += sum_j q_b(j) H[j][c]          (registers)
+// F_i goes to a [S][L][P*P] buffer; a second pass forms B and beta.
+#include <algorithm>
+#include <vector>
+#include "common.cuh"
+
+namespace modal {
+
+struct DShape {
+    int kind, nterms;
+    long tab_off;
+    double c1, c2, c3, sigma;
+};
+
+__device__ __forceinline__ double d_permsix(int i, int j, int k)
+{
+    if (i == k && i == j) return 1.0;
+    if (i == j || j == k || i == k) return 3.0;
+    return 6.0;
+}
+
+// calculate_geometric (calculate_geometric.c:59-92) for a point already known
+// to satisfy parity and the triangle condition.
+__device__ __forceinline__ double d_geo(int l1, int l2, int l3)
+{
+    double s1 = l1 + l2 + l3 + 1.0, s3 = l1 + l2 + l3 + 1.0 / 3.0, s6 = l1 + l2 + l3 + 1.0 / 6.0;
+    double s13 = l2 + l3 - l1 + 1.0 / 3.0, s23 = l3 + l1 - l2 + 1.0 / 3.0, s33 = l1 + l2 - l3 + 1.0 / 3.0;
+    double s16 = l2 + l3 - l1 + 1.0 / 6.0, s26 = l3 + l1 - l2 + 1.0 / 6.0, s36 = l1 + l2 - l3 + 1.0 / 6.0;
+    const double ipi = 0.318309886183790671537767526745028724;
+    double fact = ipi * ipi / 2.0;
+    double p1 = fact * ((2.0 * l1 + 1.0) * (2.0 * l2 + 1.0) * (2.0 * l3 + 1.0)) / s1;
+    double p2 = s3 / (s13 * s23 * s33);
+    double p3 = sqrt(s16 * s26 * s36 / s6);
+    return p1 * p2 * p3;
+}
+
+__device__ __forceinline__ double d_shape(const DShape &s, const double *__restrict__ tab, int stride, int i, int j, int k)
+{
+    if (s.kind == MODAL_SHAPE_SEPARABLE) {
+        double acc = 0.0;
+        for (int t = 0; t < s.nterms; t++) {
+            const double *f = tab + s.tab_off + (long)t * 3 * stride;
+            const double *g = f + stride, *h = g + stride;
+            double v = f[i] * g[j] * h[k] + f[i] * g[k] * h[j] + f[j] * g[i] * h[k] + f[j] * g[k] * h[i] +
+                       f[k] * g[i] * h[j] + f[k] * g[j] * h[i];
+            acc += v / 6.0;
+        }
+        return acc;
+    }
+    double L = (double)(i + j + k);
+    double x1 = i / L - s.c1, x2 = j / L - s.c2, x3 = k / L - s.c3;
+    return exp(-(x1 * x1 + x2 * x2 + x3 * x3) / (2.0 * s.sigma * s.sigma));
+}
+
+// v_l = (2l+1)^{-1/3} w_l, w_l = (2l+1)^{1/6}/sqrt(C_l + N_l/b_l^2), w_0 = w_1 = 0
+// (calculate_mode_3D.c:53-62, get_weight :283-290).
+__global__ void k_vl(int lmax, const double *__restrict__ cl, double *__restrict__ vl)
+{
+    int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l > lmax) return;
+    vl[l] = (l < 2) ? 0.0 : pow(2.0 * l + 1.0, -1.0 / 3.0) * (pow(2.0 * l + 1.0, 1.0 / 6.0) / sqrt(cl[l]));
+}
+
+constexpr int JC = 8;
+
+template <int FPT>
+__global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, int P, int S, int KMAX,
+                                                            const int *__restrict__ slab_order,
+                                                            const double *__restrict__ q, const double *__restrict__ vl,
+                                                            const DShape *__restrict__ shapes,
+                                                            const double *__restrict__ tab, double *__restrict__ Fbuf)
+{
+    extern __shared__ double sm[];
+    double *f = sm;               // [JC][KMAX]
+    double *H = sm + JC * KMAX;   // [JC][P]
+    const int slab = slab_order[blockIdx.x];
+    const int i = lmin + slab;
+    const int tid = threadIdx.x;
+    const int PP = P * P, L = lmax - lmin + 1, stride = lmax + 1;
+    const double vi = vl[i];
+    const int par = i & 1;
+    for (int s = 0; s < S; s++) {
+        const DShape sh = shapes[s];
+        double Facc[FPT];
+#pragma unroll
+        for (int t = 0; t < FPT; t++) Facc[t] = 0.0;
+        for (int j0 = i; j0 <= lmax; j0 += JC) {
+            for (int e = tid; e < JC * KMAX; e += 256) {
+                int jj = e / KMAX, kk = e - jj * KMAX, j = j0 + jj;
+                double val = 0.0;
+                if (j <= lmax) {
+                    int k = j + par + 2 * kk, k1 = min(i + j, lmax);
+                    if (k <= k1)
+                        val = d_permsix(i, j, k) * d_geo(i, j, k) * vi * vl[j] * vl[k] * d_shape(sh, tab, stride, i, j, k);
+                }
+                f[e] = val;
+            }
+            __syncthreads();
+            for (int e = tid; e < JC * P; e += 256) {
+                int jj = e / P, c = e - jj * P, j = j0 + jj;
+                double acc = 0.0;
+                if (j <= lmax) {
+                    int kf = j + par, k1 = min(i + j, lmax);
+                    int nk = (k1 >= kf) ? (k1 - kf) / 2 + 1 : 0;
+                    const double *fr = f + jj * KMAX;
+                    const double *qc = q + (size_t)(kf - lmin) * P + c;
+                    for (int kk = 0; kk < nk; kk++) acc = fma(fr[kk], qc[(size_t)2 * kk * P], acc);
+                }
+                H[e] = acc;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int t = 0; t < FPT; t++) {
+                int e = tid + 256 * t;
+                if (e < PP) {
+                    int b = e / P, c = e - b * P;
+                    double a = 0.0;
+                    for (int jj = 0; jj < JC; jj++) {
+                        int j = j0 + jj;
+                        if (j <= lmax) a = fma(q[(size_t)(j - lmin) * P + b], H[jj * P + c], a);
+                    }
+                    Facc[t] += a;
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int t = 0; t < FPT; t++) {
+            int e = tid + 256 * t;
+            if (e < PP) Fbuf[((size_t)s * L + slab) * PP + e] = Facc[t];
+        }
+    }
+}
+
+// B[s][a][bc] = sum_slab q[slab][a] Fbuf[s][slab][bc]
+__global__ void k_project_B(int L, int P, int S, const double *__restrict__ q, const double *__restrict__ Fbuf,
+                            double *__restrict__ B)
+{
+    const int PP = P * P;
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)S * P * PP) return;
+    int s = (int)(e / ((size_t)P * PP));
+    int rem = (int)(e - (size_t)s * P * PP);
+    int a = rem / PP, bc = rem - a * PP;
+    const double *F = Fbuf + (size_t)s * L * PP + bc;
+    double acc = 0.0;
+    for (int l = 0; l < L; l++) acc = fma(q[(size_t)l * P + a], F[(size_t)l * PP], acc);
+    B[e] = acc;
+}
+
+// beta[s][r] = (1/6) sum of B over the six orderings of mode r's triple
+__global__ void k_project_beta(int N, int P, int S, const int *__restrict__ triples, const double *__restrict__ B,
+                               double *__restrict__ beta)
+{
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)S * N) return;
+    int s = (int)(e / N), r = (int)(e % N);
+    int p1 = triples[3 * r], p2 = triples[3 * r + 1], p3 = triples[3 * r + 2];
+    const double *b = B + (size_t)s * P * P * P;
+#define BB(x, y, z) b[((size_t)(x) * P + (y)) * P + (z)]
+    double v = BB(p1, p2, p3) + BB(p2, p3, p1) + BB(p3, p1, p2) + BB(p3, p2, p1) + BB(p2, p1, p3) + BB(p1, p3, p2);
+#undef BB
+    beta[e] = v / 6e0;
+}
+
+static long slab_points(int i, int lmax)
+{
+    long n = 0;
+    for (int j = i; j <= lmax; j++) {
+        int kf = j + (i & 1), k1 = std::min(i + j, lmax);
+        if (k1 >= kf) n += (k1 - kf) / 2 + 1;
+    }
+    return n;
+}
+
+modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec)
+{
+    (void)prec;
+    const int lmin = ctx->lmin, lmax = ctx->lmax, L = ctx->L, P = ctx->P, N = ctx->N, PP = P * P;
+    // shapes -> device descriptors + concatenated separable tables
+    std::vector<DShape> ds(S);
+    long tab_total = 0;
+    for (int s = 0; s < S; s++) {
+        const modal_shape &m = shapes[s];
+        if (m.kind == MODAL_SHAPE_SEPARABLE) {
+            if (m.nterms < 1 || !m.tab) { set_error("shape %d: separable needs nterms >= 1 and a table", s); return MODAL_ERR_ARG; }
+            tab_total += (long)m.nterms * 3 * (lmax + 1);
+        } else if (m.kind == MODAL_SHAPE_BUMP) {
+            if (!(m.sigma > 0.0)) { set_error("shape %d: bump sigma must be > 0", s); return MODAL_ERR_ARG; }
+        } else {
+            set_error("shape %d: unknown kind %d", s, m.kind);
+            return MODAL_ERR_ARG;
+        }
+    }
+    MODAL_TRY(ensure(ctx->shape_tab, sizeof(double) * (size_t)(tab_total > 0 ? tab_total : 1)));
+    MODAL_TRY(ensure(ctx->shape_desc, sizeof(DShape) * (size_t)S));
+    long off = 0;
+    for (int s = 0; s < S; s++) {
+        const modal_shape &m = shapes[s];
+        ds[s].kind = m.kind;
+        ds[s].nterms = m.nterms;
+        ds[s].tab_off = off;
+        ds[s].c1 = m.c[0]; ds[s].c2 = m.c[1]; ds[s].c3 = m.c[2];
+        ds[s].sigma = m.sigma;
+        if (m.kind == MODAL_SHAPE_SEPARABLE) {
+            size_t n = (size_t)m.nterms * 3 * (lmax + 1);
+            MODAL_CUDA(cudaMemcpyAsync(ctx->shape_tab.as<double>() + off, m.tab, sizeof(double) * n,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+            off += (long)n;
+        }
+    }
+    MODAL_CUDA(cudaMemcpyAsync(ctx->shape_desc.ptr, ds.data(), sizeof(DShape) * S, cudaMemcpyHostToDevice, ctx->stream));
+    // slab schedule: heaviest slabs first
+    std::vector<int> order(L);
+    std::vector<long> cnt(L);
+    for (int s = 0; s < L; s++) { order[s] = s; cnt[s] = slab_points(lmin + s, lmax); }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+    MODAL_TRY(ensure(ctx->slab_order, sizeof(int) * (size_t)L));
+    MODAL_CUDA(cudaMemcpyAsync(ctx->slab_order.ptr, order.data(), sizeof(int) * L, cudaMemcpyHostToDevice, ctx->stream));
+
+    MODAL_TRY(ensure(ctx->vl, sizeof(double) * (lmax + 1)));
+    k_vl<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax, ctx->cl.as<double>(), ctx->vl.as<double>());
+    MODAL_TRY(launched(ctx, "vl"));
+
+    size_t fbytes = sizeof(double) * (size_t)S * L * PP;
+    size_t bbytes = sizeof(double) * (size_t)S * P * PP;
+    MODAL_TRY(ensure(ctx->scratch, fbytes + bbytes));
+    double *Fbuf = ctx->scratch.as<double>();
+    double *B = Fbuf + (size_t)S * L * PP;
+    const int KMAX = (lmax - lmin) / 2 + 2;
+    size_t smem = sizeof(double) * ((size_t)JC * KMAX + (size_t)JC * P);
+    if (smem > 220 * 1024) { set_error("project: lmax=%d too large for the slab tile", lmax); return MODAL_ERR_ARG; }
+    int fpt = ceil_div(PP, 256);
+    auto run = [&](auto kern) -> modal_status {
+        MODAL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<L, 256, smem, ctx->stream>>>(lmin, lmax, P, S, KMAX, ctx->slab_order.as<int>(), ctx->q.as<double>(),
+                                            ctx->vl.as<double>(), ctx->shape_desc.as<DShape>(),
+                                            ctx->shape_tab.as<double>(), Fbuf);
+        return launched(ctx, "project_slab_fp64");
+    };
+    if (fpt <= 1) MODAL_TRY(run(k_project_slab_fp64<1>));
+    else if (fpt <= 4) MODAL_TRY(run(k_project_slab_fp64<4>));
+    else if (fpt <= 8) MODAL_TRY(run(k_project_slab_fp64<8>));
+    else if (fpt <= 16) MODAL_TRY(run(k_project_slab_fp64<16>));
+    else { set_error("project: P=%d too large", P); return MODAL_ERR_ARG; }
+    size_t nb = (size_t)S * P * PP;
+    k_project_B<<<ceil_div((long)nb, 256), 256, 0, ctx->stream>>>(L, P, S, ctx->q.as<double>(), Fbuf, B);
+    MODAL_TRY(launched(ctx, "project_B"));
+    MODAL_TRY(ensure(ctx->beta, sizeof(double) * (size_t)S * N));
+    k_project_beta<<<ceil_div((long)S * N, 256), 256, 0, ctx->stream>>>(N, P, S, ctx->triples.as<int>(), B,
+                                                                          ctx->beta.as<double>());
+    return launched(ctx, "project_beta");
+}
+
+}  // namespace modal

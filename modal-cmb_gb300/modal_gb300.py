@@ -1,0 +1,372 @@
+"""Python host mirror of the C ABI in include/modal_gb300.h (ctypes).
+
+The product is the shared library libmodal_gb300.so (CUDA kernels for
+sm_103a behind a plain C ABI).  This module loads it, raises ModalError on
+any non-zero status, and builds the synthetic workloads of the benchmark
+configurations (synthetic spectrum, shifted Legendre basis, mode triples,
+separable and Gaussian-bump shapes).  There is no CPU fallback: if the
+library is missing, loading fails.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmodal_gb300.so")
+
+PREC_FP64 = 0
+PREC_SPLIT = 1
+SHAPE_SEPARABLE = 0
+SHAPE_BUMP = 1
+
+STATUS = {0: "MODAL_OK", 1: "MODAL_ERR_ARG", 2: "MODAL_ERR_CUDA", 3: "MODAL_ERR_NOT_PD", 4: "MODAL_ERR_TIMEOUT",
+          5: "MODAL_ERR_NOMEM", 6: "MODAL_ERR_STATE", 7: "MODAL_ERR_NOCONV"}
+
+# Every entry point declared in include/modal_gb300.h.
+EXPORTS = [
+    "modal_ctx_create", "modal_ctx_destroy", "modal_last_error", "modal_ctx_stream", "modal_ctx_launches",
+    "modal_ctx_sync", "modal_gl_nodes", "modal_legendre_table", "modal_basis_legendre", "modal_geometric",
+    "modal_tetrapyd_count", "modal_set_basis", "modal_set_modes", "modal_set_gl", "modal_init_glint",
+    "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_orthol_pair", "modal_orthogonalise",
+    "modal_set_spectrum", "modal_project", "modal_alpha",
+]
+
+
+class ModalError(RuntimeError):
+    def __init__(self, status, msg):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+
+
+class CShape(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("nterms", ctypes.c_int), ("tab", ctypes.c_void_p),
+                ("c", ctypes.c_double * 3), ("sigma", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libmodal_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is missing: run modal-cmb_gb300/build.py (no CPU fallback exists)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i, l, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_double
+        sig = {
+            "modal_ctx_create": (i, [i, ctypes.POINTER(vp)]),
+            "modal_ctx_destroy": (None, [vp]),
+            "modal_last_error": (ctypes.c_char_p, []),
+            "modal_ctx_stream": (vp, [vp]),
+            "modal_ctx_launches": (l, [vp]),
+            "modal_ctx_sync": (i, [vp]),
+            "modal_gl_nodes": (i, [i, vp, vp]),
+            "modal_legendre_table": (i, [i, i, vp, vp]),
+            "modal_basis_legendre": (i, [i, i, d, d, vp, vp]),
+            "modal_geometric": (i, [l, vp, vp]),
+            "modal_tetrapyd_count": (i, [i, i, ctypes.POINTER(l)]),
+            "modal_set_basis": (i, [vp, i, i, i, vp]),
+            "modal_set_modes": (i, [vp, i, vp]),
+            "modal_set_gl": (i, [vp, i, vp, vp]),
+            "modal_init_glint": (i, [vp]),
+            "modal_get_mij": (i, [vp, vp]),
+            "modal_get_gl": (i, [vp, ctypes.POINTER(i), vp, vp]),
+            "modal_gamma": (i, [vp, i, vp]),
+            "modal_orthol_pair": (i, [vp, i, i, vp]),
+            "modal_orthogonalise": (i, [vp, vp, i, vp, vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
+            "modal_set_spectrum": (i, [vp, vp]),
+            "modal_project": (i, [vp, i, vp, i, vp]),
+            "modal_alpha": (i, [vp, i, vp, vp, vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(status):
+    if status != 0:
+        raise ModalError(status, lib().modal_last_error().decode(errors="replace"))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ---------------------------------------------------------------- primitives
+
+def gl_nodes(n):
+    """Gauss-Legendre nodes/weights on the GPU (asy() layout)."""
+    x = np.empty(n)
+    w = np.empty(n)
+    _check(lib().modal_gl_nodes(n, _ptr(x), _ptr(w)))
+    return x, w
+
+
+def legendre_table(mu, lmax):
+    """[nmu][lmax+1] table (2l+1)^{2/3} P_l(mu_k) on the GPU."""
+    mu = _f64(mu)
+    out = np.empty((mu.size, lmax + 1))
+    _check(lib().modal_legendre_table(mu.size, lmax, _ptr(mu), _ptr(out)))
+    return out
+
+
+def basis_legendre(values, pmax, vmin, vmax):
+    values = _f64(values)
+    out = np.empty((values.size, pmax + 1))
+    _check(lib().modal_basis_legendre(values.size, pmax, float(vmin), float(vmax), _ptr(values), _ptr(out)))
+    return out
+
+
+def geometric(pts):
+    pts = np.ascontiguousarray(pts, dtype=np.int32).reshape(-1, 3)
+    out = np.empty(pts.shape[0])
+    _check(lib().modal_geometric(pts.shape[0], _ptr(pts), _ptr(out)))
+    return out
+
+
+def tetrapyd_count(lmin, lmax):
+    n = ctypes.c_long()
+    _check(lib().modal_tetrapyd_count(lmin, lmax, ctypes.byref(n)))
+    return n.value
+
+
+def shapes_to_c(shapes):
+    """List of shape dicts -> (ctypes array, keep-alive list)."""
+    arr = (CShape * len(shapes))()
+    keep = []
+    for s, sh in enumerate(shapes):
+        arr[s].kind = sh["kind"]
+        if sh["kind"] == SHAPE_SEPARABLE:
+            tab = _f64(sh["tab"])
+            keep.append(tab)
+            arr[s].nterms = tab.shape[0]
+            arr[s].tab = tab.ctypes.data
+        else:
+            arr[s].c[0], arr[s].c[1], arr[s].c[2] = (float(v) for v in sh["c"])
+            arr[s].sigma = float(sh["sigma"])
+    return arr, keep
+
+
+class Context:
+    """One GPU context (device buffers + one CUDA stream)."""
+
+    def __init__(self, device=0):
+        h = ctypes.c_void_p()
+        _check(lib().modal_ctx_create(device, ctypes.byref(h)))
+        self.h = h
+        self.N = self.P = self.lmin = self.lmax = None
+
+    def close(self):
+        if self.h:
+            lib().modal_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def stream(self):
+        return lib().modal_ctx_stream(self.h)
+
+    @property
+    def launches(self):
+        return lib().modal_ctx_launches(self.h)
+
+    def sync(self):
+        _check(lib().modal_ctx_sync(self.h))
+
+    def set_basis(self, lmin, lmax, q):
+        q = _f64(q)
+        assert q.shape[0] == lmax - lmin + 1
+        _check(lib().modal_set_basis(self.h, lmin, lmax, q.shape[1], _ptr(q)))
+        self.lmin, self.lmax, self.P = lmin, lmax, q.shape[1]
+
+    def set_modes(self, triples):
+        t = np.ascontiguousarray(triples, dtype=np.int32).reshape(-1, 3)
+        _check(lib().modal_set_modes(self.h, t.shape[0], _ptr(t)))
+        self.N = t.shape[0]
+
+    def set_gl(self, nodes, weights):
+        nodes, weights = _f64(nodes), _f64(weights)
+        _check(lib().modal_set_gl(self.h, nodes.size, _ptr(nodes), _ptr(weights)))
+
+    def init_glint(self):
+        _check(lib().modal_init_glint(self.h))
+
+    def get_gl(self):
+        n = ctypes.c_int()
+        _check(lib().modal_get_gl(self.h, ctypes.byref(n), None, None))
+        x, w = np.empty(n.value), np.empty(n.value)
+        _check(lib().modal_get_gl(self.h, ctypes.byref(n), _ptr(x), _ptr(w)))
+        return x, w
+
+    def get_mij(self):
+        n = ctypes.c_int()
+        _check(lib().modal_get_gl(self.h, ctypes.byref(n), None, None))
+        out = np.empty((self.P, self.P, n.value))
+        _check(lib().modal_get_mij(self.h, _ptr(out)))
+        return out
+
+    def gamma(self, prec=PREC_FP64, download=True):
+        out = np.empty((self.N, self.N)) if download else None
+        _check(lib().modal_gamma(self.h, prec, _ptr(out)))
+        return out
+
+    def orthol_pair(self, m, n):
+        r = np.zeros(4)
+        _check(lib().modal_orthol_pair(self.h, m, n, _ptr(r)))
+        return r[0]
+
+    def orthogonalise(self, gamma=None, pca_flag=1, download=True):
+        g = None if gamma is None else _f64(gamma)
+        o = np.empty((self.N, self.N)) if download else None
+        lam = np.empty((self.N, self.N)) if download else None
+        br, rk = ctypes.c_int(), ctypes.c_int()
+        _check(lib().modal_orthogonalise(self.h, _ptr(g), pca_flag, _ptr(o), _ptr(lam), ctypes.byref(br),
+                                         ctypes.byref(rk)))
+        return o, lam, br.value, rk.value
+
+    def set_spectrum(self, cl):
+        cl = _f64(cl)
+        assert cl.size >= self.lmax + 1
+        _check(lib().modal_set_spectrum(self.h, _ptr(cl)))
+
+    def project(self, shapes, prec=PREC_FP64, download=True):
+        arr, keep = shapes_to_c(shapes)
+        out = np.empty((len(shapes), self.N)) if download else None
+        _check(lib().modal_project(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), prec, _ptr(out)))
+        del keep
+        return out
+
+    def alpha(self, S, beta=None, download=True):
+        b = None if beta is None else _f64(beta)
+        a = np.empty((S, self.N)) if download else None
+        m = np.empty((S, self.N)) if download else None
+        _check(lib().modal_alpha(self.h, S, _ptr(b), _ptr(a), _ptr(m)))
+        return a, m
+
+
+# ----------------------------------------------------------- synthetic inputs
+
+def synthetic_cl(lmax):
+    """C_l = 1e3/(l(l+1)) exp(-(l/1500)^2) + 1e-4 (noise, beam 1); l < 2 set to 1."""
+    l = np.arange(lmax + 1, dtype=np.float64)
+    cl = np.ones(lmax + 1)
+    ll = l[2:]
+    cl[2:] = 1e3 / (ll * (ll + 1.0)) * np.exp(-(ll / 1500.0) ** 2) + 1e-4
+    return cl
+
+
+def legendre_q(lmin, lmax, P):
+    """Shifted Legendre basis q_p(l) = P_p(2(l-lmin)/(lmax-lmin) - 1), [L][P]
+    (basis_functions_legendre with min=lmin, max=lmax; numpy restatement used
+    only to build inputs)."""
+    l = np.arange(lmin, lmax + 1, dtype=np.float64)
+    x = (l - lmin) / (lmax - lmin)
+    q = np.zeros((l.size, P))
+    q[:, 0] = 1.0
+    if P > 1:
+        q[:, 1] = 2.0 * x - 1.0
+    for j in range(2, P):
+        q[:, j] = ((2.0 * j - 1.0) * q[:, 1] * q[:, j - 1] - (j - 1.0) * q[:, j - 2]) / j
+    return q
+
+
+def weighted_q(q, cl, lmin):
+    """q~_p(l) = q_p(l) (2l+1)^{1/6} / sqrt(C_l): with the (2l+1)^{2/3} of the
+    P_l table this gives A_pp'(mu) = sum_l (2l+1) P_l(mu) q_p q_p' / C_l."""
+    l = np.arange(lmin, lmin + q.shape[0], dtype=np.float64)
+    return q * ((2.0 * l + 1.0) ** (1.0 / 6.0) / np.sqrt(cl[lmin:lmin + q.shape[0]]))[:, None]
+
+
+def mode_triples(P):
+    """All p <= r <= s < P, in the order of set_terms_late case 2
+    (fixed_data.c:362-418: increasing total p+r+s), keeping entries < P."""
+    want = P * (P + 1) * (P + 2) // 6
+    out = []
+    i = j = k = s = 0
+    while len(out) < want:
+        if k < P:
+            out.append((i, j, k))
+        if i < j:
+            j -= 1
+            k += 1
+        elif i > 0:
+            i -= 1
+            j = (s - i) // 2
+            k = s - j - i
+        else:
+            s += 1
+            i = s // 3
+            j = (s - i) // 2
+            k = s - i - j
+    return np.array(out, dtype=np.int32)
+
+
+def separable_shapes(lmax, S, seed, tmin=1, tmax=2):
+    """S seeded shapes S = sym sum_t l1^a l2^b l3^c, a,b,c ~ U[-2,0], T ~ U{tmin..tmax}."""
+    rng = np.random.default_rng(seed)
+    l = np.arange(lmax + 1, dtype=np.float64)
+    l[0] = 1.0  # l = 0,1 never reached (lmin >= 2)
+    out = []
+    for _ in range(S):
+        T = int(rng.integers(tmin, tmax + 1))
+        ex = rng.uniform(-2.0, 0.0, size=(T, 3))
+        tab = np.empty((T, 3, lmax + 1))
+        for t in range(T):
+            for a in range(3):
+                tab[t, a] = l ** ex[t, a]
+        out.append({"kind": SHAPE_SEPARABLE, "tab": tab, "exponents": ex})
+    return out
+
+
+def bump_shapes(S, seed):
+    """S seeded Gaussian bumps, centre ~ Dirichlet(1,1,1), sigma ~ U[0.05,0.3]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(S):
+        c = rng.dirichlet([1.0, 1.0, 1.0])
+        out.append({"kind": SHAPE_BUMP, "c": c, "sigma": float(rng.uniform(0.05, 0.3))})
+    return out
+
+
+# The benchmark configurations (lmin = 2 everywhere).
+CONFIGS = {
+    "cfg1": dict(lmax=500, P=10, shapes=("sep", 4, 1, 2)),
+    "cfg2": dict(lmax=2000, P=30, shapes=("sep", 16, 1, 2)),
+    "cfg3": dict(lmax=2000, P=30, shapes=("mix", 256, 1, 4)),
+    "cfg5": dict(lmax=2500, P=40, shapes=("mix", 512, 1, 4)),
+}
+
+
+def workload(lmax, P, lmin=2):
+    """(q~ [L][P], triples [N][3], cl [lmax+1]) for a shifted-Legendre config."""
+    cl = synthetic_cl(lmax)
+    q = weighted_q(legendre_q(lmin, lmax, P), cl, lmin)
+    return q, mode_triples(P), cl
+
+
+def config_shapes(lmax, spec, seed=0):
+    kind, S, tmin, tmax = spec
+    if kind == "sep":
+        return separable_shapes(lmax, S, seed, tmin, tmax)
+    half = S // 2
+    return separable_shapes(lmax, half, seed, tmin, tmax) + bump_shapes(S - half, seed + 1)

@@ -1,0 +1,457 @@
+/* modal_oracle.c -- CPU FP64 restatement of the Modal-CMB mode-space hot path.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT CODE.  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU-baseline leg load this library, and only as a checker or
+ * as the timed CPU baseline.  The CUDA library never calls it.
+ *
+ * Each function restates one reference routine (file:line in the Modal-CMB
+ * sources) in plain C with the same arithmetic, so that outputs can be
+ * compared element-wise with the CUDA path.  The restatement is itself pinned
+ * against the reference sources compiled in place (oracle/_ref, see
+ * oracle/Makefile) and against golden vectors under tests/golden/ that were
+ * produced by that build.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+#include "shapes.h"
+
+#define ORC_PI 3.14159265358979323846
+
+/* ------------------------------------------------------------------------ */
+/* Gauss-Legendre nodes and weights.                                          */
+/* Layout as asy() (gl_integration.c:46-168): nodes ascending on [-1,1],      */
+/* symmetric pairs nodes[k-1] = -nodes[n-k], exact 0 for the middle node of  */
+/* odd n (gl_integration.c:156-165).  The reference uses the Hale-Townsend    */
+/* asymptotic method (QUADPTS, GPL-3+); this restatement instead runs Newton  */
+/* in theta (x = cos theta) from Tricomi's initial guess, evaluating P_n by   */
+/* the three-term recurrence written in differences D_l = P_l - P_{l-1} and   */
+/* y = 1 - x = 2 sin^2(theta/2):                                              */
+/*     D_{l+1} = (l D_l - (2l+1) y P_l) / (l+1),   P_{l+1} = P_l + D_{l+1},   */
+/* which keeps full relative accuracy next to x = 1 where the endpoint        */
+/* weights dominate the Gamma integrand.  Weight:                              */
+/*     w = 2 sin^2(theta) / (n (P_{n-1} - x P_n))^2.                          */
+/* Arithmetic in long double.                                                  */
+/* ------------------------------------------------------------------------ */
+static void gl_leg_diff(int n, long double th, long double *Pn, long double *Q)
+{
+    long double s = sinl(0.5L * th), y = 2.0L * s * s;
+    long double P = 1.0L, D = 0.0L;
+    for (int l = 0; l < n; l++) {
+        long double Dn = (l * D - (2.0L * l + 1.0L) * y * P) / (l + 1.0L);
+        P += Dn;
+        D = Dn;
+    }
+    *Pn = P;
+    *Q = -D + y * P; /* P_{n-1} - x P_n */
+}
+
+int orc_gl_nodes(int n, double *nodes, double *weights)
+{
+    if (n < 1) return 1;
+    const long double pi = 3.141592653589793238462643383279502884L;
+    const int half = n / 2;
+    for (int k = 1; k <= half; k++) {
+        long double th = pi * (4.0L * k - 1.0L) / (4.0L * n + 2.0L);
+        long double x0 = (1.0L - (n - 1.0L) / (8.0L * n * n * n)) * cosl(th);
+        th = acosl(x0);
+        long double Pn, Q;
+        for (int it = 0; it < 100; it++) {
+            gl_leg_diff(n, th, &Pn, &Q);
+            long double dth = Pn * sinl(th) / (n * Q);
+            th += dth;
+            if (fabsl(dth) <= 1e-19L * th) break;
+        }
+        gl_leg_diff(n, th, &Pn, &Q);
+        long double st = sinl(th);
+        long double w = 2.0L * st * st / ((long double)n * n * Q * Q);
+        nodes[n - k] = (double)cosl(th);
+        nodes[k - 1] = -(double)cosl(th);
+        weights[n - k] = (double)w;
+        weights[k - 1] = (double)w;
+    }
+    if (n & 1) {
+        long double Pn, Q;
+        gl_leg_diff(n, pi / 2.0L, &Pn, &Q);
+        nodes[half] = 0.0;
+        weights[half] = (double)(2.0L / ((long double)n * n * Q * Q));
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* gl_Pl[k][l] = (2l+1)^{2/3} P_l(mu_k), l = 0..lmax                           */
+/* (orthogonalisation_late.c:47-54).  P_l as GSL's gsl_sf_legendre_Pl: the   */
+/* upward recurrence p_l = (x(2l-1)p_{l-1} - (l-1)p_{l-2})/l from P_0, P_1,  */
+/* with P_2 = (3x^2-1)/2 returned in closed form.  One pass per mu gives the  */
+/* same values GSL computes per (l, mu) call.                                  */
+/* ------------------------------------------------------------------------ */
+int orc_legendre_table(int nmu, int lmax, const double *mu, double *out /*[nmu][lmax+1]*/)
+{
+    #pragma omp parallel for schedule(static)
+    for (int k = 0; k < nmu; k++) {
+        const double x = mu[k];
+        double *row = out + (long)k * (lmax + 1);
+        double pm2 = 1.0, pm1 = x;
+        for (int l = 0; l <= lmax; l++) {
+            double p;
+            if (l == 0) p = 1.0;
+            else if (l == 1) p = x;
+            else {
+                double pr = (x * (2 * l - 1) * pm1 - (l - 1) * pm2) / l;
+                pm2 = pm1; pm1 = pr;
+                if (l == 2) p = 0.5 * (3.0 * x * x - 1.0);
+                else if (x == 1.0) p = 1.0;
+                else if (x == -1.0) p = (l & 1) ? -1.0 : 1.0;
+                else p = pr;
+            }
+            row[l] = pow(2e0 * l + 1e0, 2e0 / 3e0) * p;
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Shifted Legendre basis q_j(v_i) = P_j(2(v_i-min)/(max-min) - 1)            */
+/* (basis_functions.c:88-107), out[size][pmax+1].                              */
+/* ------------------------------------------------------------------------ */
+int orc_basis_legendre(int size, int pmax, double min, double max, const double *values, double *out)
+{
+    for (int i = 0; i < size; i++) {
+        double *a = out + (long)i * (pmax + 1);
+        double x = (values[i] - min) / (max - min);
+        a[0] = 1e0;
+        if (pmax > 0) a[1] = 2e0 * x - 1e0;
+        for (int j = 2; j <= pmax; j++)
+            a[j] = ((2e0 * j - 1e0) * a[1] * a[j - 1] - (j - 1e0) * a[j - 2]) / (1e0 * j);
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* l-contraction M[i][j][s] = sum_{l=lmin}^{lmax} gl_Pl[s][l] q_i(l) q_j(l)   */
+/* (orthogonalisation_late.c:99-129, all P^2 (i,j) as ortho_late_mpi.c:170).  */
+/* basis[L][P] with L = lmax-lmin+1; out[P][P][nmu].                           */
+/* ------------------------------------------------------------------------ */
+int orc_mij(int nmu, int lmin, int lmax, int P, const double *gl_pl, const double *basis, double *out)
+{
+    const int L = lmax - lmin + 1;
+    #pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 0; i < P; i++)
+        for (int j = 0; j < P; j++) {
+            double *vec = malloc(sizeof(double) * (size_t)L);
+            for (int l = 0; l < L; l++) vec[l] = basis[(long)l * P + i] * basis[(long)l * P + j];
+            for (int s = 0; s < nmu; s++) {
+                const double *row = gl_pl + (long)s * (lmax + 1);
+                double sum = 0e0;
+                for (int l = lmin; l <= lmax; l++) sum += row[l] * vec[l - lmin];
+                out[((long)i * P + j) * nmu + s] = sum;
+            }
+            free(vec);
+        }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* gamma_mn = sum_k w_k/(48 pi) sum of the six products                       */
+/* (calculate_orthol, orthogonalisation_late.c:239-336, TTT part :283-295).   */
+/* ------------------------------------------------------------------------ */
+static double orthol_pair(int P, int nmu, const double *M, const double *w, const int *tm, const int *tn)
+{
+#define MM(a, b) (M + ((long)(a) * P + (b)) * nmu)
+    const double *a11 = MM(tm[0], tn[0]), *a22 = MM(tm[1], tn[1]), *a33 = MM(tm[2], tn[2]);
+    const double *a21 = MM(tm[1], tn[0]), *a32 = MM(tm[2], tn[1]), *a13 = MM(tm[0], tn[2]);
+    const double *a31 = MM(tm[2], tn[0]), *a12 = MM(tm[0], tn[1]), *a23 = MM(tm[1], tn[2]);
+#undef MM
+    double r = 0e0;
+    for (int i = 0; i < nmu; i++) {
+        double wgt1 = w[i] / (48e0 * ORC_PI);
+        double s1 = a11[i] * a22[i] * a33[i];
+        double s2 = a21[i] * a32[i] * a13[i];
+        double s3 = a31[i] * a12[i] * a23[i];
+        double s4 = a31[i] * a22[i] * a13[i];
+        double s5 = a21[i] * a12[i] * a33[i];
+        double s6 = a11[i] * a32[i] * a23[i];
+        double sum = s1 + s2 + s3 + s4 + s5 + s6;
+        r += wgt1 * sum;
+    }
+    return r;
+}
+
+int orc_orthol_pair(int P, int nmu, const double *M, const double *w, const int *triples, int m, int n, double *result)
+{
+    result[0] = orthol_pair(P, nmu, M, w, triples + 3 * m, triples + 3 * n);
+    return 0;
+}
+
+/* Full symmetric Gamma[N][N] from the upper triangle (ortho_late_mpi.c:231-363). */
+int orc_gamma(int N, const int *triples, int P, int nmu, const double *M, const double *w, int nthreads, double *out)
+{
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    #pragma omp parallel for schedule(dynamic, 4)
+    for (int i = 0; i < N; i++)
+        for (int j = i; j < N; j++) {
+            double g = orthol_pair(P, nmu, M, w, triples + 3 * i, triples + 3 * j);
+            out[(long)i * N + j] = g;
+            out[(long)j * N + i] = g;
+        }
+    return 0;
+}
+
+/* Gamma for the first `npairs` upper-triangle pairs (row-major order) only,
+ * for bounded CPU timing samples; returns the number of pairs done. */
+long orc_gamma_sample(int N, const int *triples, int P, int nmu, const double *M, const double *w, int nthreads,
+                      long npairs, double *out_pairs)
+{
+    long total = (long)N * (N + 1) / 2;
+    if (npairs <= 0 || npairs > total) npairs = total;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    #pragma omp parallel for schedule(static)
+    for (long p = 0; p < npairs; p++) {
+        /* invert p -> (i,j), i<=j, row-major over the upper triangle */
+        long i = (long)((2.0 * N + 1 - sqrt((2.0 * N + 1) * (2.0 * N + 1) - 8.0 * p)) / 2.0);
+        if (i < 0) i = 0;
+        while (i > 0 && i * N - i * (i - 1) / 2 > p) i--;
+        while ((i + 1) * N - (i + 1) * i / 2 <= p) i++;
+        long j = i + (p - (i * N - i * (i - 1) / 2));
+        out_pairs[p] = orthol_pair(P, nmu, M, w, triples + 3 * i, triples + 3 * j);
+    }
+    return npairs;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Asymptotic geometric factor h~^2 (calculate_geometric.c:59-92).            */
+/* ------------------------------------------------------------------------ */
+double orc_geometric(int l1, int l2, int l3)
+{
+    if (((l1 + l2 + l3) % 2) == 0 && l1 + l2 >= l3 && l2 + l3 >= l1 && l3 + l1 >= l2) {
+        double s1 = l1 + l2 + l3 + 1.0;
+        double s3 = l1 + l2 + l3 + 1.0 / 3.0;
+        double s6 = l1 + l2 + l3 + 1.0 / 6.0;
+        double s13 = l2 + l3 - l1 + 1.0 / 3.0;
+        double s23 = l3 + l1 - l2 + 1.0 / 3.0;
+        double s33 = l1 + l2 - l3 + 1.0 / 3.0;
+        double s16 = l2 + l3 - l1 + 1.0 / 6.0;
+        double s26 = l3 + l1 - l2 + 1.0 / 6.0;
+        double s36 = l1 + l2 - l3 + 1.0 / 6.0;
+        double fact = (1.0 / ORC_PI) * (1.0 / ORC_PI) / 2.0;
+        double p1 = fact * ((2.0 * l1 + 1.0) * (2.0 * l2 + 1.0) * (2.0 * l3 + 1.0)) / s1;
+        double p2 = s3 / (s13 * s23 * s33);
+        double p3 = sqrt(s16 * s26 * s36 / s6);
+        return p1 * p2 * p3;
+    }
+    return 0.0;
+}
+
+/* permsix (fixed_data.c:4244-4254): distinct orderings of (i,j,k). */
+double orc_permsix(int i, int j, int k)
+{
+    if (i == k && i == j) return 1.0;
+    if (i == j || j == k || i == k) return 3.0;
+    return 6.0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tetrapyd walk (tetrapyd_tools.c:104-142): i<=j<=k<=lmax, k<=i+j, i+j+k    */
+/* even, k stepping by 2, starting from check_ijk_min_XXX (:144-180).         */
+/* ------------------------------------------------------------------------ */
+int orc_tetrapyd_next(int lmax, int *i1, int *j1, int *k1)
+{
+    int i = *i1, j = *j1, k = *k1, test = 1;
+    if (i % 2 + j == lmax) { i++; j = i; k = j + i % 2; }
+    else if (k + 2 > lmax || k >= i + j) { j++; k = j + i % 2; }
+    else k += 2;
+    if (i + j + k + 1 >= 3 * lmax) {
+        test = 0;
+        if (lmax % 2 == 0) { i = lmax; j = lmax; k = lmax; }
+        else { i = lmax - 1; j = lmax; k = lmax; }
+    }
+    *i1 = i; *j1 = j; *k1 = k;
+    return test;
+}
+
+void orc_tetrapyd_start(int lmin, int *i, int *j, int *k)
+{
+    int i0 = *i < lmin ? lmin : *i, j0 = *j < lmin ? lmin : *j, k0 = *k < lmin ? lmin : *k, n;
+    if (i0 > j0) { n = j0; j0 = i0; i0 = n; }
+    if (j0 > k0) { n = j0; j0 = k0; k0 = n; if (i0 > j0) { n = j0; j0 = i0; i0 = n; } }
+    if (i0 + j0 < k0) k0 = i0 + j0;
+    else if ((i0 + j0 + k0) % 2 == 1) k0 = k0 + 1;
+    *i = i0; *j = j0; *k = k0;
+}
+
+/* Number of points the reference's decomposition assigns
+ * (decompose_tetrapyd_XXX, tetrapyd_tools.c:31-51). */
+long orc_tetrapyd_count(int lmin, int lmax)
+{
+    int i = lmin, j = lmin, k = lmin;
+    orc_tetrapyd_start(lmin, &i, &j, &k);
+    long count;
+    long countmax = (long)lmax * lmax * lmax + 1;
+    for (count = 1; count < countmax; count++)
+        if (!orc_tetrapyd_next(lmax, &i, &j, &k)) break;
+    return count + 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Projection (calculate_mode_3D, calculate_mode_3D.c:217-264):              */
+/* beta_r = sum over the walk of get_weight(i,j,k) S(i,j,k) w_i w_j w_k     */
+/*          * plijk_TTT(r,i,j,k)                                              */
+/* get_weight = permsix h~^2 prod (2l+1)^{-1/3} (:283-290);                   */
+/* w_l = (2l+1)^{1/6}/sqrt(C_l + N_l/b_l^2), w_0 = w_1 = 0 (:53-62);          */
+/* plijk_TTT (orthogonalisation_late.c:620-644) with basis index l - lmin.    */
+/* cl[l] holds C_l + N_l/b_l^2.  Walk points split over threads as          */
+/* decompose_tetrapyd_XXX does (equal contiguous counts).                     */
+/* `max_points` > 0 truncates each thread's block (timing samples).           */
+/* ------------------------------------------------------------------------ */
+static double plijk(const double *basis, int P, const int *tr, int lmin, int lmax, int l1, int l2, int l3)
+{
+    if (l1 < lmin || l1 > lmax || l2 < lmin || l2 > lmax || l3 < lmin || l3 > lmax) return 0e0;
+    const double *bi = basis + (long)(l1 - lmin) * P, *bj = basis + (long)(l2 - lmin) * P, *bk = basis + (long)(l3 - lmin) * P;
+    const int p1 = tr[0], p2 = tr[1], p3 = tr[2];
+    double b1 = bi[p1] * bj[p2] * bk[p3];
+    double b2 = bi[p2] * bj[p3] * bk[p1];
+    double b3 = bi[p3] * bj[p1] * bk[p2];
+    double b4 = bi[p3] * bj[p2] * bk[p1];
+    double b5 = bi[p2] * bj[p1] * bk[p3];
+    double b6 = bi[p1] * bj[p3] * bk[p2];
+    return (b1 + b2 + b3 + b4 + b5 + b6) / (6e0);
+}
+
+double orc_plijk(const double *basis, int P, const int *triples, int lmin, int lmax, int r, int l1, int l2, int l3)
+{
+    return plijk(basis, P, triples + 3 * r, lmin, lmax, l1, l2, l3);
+}
+
+static void weights_l(int lmax, const double *cl, double *wl)
+{
+    wl[0] = 0e0;
+    if (lmax >= 1) wl[1] = 0e0;
+    for (int i = 2; i <= lmax; i++) wl[i] = pow(2.0 * i + 1.0, 1.0 / 6.0) / sqrt(cl[i]);
+}
+
+int orc_project(int lmin, int lmax, int P, const double *basis, int N, const int *triples, const double *cl,
+                int kind, int nterms, const double *tab, double c1, double c2, double c3, double sigma,
+                int nthreads, long max_points, double *beta)
+{
+    orc_shape sh = {kind, nterms, lmax, tab, c1, c2, c3, sigma};
+    double *wl = malloc(sizeof(double) * (size_t)(lmax + 1));
+    weights_l(lmax, cl, wl);
+    long count = orc_tetrapyd_count(lmin, lmax);
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+    /* block starts as decompose_tetrapyd_XXX (one rank) */
+    long *loops = malloc(sizeof(long) * (size_t)nthreads);
+    int *start = malloc(sizeof(int) * 3 * (size_t)nthreads);
+    {
+        long size = count / nthreads, extra = count % nthreads;
+        for (int t = 0; t < nthreads; t++) loops[t] = size + (t < extra ? 1 : 0);
+        int i = lmin, j = lmin, k = lmin;
+        orc_tetrapyd_start(lmin, &i, &j, &k);
+        for (int t = 0; t < nthreads; t++) {
+            start[3 * t] = i; start[3 * t + 1] = j; start[3 * t + 2] = k;
+            for (long s = 0; s < loops[t]; s++) orc_tetrapyd_next(lmax, &i, &j, &k);
+        }
+    }
+    for (int r = 0; r < N; r++) beta[r] = 0e0;
+    omp_set_num_threads(nthreads);
+    #pragma omp parallel
+    {
+        int t = omp_get_thread_num();
+        double *priv = calloc((size_t)N, sizeof(double));
+        int i = start[3 * t], j = start[3 * t + 1], k = start[3 * t + 2];
+        long nl = loops[t];
+        if (max_points > 0 && nl > max_points) nl = max_points;
+        for (long n = 0; n < nl; n++) {
+            double gw = orc_permsix(i, j, k) * orc_geometric(i, j, k) * pow(2.0 * i + 1.0, -1.0 / 3.0)
+                      * pow(2.0 * j + 1.0, -1.0 / 3.0) * pow(2.0 * k + 1.0, -1.0 / 3.0);
+            double x = gw * orc_shape_eval(&sh, i, j, k) * wl[i] * wl[j] * wl[k];
+            for (int r = 0; r < N; r++) priv[r] += x * plijk(basis, P, triples + 3 * r, lmin, lmax, i, j, k);
+            orc_tetrapyd_next(lmax, &i, &j, &k);
+        }
+        #pragma omp critical
+        for (int r = 0; r < N; r++) beta[r] += priv[r];
+        free(priv);
+    }
+    free(loops); free(start); free(wl);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Orthogonalisation, Cholesky branch (ortho_late_mpi.c:759-773, 806-843):    */
+/*   norm_i = sqrt(gamma_ii); ghat = gamma_ij/(norm_i norm_j);               */
+/*   ghat = L L^T (gsl_linalg_cholesky_decomp);                               */
+/*   orthol[i][j] = norm_i L_ij (i>=j), 0 above;                             */
+/*   lambdal[i][j] = ((L^T)^{-1})[j][i] / norm_j (gsl_linalg_LU_invert of the */
+/*   upper factor with the identity permutation).                             */
+/* Returns 0, or 1 + the failing pivot row when ghat is not positive          */
+/* definite (GSL reports GSL_EDOM there).                                     */
+/* ------------------------------------------------------------------------ */
+long orc_ortho_cholesky(int N, const double *gamma, double *orthol, double *lambdal)
+{
+    double *norm = malloc(sizeof(double) * (size_t)N);
+    double *A = malloc(sizeof(double) * (size_t)N * N);
+    for (int i = 0; i < N; i++) norm[i] = sqrt(gamma[(long)i * N + i]);
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) A[(long)i * N + j] = gamma[(long)i * N + j] / (norm[i] * norm[j]);
+    /* left-looking Cholesky, lower triangle */
+    for (int j = 0; j < N; j++) {
+        double d = A[(long)j * N + j];
+        for (int k = 0; k < j; k++) d -= A[(long)j * N + k] * A[(long)j * N + k];
+        if (!(d > 0.0)) { free(norm); free(A); return 1 + (long)j; }
+        double ljj = sqrt(d);
+        A[(long)j * N + j] = ljj;
+        #pragma omp parallel for schedule(static)
+        for (int i = j + 1; i < N; i++) {
+            double s = A[(long)i * N + j];
+            for (int k = 0; k < j; k++) s -= A[(long)i * N + k] * A[(long)j * N + k];
+            A[(long)i * N + j] = s / ljj;
+        }
+    }
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) orthol[(long)i * N + j] = (i >= j) ? norm[i] * A[(long)i * N + j] : 0e0;
+    /* inverse of U = L^T by back substitution, column by column:
+       Uinv[r][c] for r <= c; lambdal[i][j] = Uinv[j][i] / norm[j]. */
+    double *Uinv = calloc((size_t)N * N, sizeof(double));
+    #pragma omp parallel for schedule(dynamic, 8)
+    for (int c = 0; c < N; c++) {
+        for (int r = c; r >= 0; r--) {
+            double s = (r == c) ? 1.0 : 0.0;
+            for (int k = r + 1; k <= c; k++) s -= A[(long)k * N + r] * Uinv[(long)k * N + c]; /* U[r][k] = L[k][r] */
+            Uinv[(long)r * N + c] = s / A[(long)r * N + r];
+        }
+    }
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) lambdal[(long)i * N + j] = Uinv[(long)j * N + i] / norm[j];
+    free(Uinv); free(norm); free(A);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Alpha solve (eigenmodetoday_mpi.c:148-162, 286-316):                       */
+/*   lambdainv = lower triangle of orthol; orthoinv = lambdal^T lambdal;      */
+/*   alpha = orthoinv beta; modesR_i = sum_j lambdainv[j][i] alpha_j.         */
+/* ------------------------------------------------------------------------ */
+int orc_alpha(int N, const double *orthol, const double *lambdal, const double *beta, double *alpha, double *modesR)
+{
+    double *orthoinv = malloc(sizeof(double) * (size_t)N * N);
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++) {
+            double s = 0.0;
+            for (int k = 0; k < N; k++) s += lambdal[(long)k * N + i] * lambdal[(long)k * N + j];
+            orthoinv[(long)i * N + j] = s;
+        }
+    for (int i = 0; i < N; i++) {
+        double s = 0.0;
+        for (int j = 0; j < N; j++) s += orthoinv[(long)i * N + j] * beta[j];
+        alpha[i] = s;
+    }
+    for (int i = 0; i < N; i++) {
+        double x = 0.0;
+        for (int j = 0; j < N; j++) x += (i <= j ? orthol[(long)j * N + i] : 0.0) * alpha[j];
+        modesR[i] = x;
+    }
+    free(orthoinv);
+    return 0;
+}

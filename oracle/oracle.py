@@ -1,0 +1,282 @@
+"""CPU oracle for the Modal-CMB mode-space hot path -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, and only as the checker or the timed CPU baseline; the product
+(libmodal_gb300.so) never calls it.
+
+Two CPU implementations are exposed:
+  * Oracle: the plain-C restatement in oracle/modal_oracle.c (builds anywhere);
+  * Ref:    the reference's own sources compiled in place with stand-in
+            headers (oracle/_ref/libmodalref.so, built by `make -C oracle ref`
+            when the reference checkout is present).
+The PCA branch of the orthogonalisation (gsl_eigen_symmv, absent here) is
+restated with numpy.linalg.eigh, following ortho_late_mpi.c:775-805.
+"""
+import contextlib
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libmodaloracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libmodalref.so")
+REFERENCE_DIR = "/root/reference"
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return ORACLE_SO
+
+
+def build_ref():
+    """Compile the reference's hot-path sources in place (needs the checkout)."""
+    if not os.path.isdir(REFERENCE_DIR):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REFERENCE_DIR], check=True)
+    return REF_SO
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+@contextlib.contextmanager
+def quiet_stdout():
+    """Silence C-level printf (the reference prints progress lines)."""
+    import sys
+    sys.stdout.flush()
+    fd = os.dup(1)
+    null = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(null, 1)
+    try:
+        yield
+    finally:
+        ctypes.CDLL(None).fflush(None)
+        os.dup2(fd, 1)
+        os.close(fd)
+        os.close(null)
+
+
+class Oracle:
+    """ctypes view of oracle/modal_oracle.c."""
+
+    def __init__(self, path=ORACLE_SO):
+        if not os.path.exists(path):
+            build_oracle()
+        L = ctypes.CDLL(path)
+        vp, i, l, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_double
+        for name, res, args in [
+            ("orc_gl_nodes", i, [i, vp, vp]),
+            ("orc_legendre_table", i, [i, i, vp, vp]),
+            ("orc_basis_legendre", i, [i, i, d, d, vp, vp]),
+            ("orc_mij", i, [i, i, i, i, vp, vp, vp]),
+            ("orc_orthol_pair", i, [i, i, vp, vp, vp, i, i, vp]),
+            ("orc_gamma", i, [i, vp, i, i, vp, vp, i, vp]),
+            ("orc_gamma_sample", l, [i, vp, i, i, vp, vp, i, l, vp]),
+            ("orc_geometric", d, [i, i, i]),
+            ("orc_permsix", d, [i, i, i]),
+            ("orc_tetrapyd_next", i, [i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
+            ("orc_tetrapyd_count", l, [i, i]),
+            ("orc_plijk", d, [vp, i, vp, i, i, i, i, i, i]),
+            ("orc_project", i, [i, i, i, vp, i, vp, vp, i, i, vp, d, d, d, d, i, l, vp]),
+            ("orc_ortho_cholesky", l, [i, vp, vp, vp]),
+            ("orc_alpha", i, [i, vp, vp, vp, vp, vp]),
+        ]:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        self.L = L
+
+    def gl_nodes(self, n):
+        x, w = np.empty(n), np.empty(n)
+        self.L.orc_gl_nodes(n, _p(x), _p(w))
+        return x, w
+
+    def legendre_table(self, mu, lmax):
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        out = np.empty((mu.size, lmax + 1))
+        self.L.orc_legendre_table(mu.size, lmax, _p(mu), _p(out))
+        return out
+
+    def basis_legendre(self, values, pmax, vmin, vmax):
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        out = np.empty((values.size, pmax + 1))
+        self.L.orc_basis_legendre(values.size, pmax, float(vmin), float(vmax), _p(values), _p(out))
+        return out
+
+    def mij(self, gl_pl, lmin, lmax, q):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        gl_pl = np.ascontiguousarray(gl_pl, dtype=np.float64)
+        P = q.shape[1]
+        out = np.empty((P, P, gl_pl.shape[0]))
+        self.L.orc_mij(gl_pl.shape[0], lmin, lmax, P, _p(gl_pl), _p(q), _p(out))
+        return out
+
+    def gamma(self, M, w, triples, nthreads=0):
+        triples = np.ascontiguousarray(triples, dtype=np.int32)
+        M = np.ascontiguousarray(M)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        N = triples.shape[0]
+        out = np.empty((N, N))
+        self.L.orc_gamma(N, _p(triples), M.shape[0], M.shape[2], _p(M), _p(w), nthreads, _p(out))
+        return out
+
+    def gamma_sample(self, M, w, triples, npairs, nthreads=0):
+        triples = np.ascontiguousarray(triples, dtype=np.int32)
+        out = np.empty(max(1, npairs))
+        n = self.L.orc_gamma_sample(triples.shape[0], _p(triples), M.shape[0], M.shape[2], _p(M), _p(w),
+                                    nthreads, npairs, _p(out))
+        return out[:n]
+
+    def orthol_pair(self, M, w, triples, m, n):
+        triples = np.ascontiguousarray(triples, dtype=np.int32)
+        r = np.zeros(4)
+        self.L.orc_orthol_pair(M.shape[0], M.shape[2], _p(M), _p(w), _p(triples), m, n, _p(r))
+        return r[0]
+
+    def geometric(self, i, j, k):
+        return self.L.orc_geometric(i, j, k)
+
+    def tetrapyd_count(self, lmin, lmax):
+        return self.L.orc_tetrapyd_count(lmin, lmax)
+
+    def project(self, lmin, lmax, q, triples, cl, shape, nthreads=0, max_points=0):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        triples = np.ascontiguousarray(triples, dtype=np.int32)
+        cl = np.ascontiguousarray(cl, dtype=np.float64)
+        N = triples.shape[0]
+        beta = np.empty(N)
+        if shape["kind"] == 0:
+            tab = np.ascontiguousarray(shape["tab"], dtype=np.float64)
+            args = (0, tab.shape[0], _p(tab), 0.0, 0.0, 0.0, 1.0)
+        else:
+            tab = None
+            c = shape["c"]
+            args = (1, 0, None, float(c[0]), float(c[1]), float(c[2]), float(shape["sigma"]))
+        self.L.orc_project(lmin, lmax, q.shape[1], _p(q), N, _p(triples), _p(cl), *args, nthreads, max_points,
+                           _p(beta))
+        return beta
+
+    def ortho_cholesky(self, gamma):
+        """Cholesky branch; returns (orthol, lambdal, fail) with fail = -1 or the failing pivot row."""
+        g = np.ascontiguousarray(gamma, dtype=np.float64)
+        N = g.shape[0]
+        o, lam = np.empty((N, N)), np.empty((N, N))
+        r = self.L.orc_ortho_cholesky(N, _p(g), _p(o), _p(lam))
+        return o, lam, (r - 1 if r > 0 else -1)
+
+    def alpha(self, orthol, lambdal, beta):
+        N = orthol.shape[0]
+        a, m = np.empty(N), np.empty(N)
+        self.L.orc_alpha(N, _p(np.ascontiguousarray(orthol)), _p(np.ascontiguousarray(lambdal)),
+                         _p(np.ascontiguousarray(beta, dtype=np.float64)), _p(a), _p(m))
+        return a, m
+
+
+def ortho_pca(gamma):
+    """PCA branch of ortho_late_mpi.c:775-805 with numpy.linalg.eigh standing
+    in for gsl_eigen_symmv (eigenvalues sorted descending).  Returns
+    (lambdainv, lambda, r)."""
+    norm = np.sqrt(np.diag(gamma))
+    gh = gamma / np.outer(norm, norm)
+    e, V = np.linalg.eigh(gh)
+    e, V = e[::-1], V[:, ::-1]
+    r = 0
+    for i in range(len(e)):
+        if e[i] > 0.0:
+            r = i + 1
+        else:
+            break
+    N = len(e)
+    lam = np.zeros((N, N))
+    inv = np.zeros((N, N))
+    lam[:r] = V[:, :r].T / (norm[None, :] * np.sqrt(e[:r])[:, None])
+    inv[:, :r] = norm[:, None] * V[:, :r] * np.sqrt(e[:r])[None, :]
+    return inv, lam, r
+
+
+class Ref:
+    """ctypes view of the reference compiled in place (oracle/_ref)."""
+
+    def __init__(self, path=REF_SO):
+        if not os.path.exists(path):
+            if build_ref() is None:
+                raise FileNotFoundError("reference checkout not present; oracle/_ref cannot be built")
+        L = ctypes.CDLL(path)
+        vp, i, l, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_long, ctypes.c_double
+        for name, res, args in [
+            ("ref_setup", i, [i, i, i, vp, i, vp, vp]),
+            ("ref_asy", i, [i, vp, vp]),
+            ("ref_legendre_Pl", d, [i, d]),
+            ("ref_basis_legendre", i, [i, i, d, d, vp, vp]),
+            ("ref_init_gamma", i, []),
+            ("ref_orthol_pair", i, [i, i, vp]),
+            ("ref_gamma", l, [i, l, vp]),
+            ("ref_geometric", d, [i, i, i]),
+            ("ref_plijk", d, [i, i, i, i]),
+            ("ref_tetrapyd_walk", l, [i, i, l, vp]),
+            ("ref_decompose", i, [i, i, i, vp]),
+            ("ref_project", i, [i, i, i, vp, d, d, d, d, l, vp]),
+        ]:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        self.L = L
+        self._keep = None
+
+    def setup(self, lmin, lmax, q, triples, cl):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        triples = np.ascontiguousarray(triples, dtype=np.int32)
+        cl = np.ascontiguousarray(cl, dtype=np.float64)
+        self.L.ref_setup(lmin, lmax, q.shape[1], _p(q), triples.shape[0], _p(triples), _p(cl))
+        self.N = triples.shape[0]
+
+    def asy(self, n):
+        x, w = np.empty(n), np.empty(n)
+        self.L.ref_asy(n, _p(x), _p(w))
+        return x, w
+
+    def basis_legendre(self, values, pmax, vmin, vmax):
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        out = np.empty((values.size, pmax + 1))
+        self.L.ref_basis_legendre(values.size, pmax, float(vmin), float(vmax), _p(values), _p(out))
+        return out
+
+    def init_gamma(self):
+        self.L.ref_init_gamma()
+
+    def orthol_pair(self, m, n):
+        r = np.zeros(4)
+        self.L.ref_orthol_pair(m, n, _p(r))
+        return r[0]
+
+    def gamma(self, nranks=8, npairs=0):
+        out = np.zeros((self.N, self.N))
+        n = self.L.ref_gamma(nranks, npairs, _p(out))
+        return out, n
+
+    def tetrapyd_walk(self, lmin, lmax, cap):
+        pts = np.zeros((cap + 1, 3), dtype=np.int32)
+        n = self.L.ref_tetrapyd_walk(lmin, lmax, cap, _p(pts))
+        return pts[:min(n, cap + 1)], n
+
+    def decompose(self, nthreads, lmin, lmax):
+        out = np.zeros((nthreads, 4), dtype=np.int32)
+        with quiet_stdout():
+            self.L.ref_decompose(nthreads, lmin, lmax, _p(out))
+        return out
+
+    def project(self, shape, nthreads=8, max_points=0):
+        beta = np.empty(self.N)
+        if shape["kind"] == 0:
+            tab = np.ascontiguousarray(shape["tab"], dtype=np.float64)
+            args = (0, tab.shape[0], _p(tab), 0.0, 0.0, 0.0, 1.0)
+        else:
+            tab = None
+            c = shape["c"]
+            args = (1, 0, None, float(c[0]), float(c[1]), float(c[2]), float(shape["sigma"]))
+        with quiet_stdout():
+            self.L.ref_project(nthreads, *args, max_points, _p(beta))
+        return beta

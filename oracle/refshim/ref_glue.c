@@ -1,0 +1,265 @@
+/* Glue for compiling the Modal-CMB reference's own hot-path sources in place
+ * (orthogonalisation_late.c, gl_integration.c, basis_functions.c,
+ * calculate_geometric.c, tetrapyd_tools.c, calculate_mode_3D.c,
+ * calculate_modes.c, arrays.c) into oracle/_ref/libmodalref.so.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file supplies what those sources expect
+ * from the rest of the reference (fixed_data.c accessors, parameter.c
+ * globals, GSL/MPI entry points) and exports a few driver functions that
+ * the tests call through ctypes to produce reference outputs.  Nothing in
+ * the product links or loads it.
+ *
+ * Stand-ins, each restating the behaviour the reference relies on:
+ *  - gsl_sf_legendre_Pl: GSL's upward three-term recurrence (GSL uses it for
+ *    l < 100000; P_2 in closed form).
+ *  - gsl_sf_bessel_J0/J1/Jn: the C library's j0/j1/jn.
+ *  - MPI: one rank; reductions copy.
+ *  - accessors get_basis_late_T / find_perm_late_TTT / get_cl_TT ... read the
+ *    tables passed to ref_setup (layouts of fixed_data.c:1764 basis_late_T
+ *    [Tsize][pmax+1] and order_late_TTT[n][3]).
+ *  - calculate_xint_TTT returns the synthetic shape for term 0 and 0 for the
+ *    rest, and get_eigen returns 1 for term 0, so calculate_3D_bispectrum
+ *    (calculate_mode_3D.c:266-281) evaluates exactly that shape.
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <omp.h>
+#include "mpi.h"
+#include "../shapes.h"
+
+/* ---- globals the reference declares extern (global.h:161-174) ---- */
+int eflag_T_lmax, eflag_T_lmin, eflag_E_lmax, eflag_E_lmin;
+int do_polarisation = 0;
+int model = 0;
+int l1, l2, l3, l4;
+int offload_target = 0;
+
+/* ---- reference functions compiled from the in-place sources ---- */
+extern int asy(double *nodes, double *weights, unsigned long n);
+extern double init_orthol_glint(void);
+extern void calculate_orthoMij_T(int i, int j);
+extern void sync_orthoMij(void);
+extern int calculate_orthol(int m, int n, double *result);
+extern double plijk_TTT(int r, int i, int j, int k);
+extern double calculate_geometric(int i, int j, int k);
+extern int basis_functions_legendre(double **array, int size, int pmax, double min, double max, double *values);
+extern double **create_array(int dim_x, int dim_y);
+extern int get_ijk_next_XXX(int lmax, int *i, int *j, int *k);
+extern void check_ijk_min_XXX(int lmin, int *i, int *j, int *k);
+
+typedef struct { int i_bgn, j_bgn, k_bgn, loops; } ref_tetrapyd_limits; /* tetrapyd_tools.h:333-339 */
+extern void decompose_tetrapyd_XXX(ref_tetrapyd_limits *block, int rank, int nranks, int nthreads, int lmin, int lmax);
+extern void init_3D(int mode);
+extern void calculate_mode_3D(int min, int max, ref_tetrapyd_limits *block, double *alpha);
+
+/* ---- state behind the accessors ---- */
+static int g_P, g_N, g_L;
+static double *g_basis;   /* [L][P] */
+static int *g_triples;    /* [N][3] */
+static double *g_cl;      /* [lmax+1], C_l + N_l/b_l^2 */
+static orc_shape g_shape;
+
+/* ---- MPI, one rank ---- */
+int MPI_Init(int *argc, char ***argv) { (void)argc; (void)argv; return 0; }
+int MPI_Finalize(void) { return 0; }
+int MPI_Comm_rank(MPI_Comm c, int *rank) { (void)c; *rank = 0; return 0; }
+int MPI_Comm_size(MPI_Comm c, int *size) { (void)c; *size = 1; return 0; }
+int MPI_Barrier(MPI_Comm c) { (void)c; return 0; }
+static size_t mpi_bytes(MPI_Datatype t) { return t == MPI_INT ? sizeof(int) : (t == MPI_LONG ? sizeof(long) : sizeof(double)); }
+int MPI_Allreduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op op, MPI_Comm c)
+{ (void)op; (void)c; memmove(r, s, (size_t)n * mpi_bytes(t)); return 0; }
+int MPI_Reduce(const void *s, void *r, int n, MPI_Datatype t, MPI_Op op, int root, MPI_Comm c)
+{ (void)op; (void)root; (void)c; memmove(r, s, (size_t)n * mpi_bytes(t)); return 0; }
+
+/* ---- GSL stand-ins ---- */
+double gsl_sf_bessel_J0(double x) { return j0(x); }
+double gsl_sf_bessel_J1(double x) { return j1(x); }
+double gsl_sf_bessel_Jn(int n, double x) { return jn(n, x); }
+struct refshim_glfixed { int unused; };
+struct refshim_glfixed *gsl_integration_glfixed_table_alloc(size_t n) { (void)n; return NULL; }
+void gsl_integration_glfixed_table_free(struct refshim_glfixed *t) { (void)t; }
+double gsl_sf_legendre_Pl(int l, double x)
+{
+    if (l == 0) return 1.0;
+    if (l == 1) return x;
+    if (l == 2) return 0.5 * (3.0 * x * x - 1.0);
+    if (x == 1.0) return 1.0;
+    if (x == -1.0) return (l & 1) ? -1.0 : 1.0;
+    double pm2 = 1.0, pm1 = x, p = x;
+    for (int ell = 2; ell <= l; ell++) {
+        p = (x * (2 * ell - 1) * pm1 - (ell - 1) * pm2) / ell;
+        pm2 = pm1;
+        pm1 = p;
+    }
+    return p;
+}
+
+/* ---- fixed_data.c accessors ---- */
+int get_pmax_late_T(void) { return g_P - 1; }
+int get_pmax_late_E(void) { return g_P - 1; }
+double get_basis_late_T(int i, int j) { return g_basis[(long)i * g_P + j]; }
+double get_basis_late_E(int i, int j) { return g_basis[(long)i * g_P + j]; }
+static void perm_of(int r, int *p1, int *p2, int *p3) { *p1 = g_triples[3 * r]; *p2 = g_triples[3 * r + 1]; *p3 = g_triples[3 * r + 2]; }
+void find_perm_late_TTT(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
+void find_perm_late_TTE(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
+void find_perm_late_TEE(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
+void find_perm_late_EEE(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
+int get_terms_late(void) { return g_N; }
+int get_terms_prim(void) { return g_N; }
+int get_lmax(void) { return eflag_T_lmax; }
+double get_tau0(void) { return 0.0; }
+int get_qtilde_xsize(void) { return 1; }
+int get_qtilde_xvec(double *v) { v[0] = 0.0; return 0; }
+int read_eigen(int a, int b, int c) { (void)a; (void)b; (void)c; return 0; }
+double get_eigen(int i) { return i == 0 ? 1.0 : 0.0; }
+double get_cl_TT(int l) { return g_cl[l]; }
+double get_noise_TT(int l) { (void)l; return 0.0; }
+double get_beam_TT(int l) { (void)l; return 1.0; }
+double calculate_ISW_bispectrum(int i, int j, int k) { (void)i; (void)j; (void)k; return 0.0; }
+double calculate_xint_TTT(int a, int b, int c, int n, int xsize, double *xvec)
+{ (void)xsize; (void)xvec; return n == 0 ? orc_shape_eval(&g_shape, a, b, c) : 0.0; }
+double permsix(int i, int j, int k)
+{ if (i == j && j == k) return 1.0; if (i == j || j == k || i == k) return 3.0; return 6.0; }
+int sync_tasks(int mode, int size) { (void)mode; (void)size; return 0; }
+double get_orthol_TTT(int i, int j) { (void)i; (void)j; return 0.0; }
+double get_lambdal_TTT(int i, int j) { (void)i; (void)j; return 0.0; }
+double get_lambdal_TTE(int i, int j) { (void)i; (void)j; return 0.0; }
+double get_lambdal_TEE(int i, int j) { (void)i; (void)j; return 0.0; }
+double get_lambdal_EEE(int i, int j) { (void)i; (void)j; return 0.0; }
+double get_modes_TTT(int i) { (void)i; return 0.0; }
+double get_modes_TTE(int i) { (void)i; return 0.0; }
+double get_modes_TEE(int i) { (void)i; return 0.0; }
+double get_modes_EEE(int i) { (void)i; return 0.0; }
+double get_modesR_TTT(int i) { (void)i; return 0.0; }
+
+/* ===================== exported drivers (ctypes) ===================== */
+
+/* Install the basis q[L][P] (basis_late_T layout), the mode triples [N][3]
+ * (order_late_TTT layout) and the total spectrum cl[lmax+1]. */
+int ref_setup(int lmin, int lmax, int P, const double *basis, int N, const int *triples, const double *cl)
+{
+    g_P = P; g_N = N; g_L = lmax - lmin + 1;
+    eflag_T_lmin = eflag_E_lmin = lmin;
+    eflag_T_lmax = eflag_E_lmax = lmax;
+    free(g_basis); free(g_triples); free(g_cl);
+    g_basis = malloc(sizeof(double) * (size_t)g_L * P);
+    g_triples = malloc(sizeof(int) * 3 * (size_t)N);
+    g_cl = malloc(sizeof(double) * (size_t)(lmax + 1));
+    memcpy(g_basis, basis, sizeof(double) * (size_t)g_L * P);
+    memcpy(g_triples, triples, sizeof(int) * 3 * (size_t)N);
+    memcpy(g_cl, cl, sizeof(double) * (size_t)(lmax + 1));
+    return 0;
+}
+
+int ref_asy(int n, double *nodes, double *weights) { return asy(nodes, weights, (unsigned long)n); }
+
+double ref_legendre_Pl(int l, double x) { return gsl_sf_legendre_Pl(l, x); }
+
+int ref_basis_legendre(int size, int pmax, double min, double max, const double *values, double *out)
+{
+    double **a = create_array(size, pmax + 1);
+    basis_functions_legendre(a, size, pmax, min, max, (double *)values);
+    for (int i = 0; i < size; i++) memcpy(out + (long)i * (pmax + 1), a[i], sizeof(double) * (pmax + 1));
+    free(a[0]); free(a);
+    return 0;
+}
+
+/* init_orthol_glint + calculate_orthoMij_T over all P^2 (i,j) pairs + sync,
+ * the sequence of ortho_late_mpi.c:170-229 on one rank. */
+int ref_init_gamma(void)
+{
+    init_orthol_glint();
+    for (int i = 0; i < g_P; i++)
+        for (int j = 0; j < g_P; j++) calculate_orthoMij_T(i, j);
+    sync_orthoMij();
+    return 0;
+}
+
+int ref_orthol_pair(int m, int n, double *result) { return calculate_orthol(m, n, result); }
+
+/* Gamma over the upper triangle, pairs split over `nranks` single-threaded
+ * workers exactly as ortho_late_mpi.c:242-266 splits them over MPI ranks
+ * (the per-pair OpenMP region inside calculate_orthol runs one thread).
+ * `npairs_limit` > 0 stops after that many pairs (bounded timing sample).
+ * Writes the full symmetric matrix out[N][N] (ortho_late_mpi.c:344-363). */
+long ref_gamma(int nranks, long npairs_limit, double *out)
+{
+    const int N = g_N;
+    const long total = (long)N * (N + 1) / 2;
+    const long todo = (npairs_limit > 0 && npairs_limit < total) ? npairs_limit : total;
+    int *pi = malloc(sizeof(int) * (size_t)total), *pj = malloc(sizeof(int) * (size_t)total);
+    long n = 0;
+    for (int i = 0; i < N; i++)
+        for (int j = i; j < N; j++) { pi[n] = i; pj[n] = j; n++; }
+    omp_set_max_active_levels(1);
+    #pragma omp parallel num_threads(nranks)
+    {
+        const int rank = omp_get_thread_num(), nproc = omp_get_num_threads();
+        long loops = todo / nproc, aux = todo % nproc;
+        long start = rank * loops, end = (rank + 1) * loops - 1;
+        if (aux) {
+            if (rank < aux) { start += rank; end += rank + 1; }
+            else { start += aux; end += aux; }
+        }
+        double r[4];
+        for (long p = start; p <= end; p++) {
+            calculate_orthol(pi[p], pj[p], r);
+            out[(long)pi[p] * N + pj[p]] = r[0];
+            out[(long)pj[p] * N + pi[p]] = r[0];
+        }
+    }
+    free(pi); free(pj);
+    return todo;
+}
+
+double ref_geometric(int i, int j, int k) { return calculate_geometric(i, j, k); }
+double ref_plijk(int r, int i, int j, int k) { return plijk_TTT(r, i, j, k); }
+
+/* Walk the tetrapyd with get_ijk_next_XXX from the start given by
+ * check_ijk_min_XXX; writes up to `cap` points (i,j,k) and returns the count
+ * decompose_tetrapyd_XXX would assign in total. */
+long ref_tetrapyd_walk(int lmin, int lmax, long cap, int *pts)
+{
+    int i = lmin, j = lmin, k = lmin;
+    check_ijk_min_XXX(lmin, &i, &j, &k);
+    long count = 0;
+    for (;;) {
+        if (count < cap) { pts[3 * count] = i; pts[3 * count + 1] = j; pts[3 * count + 2] = k; }
+        count++;
+        if (!get_ijk_next_XXX(lmax, &i, &j, &k)) break;
+    }
+    if (count < cap) { pts[3 * count] = i; pts[3 * count + 1] = j; pts[3 * count + 2] = k; }
+    return count + 1;
+}
+
+int ref_decompose(int nthreads, int lmin, int lmax, int *out /*[nthreads][4]*/)
+{
+    ref_tetrapyd_limits *b = malloc(sizeof(*b) * (size_t)nthreads);
+    decompose_tetrapyd_XXX(b, 0, 1, nthreads, lmin, lmax);
+    for (int t = 0; t < nthreads; t++) { out[4 * t] = b[t].i_bgn; out[4 * t + 1] = b[t].j_bgn; out[4 * t + 2] = b[t].k_bgn; out[4 * t + 3] = b[t].loops; }
+    free(b);
+    return 0;
+}
+
+/* calculate_mode_3D (calculate_mode_3D.c:217-264) for one shape with the
+ * eigenmodetoday_mpi.c:235-261 set-up (init_3D, decompose_tetrapyd_XXX over
+ * `nthreads` OpenMP threads).  shape: kind/nterms/tab/c/sigma as in shapes.h.
+ * `max_points` > 0 limits every thread's block to its first points
+ * (bounded timing sample).  beta[N] out. */
+int ref_project(int nthreads, int kind, int nterms, const double *tab, double c1, double c2, double c3,
+                double sigma, long max_points, double *beta)
+{
+    g_shape.kind = kind; g_shape.nterms = nterms; g_shape.lmax = eflag_T_lmax; g_shape.tab = tab;
+    g_shape.c1 = c1; g_shape.c2 = c2; g_shape.c3 = c3; g_shape.sigma = sigma;
+    omp_set_num_threads(nthreads);
+    omp_set_max_active_levels(1);
+    ref_tetrapyd_limits *b = malloc(sizeof(*b) * (size_t)nthreads);
+    decompose_tetrapyd_XXX(b, 0, 1, nthreads, eflag_T_lmin, eflag_T_lmax);
+    if (max_points > 0)
+        for (int t = 0; t < nthreads; t++) if (b[t].loops > max_points) b[t].loops = (int)max_points;
+    init_3D(1001);
+    calculate_mode_3D(eflag_T_lmin, eflag_T_lmax, b, beta);
+    free(b);
+    return 0;
+}

@@ -1,0 +1,71 @@
+"""Generate the golden vectors under tests/golden/ from the Modal-CMB
+reference's own sources, compiled in place (oracle/_ref, `make -C oracle ref`).
+
+Run in a container that has the reference checkout:
+    python tests/golden/make_golden.py
+The fixtures are small .npz files; tests read them without the reference.
+Inputs are rebuilt by the tests from modal_gb300's synthetic-workload
+builders with the same arguments, and their checksums are stored alongside.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "modal-cmb_gb300"))
+import modal_gb300 as M  # noqa: E402
+import oracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def inputs_digest(q, tr, cl):
+    return np.array([q.sum(), (q * q).sum(), tr.sum(), cl.sum()])
+
+
+def main():
+    ref = O.Ref()
+    # 1. asy() Gauss-Legendre nodes/weights
+    gl = {}
+    for n in (31, 91, 751, 1501, 3001):
+        x, w = ref.asy(n)
+        gl[f"x{n}"], gl[f"w{n}"] = x, w
+    np.savez_compressed(os.path.join(OUT, "gl_asy.npz"), **gl)
+
+    # 2. basis_functions_legendre for config 1's basis (l = 2..500, pmax = 9)
+    vals = np.arange(2, 501, dtype=np.float64)
+    np.savez_compressed(os.path.join(OUT, "basis_legendre.npz"), values=vals,
+                        basis=ref.basis_legendre(vals, 9, 2.0, 500.0))
+
+    # 3. calculate_geometric at seeded tetrapyd points and off-tetrapyd points
+    rng = np.random.default_rng(7)
+    pts = rng.integers(0, 2500, size=(2000, 3)).astype(np.int32)
+    geo = np.array([ref.L.ref_geometric(int(a), int(b), int(c)) for a, b, c in pts])
+    np.savez_compressed(os.path.join(OUT, "geometric.npz"), pts=pts, geo=geo)
+
+    # 4. tetrapyd walk / decomposition
+    walk, n = ref.tetrapyd_walk(2, 30, 400)
+    counts = {f"{a}_{b}": ref.tetrapyd_walk(a, b, 0)[1] for a, b in [(2, 3), (2, 10), (3, 31), (2, 100), (5, 64)]}
+    dec = ref.decompose(8, 2, 100)
+    np.savez_compressed(os.path.join(OUT, "tetrapyd.npz"), walk=walk[:400], walk_count=n, decompose=dec,
+                        **{"count_" + k: v for k, v in counts.items()})
+
+    # 5. Gamma (calculate_orthol over all pairs) and projection beta
+    #    small: lmax=60, P=4; config 1: lmax=500, P=10 (220 modes)
+    for name, lmax, P, S in [("small", 60, 4, 4), ("cfg1", 500, 10, 4)]:
+        q, tr, cl = M.workload(lmax, P)
+        ref.setup(2, lmax, q, tr, cl)
+        with O.quiet_stdout():
+            ref.init_gamma()
+        G, _ = ref.gamma(nranks=8)
+        shapes = M.separable_shapes(lmax, S // 2, seed=0) + M.bump_shapes(S - S // 2, seed=1)
+        beta = np.stack([ref.project(s, nthreads=8) for s in shapes])
+        np.savez_compressed(os.path.join(OUT, f"gamma_{name}.npz"), gamma=G, beta=beta, lmax=lmax, P=P, S=S,
+                            digest=inputs_digest(q, tr, cl))
+        print(name, "done", G.shape, beta.shape)
+
+
+if __name__ == "__main__":
+    main()

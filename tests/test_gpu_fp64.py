@@ -1,0 +1,291 @@
+"""GPU parity of the plain FP64 form against the oracle and the golden vectors
+of the reference (tolerances written per test).  Every call goes through the
+C ABI of libmodal_gb300.so."""
+import numpy as np
+import pytest
+from conftest import rel_fro, rel_max
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(mg):
+    c = mg.Context(0)
+    yield c
+    c.close()
+
+
+# ---------------------------------------------------------------- primitives
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 91, 751, 3001, 3751])
+def test_gl_nodes_vs_oracle(mg, orc, n):
+    x, w = mg.gl_nodes(n)
+    xo, wo = orc.gl_nodes(n)
+    assert np.max(np.abs(x - xo)) <= 5e-16
+    assert np.max(np.abs(w - wo) / wo) <= 1e-13  # FP64 recurrence vs long double
+
+
+@pytest.mark.parametrize("n", [751, 1501, 3001])
+def test_gl_nodes_vs_reference_asy(mg, golden, n):
+    g = golden("gl_asy")
+    x, w = mg.gl_nodes(n)
+    assert np.max(np.abs(x - g[f"x{n}"])) <= 5e-16
+    assert np.max(np.abs(w - g[f"w{n}"]) / g[f"w{n}"]) <= 1e-13
+
+
+def test_legendre_table_vs_oracle(mg, orc, golden):
+    x = golden("gl_asy")["x751"]
+    t = mg.legendre_table(x, 500)
+    to = orc.legendre_table(x, 500)
+    assert rel_max(t, to) <= 1e-13
+    # edge nodes +-1 and 0 take the exact branches
+    e = np.array([-1.0, 0.0, 1.0])
+    assert np.max(np.abs(mg.legendre_table(e, 50) - orc.legendre_table(e, 50))) <= 1e-12
+
+
+def test_basis_legendre_vs_reference(mg, golden):
+    g = golden("basis_legendre")
+    b = mg.basis_legendre(g["values"], 9, 2.0, 500.0)
+    assert np.max(np.abs(b - g["basis"])) <= 1e-14
+
+
+def test_geometric_vs_reference(mg, golden):
+    g = golden("geometric")
+    v = mg.geometric(g["pts"])
+    nz = g["geo"] != 0
+    assert np.array_equal(v == 0, g["geo"] == 0)
+    assert np.max(np.abs(v[nz] - g["geo"][nz]) / g["geo"][nz]) <= 1e-14
+
+
+# --------------------------------------------------------------------- Gamma
+
+@pytest.mark.parametrize("name", ["small", "cfg1"])
+def test_gamma_vs_reference_with_reference_nodes(mg, golden, ctx, name):
+    """Bit-level parity target 1e-12: same inputs and the reference's own asy()
+    nodes, Gamma vs calculate_orthol over all pairs."""
+    g = golden("gamma_" + name)
+    lmax, P = int(g["lmax"]), int(g["P"])
+    q, tr, cl = mg.workload(lmax, P)
+    nmu = 3 * lmax // 2 + 1
+    gl = golden("gl_asy")
+    ctx.set_basis(2, lmax, q)
+    ctx.set_modes(tr)
+    ctx.set_gl(gl[f"x{nmu}"], gl[f"w{nmu}"])
+    G = ctx.gamma(mg.PREC_FP64)
+    assert rel_fro(G, g["gamma"]) <= 1e-12
+    assert rel_max(G, g["gamma"]) <= 1e-12
+    assert np.array_equal(G, G.T)
+    # per-pair interface (calculate_orthol)
+    for m, n in [(0, 0), (1, 7), (len(tr) - 1, 3)]:
+        assert abs(ctx.orthol_pair(m, n) - g["gamma"][m, n]) <= 1e-12 * np.abs(g["gamma"]).max()
+
+
+def test_mij_vs_oracle(mg, orc, golden, ctx):
+    lmax, P = 500, 10
+    q, tr, cl = mg.workload(lmax, P)
+    gl = golden("gl_asy")
+    ctx.set_basis(2, lmax, q)
+    ctx.set_modes(tr)
+    ctx.set_gl(gl["x751"], gl["w751"])
+    ctx.init_glint()
+    M = ctx.get_mij()
+    Mo = orc.mij(orc.legendre_table(gl["x751"], lmax), 2, lmax, q)
+    assert M.shape == Mo.shape
+    assert rel_max(M, Mo) <= 1e-12
+    x, w = ctx.get_gl()
+    assert np.array_equal(x, gl["x751"]) and np.array_equal(w, gl["w751"])
+
+
+def test_gamma_own_nodes_vs_oracle(mg, orc, ctx):
+    lmax, P = 300, 7
+    q, tr, cl = mg.workload(lmax, P)
+    ctx.set_basis(2, lmax, q)
+    ctx.set_modes(tr)
+    ctx2 = mg.Context(0)
+    ctx2.set_basis(2, lmax, q)
+    ctx2.set_modes(tr)
+    G = ctx2.gamma(mg.PREC_FP64)
+    ctx2.close()
+    x, w = orc.gl_nodes(3 * lmax // 2 + 1)
+    Go = orc.gamma(orc.mij(orc.legendre_table(x, lmax), 2, lmax, q), w, tr)
+    assert rel_fro(G, Go) <= 1e-12
+
+
+@pytest.mark.parametrize("P,modes", [(1, [[0, 0, 0]]), (3, [[2, 1, 0], [0, 0, 0], [1, 1, 1], [2, 1, 0]]),
+                                     (5, None)])
+def test_gamma_edge_cases(mg, orc, P, modes):
+    """N = 1, unsorted and duplicated triples, N not a multiple of the tile."""
+    lmax = 40
+    q, tr, cl = mg.workload(lmax, P)
+    tr = np.array(modes, dtype=np.int32) if modes is not None else tr
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        G = c.gamma(mg.PREC_FP64)
+    x, w = orc.gl_nodes(3 * lmax // 2 + 1)
+    Go = orc.gamma(orc.mij(orc.legendre_table(x, lmax), 2, lmax, q), w, tr)
+    assert rel_max(G, Go) <= 1e-12
+
+
+def test_bad_arguments_are_rejected(mg):
+    with mg.Context(0) as c:
+        with pytest.raises(mg.ModalError) as e:
+            c.gamma()
+        assert e.value.status == 6
+        q, tr, cl = mg.workload(40, 3)
+        c.set_basis(2, 40, q)
+        with pytest.raises(mg.ModalError) as e:
+            c.set_modes(np.array([[0, 1, 3]]))
+        assert e.value.status == 1
+        with pytest.raises(mg.ModalError):
+            c.set_basis(2, 40, np.zeros((39, 65)))
+
+
+# ---------------------------------------------------------- orthogonalisation
+
+def _spd_gamma(mg, golden):
+    g = golden("gamma_small")
+    return g["gamma"]
+
+
+def test_cholesky_branch_vs_oracle(mg, orc, golden):
+    G = _spd_gamma(mg, golden)
+    N = G.shape[0]
+    o_ref, lam_ref, fail = orc.ortho_cholesky(G)
+    assert fail == -1
+    with mg.Context(0) as c:
+        q, tr, cl = mg.workload(60, 4)
+        c.set_basis(2, 60, q)
+        c.set_modes(tr)
+        o, lam, branch, rank = c.orthogonalise(G, pca_flag=1)
+    assert branch == 0 and rank == N
+    assert rel_max(o, o_ref) <= 1e-10
+    assert rel_max(lam, lam_ref) <= 1e-8
+    assert np.array_equal(np.triu(o, 1), np.zeros((N, N))) and np.array_equal(np.triu(lam, 1), np.zeros((N, N)))
+    assert rel_max(o @ o.T, G) <= 1e-12  # backward error
+
+
+def test_cholesky_blocked_large_spd(mg, orc):
+    """Several 64-wide panels, N not a multiple of 64."""
+    rng = np.random.default_rng(11)
+    N = 301
+    A = rng.standard_normal((N, N))
+    G = A @ A.T + N * np.eye(N)
+    o_ref, lam_ref, _ = orc.ortho_cholesky(G)
+    with mg.Context(0) as c:
+        q, _, _ = mg.workload(60, 13)
+        c.set_basis(2, 60, q)
+        c.set_modes(mg.mode_triples(13)[:N])
+        o, lam, branch, rank = c.orthogonalise(G, pca_flag=1)
+    assert branch == 0
+    assert rel_max(o, o_ref) <= 1e-12
+    assert rel_max(lam, lam_ref) <= 1e-11
+    assert np.max(np.abs(lam @ o - np.eye(N))) <= 1e-11
+
+
+def test_pca_branch_forced_and_on_failure(mg):
+    import oracle
+    rng = np.random.default_rng(12)
+    N = 150
+    A = rng.standard_normal((N, 40))
+    G_def = A @ A.T  # rank 40: not positive definite
+    with mg.Context(0) as c:
+        q, _, _ = mg.workload(60, 10)
+        c.set_basis(2, 60, q)
+        c.set_modes(mg.mode_triples(10)[:N])
+        for G, flag in [(A @ A.T + np.eye(N), 0), (G_def, 1)]:
+            o, lam, branch, rank = c.orthogonalise(G, pca_flag=flag)
+            inv_ref, lam_ref, r_ref = oracle.ortho_pca(G)
+            assert branch == 1
+            if flag == 0:
+                assert rank == r_ref == N
+            else:  # 40 true positive eigenvalues, the rest at round-off level with either sign
+                assert rank >= 40 and r_ref >= 40
+            r = min(rank, r_ref, 40 if flag == 1 else N)
+            # rows of lambda equal up to the sign of each eigenvector (well separated part)
+            for i in range(min(r, 30)):
+                s = np.sign(np.dot(lam[i], lam_ref[i]))
+                assert np.max(np.abs(lam[i] - s * lam_ref[i])) <= 1e-8 * np.max(np.abs(lam_ref[i]))
+            assert np.all(lam[rank:] == 0) and np.all(o[:, rank:] == 0)
+
+
+# ---------------------------------------------------------------- projection
+
+@pytest.mark.parametrize("name", ["small", "cfg1"])
+def test_projection_vs_reference(mg, golden, name):
+    g = golden("gamma_" + name)
+    lmax, P, S = int(g["lmax"]), int(g["P"]), int(g["S"])
+    q, tr, cl = mg.workload(lmax, P)
+    shapes = mg.separable_shapes(lmax, S // 2, seed=0) + mg.bump_shapes(S - S // 2, seed=1)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        beta = c.project(shapes, mg.PREC_FP64)
+        for s in range(S):
+            assert rel_fro(beta[s], g["beta"][s]) <= 1e-12
+        # one shape at a time gives the same as the batch
+        b1 = c.project(shapes[1:2], mg.PREC_FP64)
+        assert rel_fro(b1[0], beta[1]) <= 1e-14
+
+
+@pytest.mark.parametrize("lmin,lmax,P", [(2, 3, 2), (2, 33, 3), (5, 64, 4), (7, 40, 1)])
+def test_projection_edge_sizes_vs_oracle(mg, orc, lmin, lmax, P):
+    cl = mg.synthetic_cl(lmax)
+    q = mg.weighted_q(mg.legendre_q(lmin, lmax, P), cl, lmin)
+    tr = mg.mode_triples(P)
+    shapes = mg.separable_shapes(lmax, 1, seed=3) + mg.bump_shapes(1, seed=4)
+    with mg.Context(0) as c:
+        c.set_basis(lmin, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        beta = c.project(shapes)
+    for s, sh in enumerate(shapes):
+        bo = orc.project(lmin, lmax, q, tr, cl, sh, nthreads=2)
+        assert rel_fro(beta[s], bo) <= 1e-12
+
+
+# --------------------------------------------------------------------- alpha
+
+def test_alpha_vs_oracle(mg, orc, golden):
+    g = golden("gamma_small")
+    G, beta = g["gamma"], g["beta"]
+    o_ref, lam_ref, _ = orc.ortho_cholesky(G)
+    with mg.Context(0) as c:
+        q, tr, cl = mg.workload(60, 4)
+        c.set_basis(2, 60, q)
+        c.set_modes(tr)
+        c.orthogonalise(G, pca_flag=1, download=False)
+        a, mR = c.alpha(beta.shape[0], beta)
+    for s in range(beta.shape[0]):
+        a_ref, m_ref = orc.alpha(o_ref, lam_ref, beta[s])
+        assert rel_fro(a[s], a_ref) <= 1e-8
+        assert rel_fro(mR[s], m_ref) <= 1e-8
+        # gamma-norm error of the reconstruction
+        d = a[s] - a_ref
+        assert np.sqrt(abs(d @ G @ d)) <= 1e-8 * np.sqrt(a_ref @ G @ a_ref)
+
+
+def test_full_pipeline_on_device(mg, golden):
+    """Gamma -> orthogonalise -> project -> alpha with everything left on the device."""
+    g = golden("gamma_small")
+    lmax, P, S = 60, 4, 4
+    q, tr, cl = mg.workload(lmax, P)
+    shapes = mg.separable_shapes(lmax, 2, seed=0) + mg.bump_shapes(2, seed=1)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        gl = golden("gl_asy")
+        c.set_gl(gl["x91"], gl["w91"])
+        c.gamma(mg.PREC_FP64, download=False)
+        c.orthogonalise(None, download=False)
+        c.project(shapes, download=False)
+        a, mR = c.alpha(S)
+        n0 = c.launches
+    G = g["gamma"]
+    for s in range(S):
+        ref = np.linalg.solve(G, g["beta"][s])
+        d = a[s] - ref
+        assert np.sqrt(abs(d @ G @ d)) <= 1e-8 * np.sqrt(abs(ref @ G @ ref))
+    assert n0 > 10

@@ -1,0 +1,167 @@
+"""The CPU oracle pinned against golden vectors produced by the reference's own
+sources compiled in place (tests/golden/make_golden.py), and against
+mathematical known answers."""
+import numpy as np
+import pytest
+from conftest import rel_fro, rel_max
+
+
+@pytest.mark.parametrize("n", [751, 1501, 3001])
+def test_gl_nodes_match_reference_asy(orc, golden, n):
+    g = golden("gl_asy")
+    x, w = orc.gl_nodes(n)
+    assert np.max(np.abs(x - g[f"x{n}"])) <= 2e-16
+    assert np.max(np.abs(w - g[f"w{n}"]) / g[f"w{n}"]) <= 5e-15
+
+
+def test_gl_reference_asy_is_approximate_at_small_n(orc, golden):
+    # asy() uses large-n asymptotic expansions; at n = 31 its weights are off
+    # by ~2e-10 and its rule no longer integrates x^60 exactly.  The oracle is.
+    g = golden("gl_asy")
+    x, w = orc.gl_nodes(31)
+    assert np.max(np.abs(w - g["w31"]) / w) < 1e-9
+    exact = 2.0 / 61.0
+    assert abs(np.sum(w * x ** 60) - exact) / exact < 1e-13
+    assert abs(np.sum(g["w31"] * g["x31"] ** 60) - exact) / exact > 1e-12
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 31, 91, 751])
+def test_gl_nodes_exactness(orc, n):
+    x, w = orc.gl_nodes(n)
+    assert np.all(np.diff(x) > 0)
+    assert np.allclose(x, -x[::-1], atol=0, rtol=0) or np.max(np.abs(x + x[::-1])) < 1e-16
+    for m in range(0, n):  # exact for degree <= 2n-1
+        exact = 2.0 / (2 * m + 1)
+        assert abs(np.sum(w * x ** (2 * m)) - exact) <= 1e-13 * exact + 1e-16
+
+
+def test_legendre_table_matches_scipy(orc):
+    from scipy.special import eval_legendre
+    mu = np.linspace(-1, 1, 41)
+    t = orc.legendre_table(mu, 300)
+    l = np.arange(301)
+    ref = (2 * l + 1) ** (2 / 3) * eval_legendre(l[None, :], mu[:, None])
+    assert np.max(np.abs(t - ref)) / np.max(np.abs(ref)) < 1e-12
+
+
+def test_basis_legendre_matches_reference(orc, golden):
+    g = golden("basis_legendre")
+    b = orc.basis_legendre(g["values"], 9, 2.0, 500.0)
+    assert np.max(np.abs(b - g["basis"])) <= 1e-14
+
+
+def test_geometric_matches_reference(orc, golden):
+    g = golden("geometric")
+    v = np.array([orc.geometric(int(a), int(b), int(c)) for a, b, c in g["pts"]])
+    nz = g["geo"] != 0
+    assert np.array_equal(v == 0, g["geo"] == 0)
+    assert np.max(np.abs(v[nz] - g["geo"][nz]) / g["geo"][nz]) < 1e-14
+
+
+def _walk(orc, lmin, lmax, n):
+    import ctypes
+    i, j, k = ctypes.c_int(lmin), ctypes.c_int(lmin), ctypes.c_int(lmin)
+    # start as check_ijk_min_XXX: (lmin, lmin, lmin + parity)
+    if (3 * lmin) % 2 == 1:
+        k.value += 1
+    pts = []
+    for _ in range(n):
+        pts.append((i.value, j.value, k.value))
+        if not orc.L.orc_tetrapyd_next(lmax, ctypes.byref(i), ctypes.byref(j), ctypes.byref(k)):
+            pts.append((i.value, j.value, k.value))
+            break
+    return np.array(pts[:n])
+
+
+def test_tetrapyd_walk_and_counts(orc, golden):
+    g = golden("tetrapyd")
+    w = _walk(orc, 2, 30, 400)
+    assert np.array_equal(w, g["walk"][:len(w)])
+    for key in g.files:
+        if key.startswith("count_"):
+            a, b = map(int, key[6:].split("_"))
+            assert orc.tetrapyd_count(a, b) == int(g[key])
+
+
+def test_tetrapyd_walk_is_the_even_triangle_set(orc):
+    lmin, lmax = 3, 40
+    n = orc.tetrapyd_count(lmin, lmax)
+    w = _walk(orc, lmin, lmax, n)
+    enum = {(i, j, k) for i in range(lmin, lmax + 1) for j in range(i, lmax + 1)
+            for k in range(j, min(i + j, lmax) + 1) if (i + j + k) % 2 == 0}
+    assert len(w) == n == len(enum)
+    assert set(map(tuple, w.tolist())) == enum
+
+
+@pytest.mark.parametrize("name", ["small", "cfg1"])
+def test_gamma_matches_reference(orc, golden, mg, name):
+    g = golden("gamma_" + name)
+    gl = golden("gl_asy")
+    lmax, P = int(g["lmax"]), int(g["P"])
+    q, tr, cl = mg.workload(lmax, P)
+    nmu = 3 * lmax // 2 + 1
+    x, w = gl[f"x{nmu}"], gl[f"w{nmu}"]
+    M = orc.mij(orc.legendre_table(x, lmax), 2, lmax, q)
+    G = orc.gamma(M, w, tr)
+    assert rel_fro(G, g["gamma"]) <= 1e-13
+    assert rel_max(G, g["gamma"]) <= 1e-13
+    assert np.array_equal(G, G.T)
+
+
+def test_projection_matches_reference_small(orc, golden, mg):
+    g = golden("gamma_small")
+    lmax, P, S = int(g["lmax"]), int(g["P"]), int(g["S"])
+    q, tr, cl = mg.workload(lmax, P)
+    shapes = mg.separable_shapes(lmax, S // 2, seed=0) + mg.bump_shapes(S - S // 2, seed=1)
+    for s, sh in enumerate(shapes):
+        b = orc.project(2, lmax, q, tr, cl, sh, nthreads=4)
+        assert rel_fro(b, g["beta"][s]) <= 1e-13
+
+
+def test_cholesky_restatement_against_lapack(orc):
+    rng = np.random.default_rng(3)
+    A = rng.standard_normal((50, 50))
+    G = A @ A.T + 50 * np.eye(50)
+    o, lam, fail = orc.ortho_cholesky(G)
+    assert fail == -1
+    norm = np.sqrt(np.diag(G))
+    Lref = np.linalg.cholesky(G / np.outer(norm, norm))
+    assert np.allclose(o, norm[:, None] * Lref, rtol=1e-12, atol=1e-12)
+    assert np.allclose(o @ o.T, G, rtol=1e-12)
+    assert np.allclose(lam @ o, np.eye(50), atol=1e-12)
+    assert np.array_equal(np.triu(lam, 1), np.zeros((50, 50)))
+
+
+def test_cholesky_restatement_reports_failing_pivot(orc):
+    G = np.eye(6)
+    G[3, 3] = -1.0
+    G[3, 3] = 1.0
+    G[2, 4] = G[4, 2] = 2.0  # minor [[1,2],[2,1]] is indefinite
+    _, _, fail = orc.ortho_cholesky(G)
+    assert fail == 4
+
+
+def test_pca_restatement_properties():
+    import oracle
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((30, 12))
+    G = A @ A.T + 1e-3 * np.eye(30)
+    inv, lam, r = oracle.ortho_pca(G)
+    assert r == 30
+    assert np.allclose(lam @ G @ lam.T, np.eye(30), atol=1e-8)
+    assert np.allclose(inv @ inv.T, G, rtol=1e-10, atol=1e-10)
+    G2 = A @ A.T  # rank 12: some eigenvalues come out <= 0 in FP64
+    inv2, lam2, r2 = oracle.ortho_pca(G2)
+    assert 12 <= r2 <= 30
+    assert np.all(lam2[r2:] == 0) and np.all(inv2[:, r2:] == 0)
+
+
+def test_alpha_restatement(orc):
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((40, 40))
+    G = A @ A.T + 40 * np.eye(40)
+    o, lam, _ = orc.ortho_cholesky(G)
+    beta = rng.standard_normal(40)
+    a, mR = orc.alpha(o, lam, beta)
+    assert np.allclose(a, np.linalg.solve(G, beta), rtol=1e-10)
+    assert np.allclose(mR, lam @ beta, rtol=1e-10, atol=1e-12)

@@ -1,0 +1,402 @@
+#!/usr/bin/env python
+"""Benchmark: Modal-CMB mode-space hot path on GB300.
+
+One step = one pass of the hot path over the synthetic workload at
+l_max = 2000, 30 shifted-Legendre basis functions (4960 modes), n_mu = 3001,
+16 seeded separable shapes:
+  GL nodes + P_l(mu) table + l-contraction, Gamma (mu-contraction),
+  orthogonalisation, projection of the shapes, alpha solve.
+`value` = device seconds of "Gamma + ortho" per step (the first quantity of
+the metric), with inputs resident in HBM and L2 flushed between steps;
+`projections_per_s` is the second quantity.  `e2e` is the same quantity
+measured through the C ABI with host buffers (copies inside the timed region).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU path (the in-place build of its own
+sources when present, else the C restatement in oracle/) on the host cores,
+on bounded samples of the same workload, extrapolated per unit.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "modal-cmb_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "Gamma+ortho s and shape projections/s, split-prec vs FP64, GB300, rel err<=1e-6"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64 (nominal; no measured FP64 peak is available)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="cfg2")
+    ap.add_argument("--prec", choices=["auto", "fp64", "split"], default="auto")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    a = ap.parse_args()
+    a.warmup = max(3, a.warmup)
+    return a
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return p, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ------------------------------------------------------------------- clocks
+
+class Clocks:
+    """nvidia-smi sampler running while the timed region runs."""
+
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        load = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# -------------------------------------------------------------- our GPU arm
+
+def run_ours(a, ws, rank, local):
+    import torch
+    import modal_gb300 as mg
+
+    cfgd = mg.CONFIGS[a.config]
+    lmax, P = cfgd["lmax"], cfgd["P"]
+    q, tr, cl = mg.workload(lmax, P)
+    shapes = mg.config_shapes(lmax, cfgd["shapes"], seed=rank)
+    S, N = len(shapes), len(tr)
+    nmu = 3 * lmax // 2 + 1
+    torch.cuda.set_device(local)
+    ctx = mg.Context(local)
+    ctx.set_basis(2, lmax, q)
+    ctx.set_modes(tr)
+    ctx.set_spectrum(cl)
+    ctx.profile(True)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    split_ok = True
+    try:
+        ctx.init_glint()
+        ctx.gamma(mg.PREC_SPLIT, download=False)
+    except mg.ModalError:
+        split_ok = False
+    prec = {"auto": mg.PREC_SPLIT if split_ok else mg.PREC_FP64, "fp64": mg.PREC_FP64, "split": mg.PREC_SPLIT}[a.prec]
+
+    def step(pr):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        e[0].record(stream)
+        ctx.init_glint()
+        ctx.gamma(pr, download=False)
+        ctx.orthogonalise(None, download=False)
+        e[1].record(stream)
+        ctx.project(shapes, pr, download=False)
+        e[2].record(stream)
+        ctx.alpha(S, download=False)
+        e[3].record(stream)
+        return e
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    def run(pr, steps, warm):
+        for _ in range(warm):
+            step(pr)
+            flush.zero_()
+            torch.cuda.synchronize()
+        ctx.timer_reset()
+        times = []
+        launches0 = ctx.launches
+        barrier()
+        torch.cuda.synchronize()
+        clk = Clocks(local) if pr == prec else None
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            ev = step(pr)
+            torch.cuda.synchronize()
+            times.append([ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])])
+            flush.zero_()  # L2 flush between steps (outside the events)
+            torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        clocks = clk.stop() if clk else None
+        barrier()
+        launches = ctx.launches - launches0
+        tm = {k: ctx.timer(k) for k in ("gl", "pl", "mij", "gamma", "ortho", "project", "alpha")}
+        return np.array(times), wall, launches, tm, clocks
+
+    times, wall, launches, tm, clocks = run(prec, a.steps, a.warmup)
+    go_ms = float(np.median(times[:, 0]))
+    proj_ms = float(np.median(times[:, 1]))
+    step_ms = float(np.median(times.sum(axis=1)))
+    if ws > 1:  # max over ranks
+        t = torch.tensor([go_ms, proj_ms, step_ms], device=f"cuda:{local}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        go_ms, proj_ms, step_ms = t.tolist()
+
+    # the other precision, for the split-vs-FP64 ratio and the error against FP64
+    extra = {}
+    ctx.init_glint()
+    ctx.gamma(mg.PREC_FP64, download=False)
+    G64 = ctx.gamma(mg.PREC_FP64)
+    ctx.orthogonalise(None, download=False)
+    b64 = ctx.project(shapes, mg.PREC_FP64)
+    a64, m64 = ctx.alpha(S)
+    if split_ok:
+        other = mg.PREC_FP64 if prec == mg.PREC_SPLIT else mg.PREC_SPLIT
+        t2, _, _, tm2, _ = run(other, max(1, min(a.steps, 2)), 1 if other == mg.PREC_FP64 else 3)
+        Gs = ctx.gamma(mg.PREC_SPLIT)
+        ctx.orthogonalise(None, download=False)
+        bs = ctx.project(shapes, mg.PREC_SPLIT)
+        as_, ms_ = ctx.alpha(S)
+        fp = t2 if other == mg.PREC_FP64 else times
+        sp = times if other == mg.PREC_FP64 else t2
+        d = as_ - a64
+        gnorm = lambda v: np.sqrt(np.abs(np.einsum("si,ij,sj->s", v, G64, v)))  # noqa: E731
+        extra = {
+            "fp64_gamma_ortho_ms": float(np.median(fp[:, 0])), "split_gamma_ortho_ms": float(np.median(sp[:, 0])),
+            "fp64_projection_ms": float(np.median(fp[:, 1])), "split_projection_ms": float(np.median(sp[:, 1])),
+            "split_vs_fp64_gamma_ortho_projection": float(np.median(fp[:, :2].sum(1)) / np.median(sp[:, :2].sum(1))),
+            "rel_err_vs_fp64": {
+                "gamma_fro": float(np.linalg.norm(Gs - G64) / np.linalg.norm(G64)),
+                "beta_fro": float(np.linalg.norm(bs - b64) / np.linalg.norm(b64)),
+                "alpha_gamma_norm": float(np.max(gnorm(d) / np.maximum(gnorm(a64), 1e-300))),
+                "modesR_fro": float(np.linalg.norm(ms_ - m64) / np.linalg.norm(m64)),
+            },
+        }
+
+    # roofline of the dominant kernel: the mu-contraction (Gamma)
+    pk, pk_kind = peaks()
+    g_ms, g_n = tm["gamma"]
+    g_launch_ms = g_ms / max(1, g_n)
+    flops = 18.0 * N * (N + 1) / 2.0 * nmu
+    achieved = flops / (g_launch_ms * 1e-3) / 1e12
+    if prec == mg.PREC_FP64:
+        roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
+                "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": None,
+                "kernel": "k_gamma_fp64", "peak_kind": "nominal FP64 (no measured FP64 peak)",
+                "algorithmic": "18 N(N+1)/2 n_mu flop per launch"}
+    else:
+        peak = pk.get("bf16_tflops", 1900.0)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "gamma split", "peak_kind": pk_kind + " bf16 burst",
+                "algorithmic": "18 N(N+1)/2 n_mu flop per launch"}
+
+    # end to end through the C ABI with host buffers
+    e2e = run_e2e(ctx, mg, q, tr, cl, shapes, prec, a.steps)
+    cpu = None
+    if rank == 0 and not a.no_cpu_baseline:
+        cpu = cpu_baseline(a.config, lmax, P, q, tr, cl, shapes, samples=1)
+    ctx.close()
+    line = {
+        "metric": METRIC, "value": go_ms * 1e-3, "unit": "s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == mg.PREC_FP64 else "bf16x3 split, f32 tile acc, f64 sum",
+        "data": "synthetic (seeded shapes; synthetic C_l; shifted Legendre basis)",
+        "config": {"workload": f"{a.config}: l=2..{lmax}, P={P}, N={N}, n_mu={nmu}, S={S} shapes",
+                   "l2": "flushed (256 MB write between steps)", "parallelism": f"replicas x{ws}",
+                   "precision": "fp64" if prec == mg.PREC_FP64 else "split"},
+        "projections_per_s": S * ws / (proj_ms * 1e-3),
+        "stage_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in tm.items()},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    line.update(extra)
+    return line
+
+
+def run_e2e(ctx, mg, q, tr, cl, shapes, prec, steps):
+    """Gamma + ortho through the public C ABI from host inputs to host outputs."""
+    ts = []
+    N = len(tr)
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        ctx.set_basis(2, q.shape[0] + 1, q)
+        ctx.set_modes(tr)
+        ctx.init_glint()
+        G = ctx.gamma(prec)
+        o, lam, _, _ = ctx.orthogonalise(None)
+        ts.append(time.perf_counter() - t0)
+    ctx.set_spectrum(cl)
+    h2d = q.nbytes + tr.astype(np.int32).nbytes
+    d2h = G.nbytes + o.nbytes + lam.nbytes
+    return {"value": float(np.median(ts)), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "what": "set_basis/set_modes (H2D) + init_glint + gamma (D2H Gamma) + orthogonalise (D2H orthol, lambdal)",
+            "N": N}
+
+
+# -------------------------------------------------------- CPU reference arm
+
+def cpu_baseline(config, lmax, P, q, tr, cl, shapes, samples=1):
+    """Reference CPU path on the host cores, on bounded samples extrapolated to
+    the full workload: Gamma (P_l table + l-contraction in full, calculate_orthol
+    over a sample of pairs), orthogonalisation (the reference always runs the
+    full eigen-decomposition, ortho_late_mpi.c:775, then Cholesky; timed at a
+    sample size and scaled as N^3) and the projection (calculate_mode_3D over a
+    sample of tetrapyd points per thread)."""
+    import oracle
+    cores = os.cpu_count() or 1
+    ref = None
+    kind = "port"
+    try:
+        if os.path.exists(oracle.REF_SO):
+            ref = oracle.Ref()
+            kind = "reference"
+    except Exception:
+        ref = None
+    orc = oracle.Oracle()
+    N = len(tr)
+    nmu = 3 * lmax // 2 + 1
+    total_pairs = N * (N + 1) // 2
+    npairs = min(total_pairs, 20000)
+    if ref is not None:
+        # the reference's own init_orthol_glint + calculate_orthoMij_T and calculate_orthol loop
+        ref.setup(2, lmax, q, tr, cl)
+        t0 = time.perf_counter()
+        with oracle.quiet_stdout():
+            ref.init_gamma()
+        t_init = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        ref.gamma(nranks=cores, npairs=npairs)
+        t_pairs = time.perf_counter() - t0
+    else:
+        t0 = time.perf_counter()
+        x, w = orc.gl_nodes(nmu)
+        pl = orc.legendre_table(x, lmax)
+        M = orc.mij(pl, 2, lmax, q)
+        t_init = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        orc.gamma_sample(M, w, tr, npairs, nthreads=cores)
+        t_pairs = time.perf_counter() - t0
+    t_gamma = t_init + t_pairs * total_pairs / npairs
+    # orthogonalisation: eigen (numpy/LAPACK standing in for gsl_eigen_symmv) + Cholesky restatement
+    ns = min(N, 1024)
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((ns, ns))
+    Gs = A @ A.T + ns * np.eye(ns)
+    t0 = time.perf_counter()
+    np.linalg.eigh(Gs)
+    orc.ortho_cholesky(Gs)
+    t_ortho = (time.perf_counter() - t0) * (N / ns) ** 3
+    # projection sample
+    npts_total = orc.tetrapyd_count(2, lmax)
+    per_thread = 2000 if N > 1000 else 20000
+    sh = shapes[0]
+    t0 = time.perf_counter()
+    if ref is not None:
+        ref.project(sh, nthreads=cores, max_points=per_thread)
+    else:
+        orc.project(2, lmax, q, tr, cl, sh, nthreads=cores, max_points=per_thread)
+    t_proj = (time.perf_counter() - t0) * npts_total / (per_thread * cores)
+    return {"value": t_gamma + t_ortho, "unit": "s", "cores": cores, "kind": kind,
+            "sample": (f"Gamma: l-contraction in full + {npairs} of {total_pairs} pairs; ortho: eigh+Cholesky at "
+                       f"N={ns} scaled by (N/{ns})^3; projection: {per_thread} points/thread of {npts_total}"),
+            "gamma_s": t_gamma, "ortho_s": t_ortho, "projections_per_s": 1.0 / t_proj}
+
+
+def run_reference(a, ws, rank):
+    import modal_gb300 as mg
+    cfgd = mg.CONFIGS[a.config]
+    lmax, P = cfgd["lmax"], cfgd["P"]
+    q, tr, cl = mg.workload(lmax, P)
+    shapes = mg.config_shapes(lmax, cfgd["shapes"], seed=0)
+    res = []
+    for i in range(a.warmup // 3 + a.steps):
+        r = cpu_baseline(a.config, lmax, P, q, tr, cl, shapes)
+        if i >= a.warmup // 3:
+            res.append(r)
+    v = float(np.median([r["value"] for r in res]))
+    c = dict(res[-1])
+    c["value"] = v
+    N = len(tr)
+    return {"metric": METRIC, "value": v, "unit": "s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{a.config}: l=2..{lmax}, P={P}, N={N}, n_mu={3 * lmax // 2 + 1}, S={len(shapes)} shapes"},
+            "projections_per_s": float(np.median([r["projections_per_s"] for r in res])),
+            "cpu_baseline": c, "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    a = parse()
+    ws, rank, local = dist()
+    if a.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(a, ws, rank)), flush=True)
+        return
+    if ws > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    line = run_ours(a, ws, rank, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

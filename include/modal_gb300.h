@@ -69,6 +69,25 @@ long modal_ctx_launches(const modal_ctx *ctx);
 /* Block until all work on the context's stream is done. */
 modal_status modal_ctx_sync(modal_ctx *ctx);
 
+/* Per-stage device timers (CUDA events on the context's stream).  With
+ * profiling enabled every stage below records an event pair around its
+ * kernels; modal_ctx_timer synchronises and returns the summed milliseconds
+ * and the number of timed runs since the last reset.  No reference
+ * counterpart (the reference prints CPU times, mtime.c:17-25). */
+typedef enum {
+    MODAL_T_GL = 0,       /* Gauss-Legendre nodes */
+    MODAL_T_PL = 1,       /* P_l(mu) table */
+    MODAL_T_MIJ = 2,      /* l-contraction */
+    MODAL_T_GAMMA = 3,    /* mu-contraction (Gamma) */
+    MODAL_T_ORTHO = 4,    /* orthogonalisation */
+    MODAL_T_PROJECT = 5,  /* projection of the shapes */
+    MODAL_T_ALPHA = 6,    /* alpha solve */
+    MODAL_T_COUNT = 7
+} modal_timer;
+modal_status modal_ctx_profile(modal_ctx *ctx, int enable);
+modal_status modal_ctx_timer(modal_ctx *ctx, int timer, double *ms, long *count);
+modal_status modal_ctx_timer_reset(modal_ctx *ctx);
+
 /* ------------------------------------------------- stand-alone primitives */
 
 /* Gauss-Legendre nodes and weights on [-1,1], ascending, computed on the GPU.

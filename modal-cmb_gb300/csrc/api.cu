@@ -89,6 +89,47 @@ static modal_status need(modal_ctx *c, bool ok, const char *what)
     return MODAL_OK;
 }
 
+static cudaEvent_t take_event(modal_ctx *c)
+{
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    return e;
+}
+
+StageTimer::StageTimer(modal_ctx *c, int i) : ctx(c), id(i)
+{
+    if (ctx && ctx->profile) {
+        a = take_event(ctx);
+        if (a) cudaEventRecord(a, ctx->stream);
+    }
+}
+
+void StageTimer::stop()
+{
+    if (!a) return;
+    cudaEvent_t b = take_event(ctx);
+    if (b) {
+        cudaEventRecord(b, ctx->stream);
+        ctx->timers[id].push_back({a, b});
+    } else {
+        ctx->event_pool.push_back(a);
+    }
+    a = nullptr;
+}
+
+static void timers_clear(modal_ctx *c)
+{
+    for (auto &v : c->timers) {
+        for (auto &r : v) { c->event_pool.push_back(r.a); c->event_pool.push_back(r.b); }
+        v.clear();
+    }
+}
+
 }  // namespace modal
 
 using namespace modal;
@@ -122,8 +163,42 @@ void modal_ctx_destroy(modal_ctx *c)
                       &c->orthol, &c->lambdal, &c->norm, &c->info, &c->cl, &c->vl, &c->beta, &c->alpha,
                       &c->modesr, &c->scratch, &c->scratch2, &c->shape_tab, &c->shape_desc, &c->slab_order};
     for (DevBuf *b : bufs) release(*b);
+    timers_clear(c);
+    for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
+}
+
+modal_status modal_ctx_profile(modal_ctx *c, int enable)
+{
+    if (!c) { set_error("ctx is NULL"); return MODAL_ERR_ARG; }
+    c->profile = enable != 0;
+    return MODAL_OK;
+}
+
+modal_status modal_ctx_timer(modal_ctx *c, int id, double *ms, long *count)
+{
+    if (!c || id < 0 || id >= MODAL_T_COUNT) { set_error("modal_ctx_timer: bad args"); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    MODAL_TRY(sync(c));
+    double tot = 0.0;
+    for (auto &r : c->timers[id]) {
+        float t = 0.f;
+        MODAL_CUDA(cudaEventElapsedTime(&t, r.a, r.b));
+        tot += t;
+    }
+    if (ms) *ms = tot;
+    if (count) *count = (long)c->timers[id].size();
+    return MODAL_OK;
+}
+
+modal_status modal_ctx_timer_reset(modal_ctx *c)
+{
+    if (!c) { set_error("ctx is NULL"); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    MODAL_TRY(sync(c));
+    timers_clear(c);
+    return MODAL_OK;
 }
 
 void *modal_ctx_stream(modal_ctx *c) { return c ? (void *)c->stream : nullptr; }
@@ -292,11 +367,18 @@ modal_status modal_init_glint(modal_ctx *c)
         c->nmu = 3 * c->lmax / 2 + 1;  // orthogonalisation_late.c:37
         MODAL_TRY(ensure(c->mu, sizeof(double) * c->nmu));
         MODAL_TRY(ensure(c->w, sizeof(double) * c->nmu));
+        StageTimer t(c, MODAL_T_GL);
         MODAL_TRY(gl_nodes_dev(c, c->nmu, c->mu.as<double>(), c->w.as<double>()));
     }
     MODAL_TRY(ensure(c->pl, sizeof(double) * (size_t)(c->lmax + 1) * c->nmu));
-    MODAL_TRY(legendre_table_dev(c, c->nmu, c->lmax, c->mu.as<double>(), c->pl.as<double>()));
-    MODAL_TRY(mij_dev(c));
+    {
+        StageTimer t(c, MODAL_T_PL);
+        MODAL_TRY(legendre_table_dev(c, c->nmu, c->lmax, c->mu.as<double>(), c->pl.as<double>()));
+    }
+    {
+        StageTimer t(c, MODAL_T_MIJ);
+        MODAL_TRY(mij_dev(c));
+    }
     MODAL_TRY(sync(c));
     c->have_glint = true;
     c->have_gamma = c->have_ortho = false;
@@ -332,8 +414,11 @@ modal_status modal_gamma(modal_ctx *c, modal_prec prec, double *gamma)
     if (prec != MODAL_PREC_FP64 && prec != MODAL_PREC_SPLIT) { set_error("modal_gamma: prec=%d", (int)prec); return MODAL_ERR_ARG; }
     MODAL_CUDA(cudaSetDevice(c->device));
     if (!c->have_glint) MODAL_TRY(modal_init_glint(c));
-    if (prec == MODAL_PREC_FP64) MODAL_TRY(gamma_fp64_dev(c));
-    else MODAL_TRY(gamma_split_dev(c));
+    {
+        StageTimer t(c, MODAL_T_GAMMA);
+        if (prec == MODAL_PREC_FP64) MODAL_TRY(gamma_fp64_dev(c));
+        else MODAL_TRY(gamma_split_dev(c));
+    }
     c->have_gamma = true;
     c->have_ortho = false;
     if (gamma) MODAL_TRY(d2h(c, gamma, c->gamma.ptr, sizeof(double) * (size_t)c->N * c->N));
@@ -361,7 +446,10 @@ modal_status modal_orthogonalise(modal_ctx *c, const double *gamma, int pca_flag
         c->have_gamma = true;
     }
     if (!c->have_gamma) { set_error("modal_orthogonalise: no Gamma (pass one or call modal_gamma)"); return MODAL_ERR_STATE; }
-    MODAL_TRY(ortho_dev(c, pca_flag));
+    {
+        StageTimer t(c, MODAL_T_ORTHO);
+        MODAL_TRY(ortho_dev(c, pca_flag));
+    }
     size_t NN = (size_t)c->N * c->N;
     if (orthol) MODAL_TRY(d2h(c, orthol, c->orthol.ptr, sizeof(double) * NN));
     if (lambdal) MODAL_TRY(d2h(c, lambdal, c->lambdal.ptr, sizeof(double) * NN));
@@ -390,7 +478,10 @@ modal_status modal_project(modal_ctx *c, int S, const modal_shape *shapes, modal
     if (S < 1 || !shapes) { set_error("modal_project: S=%d", S); return MODAL_ERR_ARG; }
     if (c->lmin < 2) { set_error("modal_project: lmin must be >= 2 (w_0 = w_1 = 0)"); return MODAL_ERR_ARG; }
     MODAL_CUDA(cudaSetDevice(c->device));
-    MODAL_TRY(project_dev(c, S, shapes, prec));
+    {
+        StageTimer t(c, MODAL_T_PROJECT);
+        MODAL_TRY(project_dev(c, S, shapes, prec));
+    }
     c->have_beta = true;
     c->beta_S = S;
     if (beta) MODAL_TRY(d2h(c, beta, c->beta.ptr, sizeof(double) * (size_t)S * c->N));
@@ -408,7 +499,10 @@ modal_status modal_alpha(modal_ctx *c, int S, const double *beta, double *alpha,
         set_error("modal_alpha: no device beta for S=%d (pass beta or call modal_project)", S);
         return MODAL_ERR_STATE;
     }
-    MODAL_TRY(alpha_dev(c, S));
+    {
+        StageTimer t(c, MODAL_T_ALPHA);
+        MODAL_TRY(alpha_dev(c, S));
+    }
     if (alpha) MODAL_TRY(d2h(c, alpha, c->alpha.ptr, sizeof(double) * (size_t)S * c->N));
     if (modesR) MODAL_TRY(d2h(c, modesR, c->modesr.ptr, sizeof(double) * (size_t)S * c->N));
     return sync(c);

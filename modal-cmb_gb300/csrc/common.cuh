@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 #include "../../include/modal_gb300.h"
 
 namespace modal {
@@ -58,6 +59,12 @@ struct modal_ctx {
     modal::DevBuf shape_desc;  // device shape descriptors
     modal::DevBuf slab_order;  // projection slab schedule
     double *h_info = nullptr;  // pinned readback
+
+    // profiling: event pairs per stage, summed on read
+    bool profile = false;
+    struct TimerRec { cudaEvent_t a, b; };
+    std::vector<TimerRec> timers[MODAL_T_COUNT];
+    std::vector<cudaEvent_t> event_pool;
 };
 
 namespace modal {
@@ -94,6 +101,16 @@ inline modal_status launched(modal_ctx *ctx, const char *what)
 }
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+
+// Stage timer: records an event at construction and at stop() when profiling.
+struct StageTimer {
+    modal_ctx *ctx;
+    int id;
+    cudaEvent_t a = nullptr;
+    StageTimer(modal_ctx *c, int i);
+    void stop();
+    ~StageTimer() { stop(); }
+};
 
 // ---- entry points implemented per translation unit (internal) ----
 modal_status gl_nodes_dev(modal_ctx *ctx, int n, double *d_mu, double *d_w);

@@ -29,8 +29,11 @@ EXPORTS = [
     "modal_ctx_sync", "modal_gl_nodes", "modal_legendre_table", "modal_basis_legendre", "modal_geometric",
     "modal_tetrapyd_count", "modal_set_basis", "modal_set_modes", "modal_set_gl", "modal_init_glint",
     "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_orthol_pair", "modal_orthogonalise",
-    "modal_set_spectrum", "modal_project", "modal_alpha",
+    "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
+    "modal_ctx_timer_reset",
 ]
+
+TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6}
 
 
 class ModalError(RuntimeError):
@@ -79,6 +82,9 @@ def lib():
             "modal_set_spectrum": (i, [vp, vp]),
             "modal_project": (i, [vp, i, vp, i, vp]),
             "modal_alpha": (i, [vp, i, vp, vp, vp]),
+            "modal_ctx_profile": (i, [vp, i]),
+            "modal_ctx_timer": (i, [vp, i, ctypes.POINTER(d), ctypes.POINTER(l)]),
+            "modal_ctx_timer_reset": (i, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -193,6 +199,18 @@ class Context:
     def sync(self):
         _check(lib().modal_ctx_sync(self.h))
 
+    def profile(self, enable=True):
+        _check(lib().modal_ctx_profile(self.h, int(enable)))
+
+    def timer(self, name):
+        """(summed ms, count) of a stage's device time since the last reset."""
+        ms, n = ctypes.c_double(), ctypes.c_long()
+        _check(lib().modal_ctx_timer(self.h, TIMERS[name], ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def timer_reset(self):
+        _check(lib().modal_ctx_timer_reset(self.h))
+
     def set_basis(self, lmin, lmax, q):
         q = _f64(q)
         assert q.shape[0] == lmax - lmin + 1
@@ -226,7 +244,7 @@ class Context:
         return out
 
     def gamma(self, prec=PREC_FP64, download=True):
-        out = np.empty((self.N, self.N)) if download else None
+        out = np.empty((self.N, self.N)) if (download and self.N) else None
         _check(lib().modal_gamma(self.h, prec, _ptr(out)))
         return out
 

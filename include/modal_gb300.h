@@ -179,6 +179,35 @@ modal_status modal_project(modal_ctx *ctx, int S, const modal_shape *shapes, mod
  * alpha/modesR: host [S][N] or NULL. */
 modal_status modal_alpha(modal_ctx *ctx, int S, const double *beta, double *alpha, double *modesR);
 
+/* ------------------------------------------------- allocation-free Gamma */
+
+/* FP64 Gamma for callers that cannot allocate device memory: code running
+ * inside an engine or CUDA-graph executor that owns every device byte and
+ * forbids cudaMalloc/cudaFree (which synchronise the device and fragment
+ * its arena), or a plugin that is handed pre-allocated buffers.  No
+ * counterpart in the reference (it allocates with malloc on the host).
+ *
+ * All buffers are DEVICE pointers owned by the caller: d_q[L][P] basis
+ * (L = lmax-lmin+1), d_triples[N][3], optional d_nodes/d_weights[nmu] (both
+ * NULL: n_mu = 3 lmax/2 + 1 GPU nodes; nmu is then ignored), d_gamma[N][N]
+ * output.  Same result as modal_gamma(..., MODAL_PREC_FP64, ...) with the
+ * same quadrature.  Work runs on `stream` (a cudaStream_t, NULL = default
+ * stream); the call waits for it to finish before returning.
+ *
+ * The intermediates live in one 8 MiB array built into the library
+ * (MODAL_NOALLOC_SCRATCH_BYTES); every GPU that loads the library holds it
+ * until exit.  Problems needing more (about lmax <= 500 with P <= 10, or
+ * lmax <= 600 with P <= 6, fit) are rejected with MODAL_ERR_ARG and a
+ * message giving the size needed; no device memory is ever allocated.  The
+ * first call on a device looks up the array's device address and should
+ * come before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (different streams or threads) race, so serialise them.
+ * Out-of-range triples give MODAL_ERR_ARG. */
+#define MODAL_NOALLOC_SCRATCH_BYTES (8u << 20)
+modal_status modal_gamma_fp64_noalloc(int lmin, int lmax, int P, const double *d_q, int N,
+                                      const int *d_triples, int nmu, const double *d_nodes,
+                                      const double *d_weights, double *d_gamma, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

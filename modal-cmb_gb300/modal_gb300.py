@@ -30,7 +30,7 @@ EXPORTS = [
     "modal_tetrapyd_count", "modal_set_basis", "modal_set_modes", "modal_set_gl", "modal_init_glint",
     "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_orthol_pair", "modal_orthogonalise",
     "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
-    "modal_ctx_timer_reset",
+    "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6}
@@ -85,6 +85,7 @@ def lib():
             "modal_ctx_profile": (i, [vp, i]),
             "modal_ctx_timer": (i, [vp, i, ctypes.POINTER(d), ctypes.POINTER(l)]),
             "modal_ctx_timer_reset": (i, [vp]),
+            "modal_gamma_fp64_noalloc": (i, [i, i, i, vp, i, vp, i, vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)

@@ -161,7 +161,8 @@ void modal_ctx_destroy(modal_ctx *c)
     if (c->stream) cudaStreamSynchronize(c->stream);
     DevBuf *bufs[] = {&c->q, &c->triples, &c->mu, &c->w, &c->pl, &c->mt, &c->gamma, &c->chol, &c->linv,
                       &c->orthol, &c->lambdal, &c->norm, &c->info, &c->cl, &c->vl, &c->beta, &c->alpha,
-                      &c->modesr, &c->scratch, &c->scratch2, &c->shape_tab, &c->shape_desc, &c->slab_order};
+                      &c->modesr, &c->scratch, &c->scratch2, &c->shape_tab, &c->shape_desc, &c->slab_order,
+                      &c->split};
     for (DevBuf *b : bufs) release(*b);
     timers_clear(c);
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);

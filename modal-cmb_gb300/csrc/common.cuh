@@ -58,6 +58,8 @@ struct modal_ctx {
     modal::DevBuf shape_tab;   // separable tables
     modal::DevBuf shape_desc;  // device shape descriptors
     modal::DevBuf slab_order;  // projection slab schedule
+    modal::DevBuf split;       // split-precision Gamma: operand pieces, T table, per-P tables
+    int split_P = -1;          // P the per-P tables in `split` were built for
     double *h_info = nullptr;  // pinned readback
 
     // profiling: event pairs per stage, summed on read

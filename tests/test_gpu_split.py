@@ -1,0 +1,43 @@
+"""Split-precision (FP16x2, tensor-core) Gamma against the FP64 form on the
+GPU.  Tolerance: relative Frobenius and relative max error <= 1e-6 (the
+target for the split form); emulation predicts ~5e-8."""
+import numpy as np
+import pytest
+from conftest import rel_fro, rel_max
+
+pytestmark = pytest.mark.gpu
+
+
+def _both(mg, lmin, lmax, P, triples=None):
+    cl = mg.synthetic_cl(lmax)
+    q = mg.weighted_q(mg.legendre_q(lmin, lmax, P), cl, lmin)
+    tr = mg.mode_triples(P) if triples is None else np.asarray(triples, dtype=np.int32)
+    with mg.Context(0) as c:
+        c.set_basis(lmin, lmax, q)
+        c.set_modes(tr)
+        G64 = c.gamma(mg.PREC_FP64)
+        Gs = c.gamma(mg.PREC_SPLIT)
+        Gs2 = c.gamma(mg.PREC_SPLIT)
+    return G64, Gs, Gs2
+
+
+@pytest.mark.parametrize("lmin,lmax,P", [(2, 40, 1), (2, 60, 4), (2, 500, 10), (3, 600, 17), (2, 700, 20)])
+def test_split_gamma_vs_fp64(mg, lmin, lmax, P):
+    G64, Gs, Gs2 = _both(mg, lmin, lmax, P)
+    assert np.all(np.isfinite(Gs))
+    assert rel_fro(Gs, G64) <= 1e-6
+    assert rel_max(Gs, G64) <= 1e-6
+    assert np.array_equal(Gs, Gs.T)
+    assert np.array_equal(Gs, Gs2)  # deterministic
+
+
+def test_split_gamma_unsorted_duplicate_modes(mg):
+    G64, Gs, _ = _both(mg, 2, 300, 6, triples=[[5, 1, 0], [0, 0, 0], [2, 2, 2], [5, 1, 0], [1, 3, 5]])
+    assert rel_max(Gs, G64) <= 1e-6
+
+
+def test_split_gamma_cfg2(mg):
+    """Full benchmark size: l <= 2000, P = 30, N = 4960, n_mu = 3001."""
+    G64, Gs, _ = _both(mg, 2, 2000, 30)
+    assert rel_fro(Gs, G64) <= 1e-6
+    assert rel_max(Gs, G64) <= 1e-6

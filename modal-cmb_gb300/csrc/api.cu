@@ -354,6 +354,7 @@ modal_status modal_set_gl(modal_ctx *c, int nmu, const double *nodes, const doub
     c->nmu = nmu;
     MODAL_TRY(h2d(c, c->mu, nodes, sizeof(double) * nmu));
     MODAL_TRY(h2d(c, c->w, weights, sizeof(double) * nmu));
+    c->gl_n = -1;
     MODAL_TRY(sync(c));
     c->have_user_gl = true;
     c->have_glint = c->have_gamma = c->have_ortho = false;
@@ -366,10 +367,13 @@ modal_status modal_init_glint(modal_ctx *c)
     MODAL_CUDA(cudaSetDevice(c->device));
     if (!c->have_user_gl) {
         c->nmu = 3 * c->lmax / 2 + 1;  // orthogonalisation_late.c:37
-        MODAL_TRY(ensure(c->mu, sizeof(double) * c->nmu));
-        MODAL_TRY(ensure(c->w, sizeof(double) * c->nmu));
-        StageTimer t(c, MODAL_T_GL);
-        MODAL_TRY(gl_nodes_dev(c, c->nmu, c->mu.as<double>(), c->w.as<double>()));
+        if (c->gl_n != c->nmu) {      // the nodes depend on n only: computed once per n
+            MODAL_TRY(ensure(c->mu, sizeof(double) * c->nmu));
+            MODAL_TRY(ensure(c->w, sizeof(double) * c->nmu));
+            StageTimer t(c, MODAL_T_GL);
+            MODAL_TRY(gl_nodes_dev(c, c->nmu, c->mu.as<double>(), c->w.as<double>()));
+            c->gl_n = c->nmu;
+        }
     }
     MODAL_TRY(ensure(c->pl, sizeof(double) * (size_t)(c->lmax + 1) * c->nmu));
     {

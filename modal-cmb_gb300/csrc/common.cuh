@@ -60,6 +60,7 @@ struct modal_ctx {
     modal::DevBuf slab_order;  // projection slab schedule
     modal::DevBuf split;       // split-precision Gamma: operand pieces, T table, per-P tables
     int split_P = -1;          // P the per-P tables in `split` were built for
+    int gl_n = -1;             // n of the GPU quadrature held in mu/w (-1: none or caller-supplied)
     double *h_info = nullptr;  // pinned readback
 
     // profiling: event pairs per stage, summed on read

@@ -373,6 +373,8 @@ CONFIGS = {
     "cfg2": dict(lmax=2000, P=30, shapes=("sep", 16, 1, 2)),
     "cfg3": dict(lmax=2000, P=30, shapes=("mix", 256, 1, 4)),
     "cfg5": dict(lmax=2500, P=40, shapes=("mix", 512, 1, 4)),
+    # mid-size case for kernel captures: operands larger than L2, a few GB at most
+    "prof": dict(lmax=1000, P=20, shapes=("sep", 4, 1, 2)),
 }
 
 

@@ -179,6 +179,244 @@ __global__ void k_project_beta(int N, int P, int S, const int *__restrict__ trip
     beta[e] = v / 6e0;
 }
 
+
+// ---------------------------------------------------------------------------
+// Split-precision (FP32) form of the slab kernel, for many shapes per launch.
+// Same sum factorisation; FP32 products with compensated (Kahan) FP32
+// accumulation, because GB300's FP64 rate is 1/64 of FP32.
+//   grid (slab, shape group of SG shapes), 8 warps; each warp takes two
+//   tetrapyd rows j and j+2 (same k parity, overlapping k windows, so each
+//   q_c(k) load serves both rows and all SG shapes); lanes own c.
+//   Per 32-point block a lane evaluates h~^2 once and the SG shapes, the warp
+//   then accumulates H_s[j][c] in FP32 and folds each block into a Kahan sum.
+//   The 16 rows' H go through shared memory into F_s[b][c] (Kahan pairs in
+//   shared memory); F_i is written in FP32 for the reduction over slabs.
+// ---------------------------------------------------------------------------
+struct FShape {
+    int kind, nterms;
+    long tab_off;
+    float ch[3], cl[3];  // bump centre as hi + lo float pairs
+    float inv2s2;
+};
+
+__device__ __forceinline__ void kahan_add(float &hi, float &lo, float x)
+{
+    float y = x - lo;
+    float t = hi + y;
+    lo = (t - hi) - y;
+    hi = t;
+}
+
+__device__ __forceinline__ float geo_f(int l1, int l2, int l3)
+{
+    const float L3 = (float)(l1 + l2 + l3);
+    const float a1 = (float)(l2 + l3 - l1), a2 = (float)(l3 + l1 - l2), a3 = (float)(l1 + l2 - l3);
+    const float third = 1.f / 3.f, sixth = 1.f / 6.f;
+    const float fact = 0.0506605918211689f;  // 1/(2 pi^2)
+    float p1 = fact * ((2.f * l1 + 1.f) * (2.f * l2 + 1.f) * (2.f * l3 + 1.f)) / (L3 + 1.f);
+    float p2 = (L3 + third) / ((a1 + third) * (a2 + third) * (a3 + third));
+    float p3 = sqrtf((a1 + sixth) * (a2 + sixth) * (a3 + sixth) / (L3 + sixth));
+    return p1 * p2 * p3;
+}
+
+__device__ __forceinline__ float permsix_f(int i, int j, int k)
+{
+    return (i == k && i == j) ? 1.f : ((i == j || j == k || i == k) ? 3.f : 6.f);
+}
+
+__device__ __forceinline__ float shape_f(const FShape &s, const float *__restrict__ tab, int stride, int i, int j, int k)
+{
+    if (s.kind == MODAL_SHAPE_SEPARABLE) {
+        float acc = 0.f;
+        for (int t = 0; t < s.nterms; t++) {
+            const float *f = tab + s.tab_off + (long)t * 3 * stride;
+            const float *g = f + stride, *h = g + stride;
+            float fi = f[i], fj = f[j], fk = f[k], gi = g[i], gj = g[j], gk = g[k], hi = h[i], hj = h[j], hk = h[k];
+            acc += (fi * (gj * hk + gk * hj) + fj * (gi * hk + gk * hi) + fk * (gi * hj + gj * hi)) * (1.f / 6.f);
+        }
+        return acc;
+    }
+    // Gaussian bump: exp(-|(l1,l2,l3)/L - c|^2 / (2 sigma^2)).  l_m/L - c_m is
+    // formed as (l_m - c_m L)/L with c_m = hi + lo and the exact FMA residual of
+    // hi*L, so it is accurate relative to itself: the exponent (up to ~200 |x|^2
+    // for sigma = 0.05) then keeps ~1e-7 relative accuracy in FP32.
+    const float L = (float)(i + j + k), invL = 1.f / L;
+    const float l3[3] = {(float)i, (float)j, (float)k};
+    float a = 0.f;
+#pragma unroll
+    for (int m = 0; m < 3; m++) {
+        const float p = s.ch[m] * L;
+        const float e = fmaf(s.ch[m], L, -p);
+        const float d = (((l3[m] - p) - e) - s.cl[m] * L) * invL;
+        a = fmaf(d, d, a);
+    }
+    return expf(-a * s.inv2s2);
+}
+
+template <int SG, int CPL>
+__global__ void __launch_bounds__(256) k_project_slab_f32(int lmin, int lmax, int P, int S,
+                                                           const int *__restrict__ slab_order,
+                                                           const float *__restrict__ qf, const float *__restrict__ vlf,
+                                                           const FShape *__restrict__ shapes,
+                                                           const float *__restrict__ tabf, float *__restrict__ Fbuf)
+{
+    constexpr int JC = 16, CW = 32 * CPL;
+    __shared__ float fsm[8][2][32][SG];
+    __shared__ float Hs[JC][SG][CW];
+    __shared__ FShape sh[SG];
+    extern __shared__ float Fsm[];  // [SG*P*P] hi, then [SG*P*P] lo
+    const int slab = slab_order[blockIdx.x];
+    const int i = lmin + slab;
+    const int s0 = blockIdx.y * SG;
+    const int sgv = min(SG, S - s0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int par = i & 1, PP = P * P, L = lmax - lmin + 1, stride = lmax + 1;
+    if (threadIdx.x < SG) {
+        FShape z = {1, 0, 0, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 0.f};
+        sh[threadIdx.x] = (threadIdx.x < sgv) ? shapes[s0 + threadIdx.x] : z;
+    }
+    float *Fhi = Fsm, *Flo = Fsm + SG * PP;
+    for (int e = threadIdx.x; e < 2 * SG * PP; e += 256) Fsm[e] = 0.f;
+    __syncthreads();
+    const float vi = vlf[i];
+    const int jo = (warp >> 1) * 4 + (warp & 1);  // rows jo and jo+2 of each chunk
+
+    for (int j0 = i; j0 <= lmax; j0 += JC) {
+        const int jA = j0 + jo, jB = jA + 2;
+        float HAh[SG][CPL], HAl[SG][CPL], HBh[SG][CPL], HBl[SG][CPL];
+#pragma unroll
+        for (int s = 0; s < SG; s++)
+#pragma unroll
+            for (int cc = 0; cc < CPL; cc++) HAh[s][cc] = HAl[s][cc] = HBh[s][cc] = HBl[s][cc] = 0.f;
+        if (jA <= lmax) {
+            const bool hasB = jB <= lmax;
+            const int kstart = jA + par;
+            const int kendA = min(i + jA, lmax), kendB = hasB ? min(i + jB, lmax) : -1;
+            const int kend = max(kendA, kendB);
+            const int nk = (kend >= kstart) ? (kend - kstart) / 2 + 1 : 0;
+            const float vA = vi * vlf[jA], vB = hasB ? vi * vlf[jB] : 0.f;
+            for (int kb = 0; kb < nk; kb += 32) {
+                const int kk = kb + lane, k = kstart + 2 * kk;
+                float fa[SG], fb2[SG];
+#pragma unroll
+                for (int s = 0; s < SG; s++) fa[s] = fb2[s] = 0.f;
+                if (kk < nk) {
+                    const float vk = vlf[k];
+                    if (k <= kendA) {
+                        float g = permsix_f(i, jA, k) * geo_f(i, jA, k) * vA * vk;
+#pragma unroll
+                        for (int s = 0; s < SG; s++)
+                            if (s < sgv) fa[s] = g * shape_f(sh[s], tabf, stride, i, jA, k);
+                    }
+                    if (hasB && k >= jB + par && k <= kendB) {
+                        float g = permsix_f(i, jB, k) * geo_f(i, jB, k) * vB * vk;
+#pragma unroll
+                        for (int s = 0; s < SG; s++)
+                            if (s < sgv) fb2[s] = g * shape_f(sh[s], tabf, stride, i, jB, k);
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < SG; s++) { fsm[warp][0][lane][s] = fa[s]; fsm[warp][1][lane][s] = fb2[s]; }
+                __syncwarp();
+                const int nt = min(32, nk - kb);
+                float hA[SG][CPL], hB[SG][CPL];
+#pragma unroll
+                for (int s = 0; s < SG; s++)
+#pragma unroll
+                    for (int cc = 0; cc < CPL; cc++) hA[s][cc] = hB[s][cc] = 0.f;
+                for (int t = 0; t < nt; t++) {
+                    const int kt = kstart + 2 * (kb + t);
+                    const float *qrow = qf + (size_t)(kt - lmin) * P;
+                    float qv[CPL];
+#pragma unroll
+                    for (int cc = 0; cc < CPL; cc++) qv[cc] = (lane + 32 * cc < P) ? qrow[lane + 32 * cc] : 0.f;
+#pragma unroll
+                    for (int s = 0; s < SG; s++) {
+                        const float a = fsm[warp][0][t][s], b = fsm[warp][1][t][s];
+#pragma unroll
+                        for (int cc = 0; cc < CPL; cc++) {
+                            hA[s][cc] = fmaf(a, qv[cc], hA[s][cc]);
+                            hB[s][cc] = fmaf(b, qv[cc], hB[s][cc]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < SG; s++)
+#pragma unroll
+                    for (int cc = 0; cc < CPL; cc++) {
+                        kahan_add(HAh[s][cc], HAl[s][cc], hA[s][cc]);
+                        kahan_add(HBh[s][cc], HBl[s][cc], hB[s][cc]);
+                    }
+                __syncwarp();
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < SG; s++)
+#pragma unroll
+            for (int cc = 0; cc < CPL; cc++) {
+                Hs[jo][s][lane + 32 * cc] = HAh[s][cc] + HAl[s][cc];
+                Hs[jo + 2][s][lane + 32 * cc] = HBh[s][cc] + HBl[s][cc];
+            }
+        __syncthreads();
+        for (int e = threadIdx.x; e < sgv * PP; e += 256) {
+            const int s = e / PP, rem = e - s * PP, b = rem / P, c = rem - b * P;
+            float acc = 0.f;
+#pragma unroll 4
+            for (int r = 0; r < JC; r++) {
+                const int j = j0 + r;
+                if (j <= lmax) acc = fmaf(qf[(size_t)(j - lmin) * P + b], Hs[r][s][c], acc);
+            }
+            kahan_add(Fhi[e], Flo[e], acc);
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < sgv * PP; e += 256) {
+        const int s = e / PP, rem = e - s * PP;
+        Fbuf[((size_t)(s0 + s) * L + slab) * PP + rem] = Fhi[e] + Flo[e];
+    }
+}
+
+// B[s][a][bc] = sum_slab q[slab][a] F[s][slab][bc], FP32 with Kahan compensation.
+__global__ void k_project_B_f32(int L, int P, int S, const float *__restrict__ qf, const float *__restrict__ Fbuf,
+                                double *__restrict__ B)
+{
+    const int PP = P * P;
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)S * P * PP) return;
+    int s = (int)(e / ((size_t)P * PP));
+    int rem = (int)(e - (size_t)s * P * PP);
+    int a = rem / PP, bc = rem - a * PP;
+    const float *F = Fbuf + (size_t)s * L * PP + bc;
+    float hi = 0.f, lo = 0.f;
+    for (int l = 0; l < L; l++) kahan_add(hi, lo, qf[(size_t)l * P + a] * F[(size_t)l * PP]);
+    B[e] = (double)hi + (double)lo;
+}
+
+__global__ void k_d2f(long n, const double *__restrict__ in, float *__restrict__ out)
+{
+    long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) out[e] = (float)in[e];
+}
+
+__global__ void k_fshapes(int S, const DShape *__restrict__ in, FShape *__restrict__ out)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    DShape d = in[s];
+    FShape f;
+    f.kind = d.kind;
+    f.nterms = d.nterms;
+    f.tab_off = d.tab_off;
+    const double c[3] = {d.c1, d.c2, d.c3};
+    for (int m = 0; m < 3; m++) {
+        f.ch[m] = (float)c[m];
+        f.cl[m] = (float)(c[m] - (double)f.ch[m]);
+    }
+    f.inv2s2 = (float)(1.0 / (2.0 * d.sigma * d.sigma));
+    out[s] = f;
+}
+
+
 static long slab_points(int i, int lmax)
 {
     long n = 0;
@@ -189,9 +427,10 @@ static long slab_points(int i, int lmax)
     return n;
 }
 
+modal_status project_split(modal_ctx *ctx, int S, long tab_total);
+
 modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec)
 {
-    (void)prec;
     const int lmin = ctx->lmin, lmax = ctx->lmax, L = ctx->L, P = ctx->P, N = ctx->N, PP = P * P;
     // shapes -> device descriptors + concatenated separable tables
     std::vector<DShape> ds(S);
@@ -238,6 +477,7 @@ modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal
     k_vl<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax, ctx->cl.as<double>(), ctx->vl.as<double>());
     MODAL_TRY(launched(ctx, "vl"));
 
+    if (prec == MODAL_PREC_SPLIT) return project_split(ctx, S, tab_total);
     size_t fbytes = sizeof(double) * (size_t)S * L * PP;
     size_t bbytes = sizeof(double) * (size_t)S * P * PP;
     MODAL_TRY(ensure(ctx->scratch, fbytes + bbytes));
@@ -262,6 +502,54 @@ modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal
     size_t nb = (size_t)S * P * PP;
     k_project_B<<<ceil_div((long)nb, 256), 256, 0, ctx->stream>>>(L, P, S, ctx->q.as<double>(), Fbuf, B);
     MODAL_TRY(launched(ctx, "project_B"));
+    MODAL_TRY(ensure(ctx->beta, sizeof(double) * (size_t)S * N));
+    k_project_beta<<<ceil_div((long)S * N, 256), 256, 0, ctx->stream>>>(N, P, S, ctx->triples.as<int>(), B,
+                                                                          ctx->beta.as<double>());
+    return launched(ctx, "project_beta");
+}
+
+// FP32 path: operands converted once, all shapes in one slab launch.
+modal_status project_split(modal_ctx *ctx, int S, long tab_total)
+{
+    const int lmin = ctx->lmin, lmax = ctx->lmax, L = ctx->L, P = ctx->P, N = ctx->N, PP = P * P;
+    const int CPL = (P <= 32) ? 1 : 2;
+    const int SG = (P <= 32) ? 8 : 4;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    size_t o = 0;
+    const size_t o_q = o; o += al(sizeof(float) * (size_t)L * P);
+    const size_t o_v = o; o += al(sizeof(float) * (lmax + 1));
+    const size_t o_t = o; o += al(sizeof(float) * (size_t)(tab_total > 0 ? tab_total : 1));
+    const size_t o_s = o; o += al(sizeof(FShape) * (size_t)S);
+    const size_t o_F = o; o += al(sizeof(float) * (size_t)S * L * PP);
+    const size_t o_B = o; o += al(sizeof(double) * (size_t)S * P * PP);
+    MODAL_TRY(ensure(ctx->scratch, o));
+    uint8_t *b = ctx->scratch.as<uint8_t>();
+    float *qf = reinterpret_cast<float *>(b + o_q), *vlf = reinterpret_cast<float *>(b + o_v);
+    float *tabf = reinterpret_cast<float *>(b + o_t), *Fbuf = reinterpret_cast<float *>(b + o_F);
+    FShape *fs = reinterpret_cast<FShape *>(b + o_s);
+    double *B = reinterpret_cast<double *>(b + o_B);
+    k_d2f<<<ceil_div((long)L * P, 256), 256, 0, ctx->stream>>>((long)L * P, ctx->q.as<double>(), qf);
+    MODAL_TRY(launched(ctx, "d2f_q"));
+    k_d2f<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax + 1, ctx->vl.as<double>(), vlf);
+    MODAL_TRY(launched(ctx, "d2f_vl"));
+    if (tab_total > 0) {
+        k_d2f<<<ceil_div(tab_total, 256), 256, 0, ctx->stream>>>(tab_total, ctx->shape_tab.as<double>(), tabf);
+        MODAL_TRY(launched(ctx, "d2f_tab"));
+    }
+    k_fshapes<<<ceil_div(S, 64), 64, 0, ctx->stream>>>(S, ctx->shape_desc.as<DShape>(), fs);
+    MODAL_TRY(launched(ctx, "fshapes"));
+    size_t smem = sizeof(float) * 2 * (size_t)SG * PP;
+    dim3 grid(L, ceil_div(S, SG));
+    auto run = [&](auto kern) -> modal_status {
+        MODAL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        kern<<<grid, 256, smem, ctx->stream>>>(lmin, lmax, P, S, ctx->slab_order.as<int>(), qf, vlf, fs, tabf, Fbuf);
+        return launched(ctx, "project_slab_f32");
+    };
+    if (CPL == 1) MODAL_TRY(run(k_project_slab_f32<8, 1>));
+    else MODAL_TRY(run(k_project_slab_f32<4, 2>));
+    size_t nb = (size_t)S * P * PP;
+    k_project_B_f32<<<ceil_div((long)nb, 256), 256, 0, ctx->stream>>>(L, P, S, qf, Fbuf, B);
+    MODAL_TRY(launched(ctx, "project_B_f32"));
     MODAL_TRY(ensure(ctx->beta, sizeof(double) * (size_t)S * N));
     k_project_beta<<<ceil_div((long)S * N, 256), 256, 0, ctx->stream>>>(N, P, S, ctx->triples.as<int>(), B,
                                                                           ctx->beta.as<double>());

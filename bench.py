@@ -35,6 +35,10 @@ import numpy as np  # noqa: E402
 METRIC = "Gamma+ortho s and shape projections/s, split-prec vs FP64, GB300, rel err<=1e-6"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64 (nominal; no measured FP64 peak is available)
+# From the ncu capture of k_gamma_lift at cfg2 (profiles/gamma_lift_cfg2.md):
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch, and tensor-pipe activity.
+TRAFFIC_LIFT_CFG2 = 1.356191e9 + 46.257152e6
+NCU_TENSOR_ACTIVE_CFG2 = 50.6
 
 
 def parse():
@@ -182,7 +186,7 @@ def run_ours(a, ws, rank, local):
         clocks = clk.stop() if clk else None
         barrier()
         launches = ctx.launches - launches0
-        tm = {k: ctx.timer(k) for k in ("gl", "pl", "mij", "gamma", "ortho", "project", "alpha")}
+        tm = {k: ctx.timer(k) for k in ("gl", "pl", "mij", "gamma", "lift", "ortho", "project", "alpha")}
         return np.array(times), wall, launches, tm, clocks
 
     times, wall, launches, tm, clocks = run(prec, a.steps, a.warmup)
@@ -225,22 +229,65 @@ def run_ours(a, ws, rank, local):
             },
         }
 
-    # roofline of the dominant kernel: the mu-contraction (Gamma)
+    # the 256-shape batch at this size (128 separable sums of 1-4 terms + 128
+    # Gaussian bumps), split form; the FP64 form is scaled from the timed shapes
+    if split_ok and a.config in ("cfg2", "cfg3"):
+        sh256 = mg.config_shapes(lmax, ("mix", 256, 1, 4), seed=rank)
+        for _ in range(2):
+            ctx.project(sh256, mg.PREC_SPLIT, download=False)
+        torch.cuda.synchronize()
+        p_ms = []
+        for _ in range(2):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ctx.project(sh256, mg.PREC_SPLIT, download=False)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            p_ms.append(e0.elapsed_time(e1))
+        p256 = float(np.median(p_ms))
+        fp64_256 = extra.get("fp64_projection_ms", proj_ms) * 256.0 / S
+        go64 = extra.get("fp64_gamma_ortho_ms", go_ms)
+        gos = extra.get("split_gamma_ortho_ms", go_ms)
+        extra["projection_256_shapes"] = {
+            "split_ms": p256, "split_projections_per_s": 256.0 / (p256 * 1e-3),
+            "fp64_ms_scaled_from_%d_shapes" % S: fp64_256,
+            "split_vs_fp64_gamma_ortho_plus_256_projections": (go64 + fp64_256) / (gos + p256)}
+
+    # roofline of the dominant kernel of this library on the path: the mu-contraction.
+    # achieved = algorithmic flop of Gamma (18 N(N+1)/2 n_mu, counted once per pair)
+    # / that kernel's mean device time in the timed steps (CUDA events on its stream).
     pk, pk_kind = peaks()
-    g_ms, g_n = tm["gamma"]
-    g_launch_ms = g_ms / max(1, g_n)
     flops = 18.0 * N * (N + 1) / 2.0 * nmu
-    achieved = flops / (g_launch_ms * 1e-3) / 1e12
     if prec == mg.PREC_FP64:
+        g_ms, g_n = tm["gamma"]
+        t_ms = g_ms / max(1, g_n)
+        achieved = flops / (t_ms * 1e-3) / 1e12
         roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
                 "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": None,
-                "kernel": "k_gamma_fp64", "peak_kind": "nominal FP64 (no measured FP64 peak)",
+                "kernel": "k_gamma_fp64", "kernel_ms": t_ms, "peak_kind": "nominal FP64 (no measured FP64 peak)",
                 "algorithmic": "18 N(N+1)/2 n_mu flop per launch"}
     else:
-        peak = pk.get("bf16_tflops", 1900.0)
+        l_ms, l_n = tm["lift"]
+        t_ms = l_ms / max(1, l_n)
+        achieved = flops / (t_ms * 1e-3) / 1e12
+        U = P * (P + 1) // 2
+        rows = 0
+        UV = U * (U + 1) // 2
+        v_of = np.repeat(np.arange(U), np.arange(U, 0, -1))
+        for j in range((UV + 255) // 256):
+            rows += min(256, UV - j * 256) * (v_of[min(UV, (j + 1) * 256) - 1] // 128 + 1)
+        kpad = -(-nmu // 64) * 64
+        executed = 2.0 * 3 * rows * 128 * kpad  # three FP16 products, tiles actually computed
+        peak = pk.get("bf16_tflops", 1933.1)
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": None, "kernel": "gamma split", "peak_kind": pk_kind + " bf16 burst",
-                "algorithmic": "18 N(N+1)/2 n_mu flop per launch"}
+                "traffic": TRAFFIC_LIFT_CFG2 if a.config == "cfg2" else None,
+                "kernel": "k_gamma_lift", "kernel_ms": t_ms, "peak_kind": pk_kind + " bf16 burst (FP16 dense rate is equal)",
+                "algorithmic": "18 N(N+1)/2 n_mu flop per launch",
+                "executed_tensor_tflops": executed / (t_ms * 1e-3) / 1e12,
+                "executed_frac": executed / (t_ms * 1e-3) / 1e12 / peak,
+                "ncu_tensor_pipe_active_pct": NCU_TENSOR_ACTIVE_CFG2 if a.config == "cfg2" else None}
 
     # end to end through the C ABI with host buffers
     e2e = run_e2e(ctx, mg, q, tr, cl, shapes, prec, a.steps)

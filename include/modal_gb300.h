@@ -82,7 +82,8 @@ typedef enum {
     MODAL_T_ORTHO = 4,    /* orthogonalisation */
     MODAL_T_PROJECT = 5,  /* projection of the shapes */
     MODAL_T_ALPHA = 6,    /* alpha solve */
-    MODAL_T_COUNT = 7
+    MODAL_T_LIFT = 7,     /* split form: the tensor-core GEMM of the mu-contraction alone */
+    MODAL_T_COUNT = 8
 } modal_timer;
 modal_status modal_ctx_profile(modal_ctx *ctx, int enable);
 modal_status modal_ctx_timer(modal_ctx *ctx, int timer, double *ms, long *count);

@@ -16,10 +16,12 @@
 // whole of K; T is stored in FP32 and Gamma summed in FP64.  Measured error vs
 // the FP64 form: ~5e-8 relative (Frobenius) in emulation at l <= 1000.
 //
-// Kernel k_gamma_lift: one CTA per (u tile, vt tile), 6 warps:
-//   warp 0   TMA producer (2-stage ring of 96 KB: X1, X2 [128 x 64], Y1, Y2 [256 x 64],
-//            128-byte swizzle), warp 1 MMA issuer (tcgen05.mma kind::f16, M=128 N=256 K=16)
-//            and TMEM owner (256 columns), warps 2-5 epilogue (tcgen05.ld -> T).
+// Kernel k_gamma_lift: persistent, one CTA per SM walking the (u tile, vt tile)
+// list, 6 warps:
+//   warp 0   TMA producer (4-stage ring of 48 KB: X1, X2 [128 x 32], Y1, Y2 [256 x 32],
+//            64-byte swizzle), warp 1 MMA issuer (tcgen05.mma kind::f16, M=128 N=256 K=16)
+//            and TMEM owner (2 accumulators x 256 columns), warps 2-5 epilogue
+//            (tcgen05.ld -> T) draining one accumulator while the next tile fills the other.
 // Every mbarrier wait is bounded (~1 s of clock64); on expiry the CTA records an
 // error code, stops issuing, drains, frees its TMEM and returns.
 #include <cuda.h>
@@ -31,14 +33,16 @@
 
 namespace modal {
 
-constexpr int SP_BK = 64;    // K elements per stage: 128-byte FP16 rows
+constexpr int SP_BK = 32;    // K elements per stage: 64-byte FP16 rows, 64-byte swizzle
 constexpr int SP_BM = 128;   // u rows per tile = TMEM lanes
-constexpr int SP_BN = 256;   // vt columns per tile = TMEM columns
-constexpr int SP_STAGES = 2;
-constexpr uint32_t SP_A_BYTES = SP_BM * SP_BK * 2;                          // 16 KB
-constexpr uint32_t SP_B_BYTES = SP_BN * SP_BK * 2;                          // 32 KB
-constexpr uint32_t SP_STAGE_BYTES = 2 * SP_A_BYTES + 2 * SP_B_BYTES;        // 96 KB
+constexpr int SP_BN = 256;   // vt columns per tile = TMEM columns of one accumulator
+constexpr int SP_STAGES = 4;
+constexpr int SP_KPAD = 64;  // K padding of the operand rows
+constexpr uint32_t SP_A_BYTES = SP_BM * SP_BK * 2;                          // 8 KB
+constexpr uint32_t SP_B_BYTES = SP_BN * SP_BK * 2;                          // 16 KB
+constexpr uint32_t SP_STAGE_BYTES = 2 * SP_A_BYTES + 2 * SP_B_BYTES;        // 48 KB
 constexpr uint32_t SP_SMEM = SP_STAGES * SP_STAGE_BYTES + 1024 + 256;       // + alignment + barriers
+constexpr uint32_t SP_TMEM_COLS = 2 * SP_BN;                                 // two accumulators
 constexpr long long SP_WAIT_CYCLES = 1ll << 31;                              // ~1 s
 
 // ---------------------------------------------------------------- PTX helpers
@@ -86,16 +90,22 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart.
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle (64-byte rows),
+// 8-row groups 512 B apart.
 __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
 {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFF) >> 4);  // start address
     d |= (uint64_t)1 << 16;                   // leading byte offset (unused for this layout)
-    d |= (uint64_t)(1024 >> 4) << 32;         // stride byte offset
+    d |= (uint64_t)(512 >> 4) << 32;          // stride byte offset
     d |= (uint64_t)1 << 46;                   // descriptor version
-    d |= (uint64_t)2 << 61;                   // 128-byte swizzle
+    d |= (uint64_t)4 << 61;                   // 64-byte swizzle
     return d;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 // Instruction descriptor, kind::f16: D = F32, A = B = F16, both K-major, M = 128, N = 256.
@@ -233,8 +243,8 @@ __global__ void k_split_y(int UV, int UVpad, int Kpad, const int2 *__restrict__ 
 
 // ------------------------------------------------------------------ the GEMM
 struct LiftArgs {
-    const int2 *tiles;        // (u tile, vt tile)
-    int nK, U, UV;
+    const int2 *tiles;        // (u tile, vt tile), vt-major
+    int ntiles, nK, U, UV;
     const int2 *vt_pairs;     // [UV]
     const long long *vt_off;  // [UV] offset of row (v,t) in Tsym
     const double *sx_inv, *sy_inv;
@@ -242,6 +252,8 @@ struct LiftArgs {
     int *err;
 };
 
+// Persistent: CTA b takes tiles b, b + grid, ...; the MMA warp fills one TMEM
+// accumulator while the epilogue warps drain the other.
 __global__ void __launch_bounds__(192, 1) k_gamma_lift(const __grid_constant__ CUtensorMap tmX1,
                                                       const __grid_constant__ CUtensorMap tmX2,
                                                       const __grid_constant__ CUtensorMap tmY1,
@@ -250,28 +262,30 @@ __global__ void __launch_bounds__(192, 1) k_gamma_lift(const __grid_constant__ C
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + SP_STAGES * SP_STAGE_BYTES);
-    // bars[0..1] full, bars[2..3] empty, bars[4] done
-    volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(bars + 8);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 9);
+    // bars[0..S) full, [S..2S) empty, [2S..2S+2) accumulator full, [2S+2..2S+4) accumulator empty
+    uint64_t *full = bars, *empty = bars + SP_STAGES, *afull = bars + 2 * SP_STAGES, *aempty = afull + 2;
+    volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(bars + 2 * SP_STAGES + 4);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 2 * SP_STAGES + 5);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int2 tile = a.tiles[blockIdx.x];
-    const int u0 = tile.x * SP_BM, vt0 = tile.y * SP_BN;
     const int nK = a.nK;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < SP_STAGES; s++) {
-            mbar_init(smem_u32(&bars[s]), 1);
-            mbar_init(smem_u32(&bars[2 + s]), 1);
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
         }
-        mbar_init(smem_u32(&bars[4]), 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&afull[b]), 1);
+            mbar_init(smem_u32(&aempty[b]), 4);  // one arrival per epilogue warp
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32((const void *)tmem_slot)),
-                     "r"(SP_BN)
+                     "r"(SP_TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -282,79 +296,106 @@ __global__ void __launch_bounds__(192, 1) k_gamma_lift(const __grid_constant__ C
 
     if (warp == 0) {
         if (lane == 0) {
-            int issued = 0;
-            for (int kc = 0; kc < nK; kc++) {
-                const int s = kc % SP_STAGES, it = kc / SP_STAGES;
-                if (it > 0 && !mbar_wait(smem_u32(&bars[2 + s]), (it - 1) & 1, abort_flag)) {
-                    if (!*abort_flag) { *abort_flag = 1; atomicCAS(a.err, 0, 1); }
-                    break;
+            long g = 0;
+            for (int t = blockIdx.x; t < a.ntiles && !*abort_flag; t += gridDim.x) {
+                const int2 tile = a.tiles[t];
+                const int u0 = tile.x * SP_BM, vt0 = tile.y * SP_BN;
+                for (int kc = 0; kc < nK; kc++, g++) {
+                    const int s = (int)(g % SP_STAGES);
+                    const long it = g / SP_STAGES;
+                    if (it > 0 && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((it - 1) & 1), abort_flag)) {
+                        if (!*abort_flag) { *abort_flag = 1; atomicCAS(a.err, 0, 1); }
+                        break;
+                    }
+                    uint8_t *st = smem + (size_t)s * SP_STAGE_BYTES;
+                    const uint32_t fb = smem_u32(&full[s]);
+                    mbar_expect_tx(fb, SP_STAGE_BYTES);
+                    tma_load_2d(smem_u32(st), &tmX1, kc * SP_BK, u0, fb);
+                    tma_load_2d(smem_u32(st + SP_A_BYTES), &tmX2, kc * SP_BK, u0, fb);
+                    tma_load_2d(smem_u32(st + 2 * SP_A_BYTES), &tmY1, kc * SP_BK, vt0, fb);
+                    tma_load_2d(smem_u32(st + 2 * SP_A_BYTES + SP_B_BYTES), &tmY2, kc * SP_BK, vt0, fb);
                 }
-                uint8_t *st = smem + (size_t)s * SP_STAGE_BYTES;
-                const uint32_t full = smem_u32(&bars[s]);
-                mbar_expect_tx(full, SP_STAGE_BYTES);
-                tma_load_2d(smem_u32(st), &tmX1, kc * SP_BK, u0, full);
-                tma_load_2d(smem_u32(st + SP_A_BYTES), &tmX2, kc * SP_BK, u0, full);
-                tma_load_2d(smem_u32(st + 2 * SP_A_BYTES), &tmY1, kc * SP_BK, vt0, full);
-                tma_load_2d(smem_u32(st + 2 * SP_A_BYTES + SP_B_BYTES), &tmY2, kc * SP_BK, vt0, full);
-                issued = kc + 1;
             }
-            // drain: copies still in flight into stages nobody will consume
-            for (int kc = (issued > SP_STAGES ? issued - SP_STAGES : 0); kc < issued; kc++) {
-                const int s = kc % SP_STAGES, it = kc / SP_STAGES;
+            // drain: wait for the copies of the last stages to land before the CTA can exit
+            for (long h = (g > SP_STAGES ? g - SP_STAGES : 0); h < g; h++) {
+                const int s = (int)(h % SP_STAGES);
                 long long t0 = clock64();
-                while (!mbar_try(smem_u32(&bars[s]), it & 1) && clock64() - t0 < SP_WAIT_CYCLES) {
+                while (!mbar_try(smem_u32(&full[s]), (uint32_t)((h / SP_STAGES) & 1)) && clock64() - t0 < SP_WAIT_CYCLES) {
                 }
             }
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            for (int kc = 0; kc < nK; kc++) {
-                const int s = kc % SP_STAGES, it = kc / SP_STAGES;
-                if (!mbar_wait(smem_u32(&bars[s]), it & 1, abort_flag)) {
-                    if (!*abort_flag) { *abort_flag = 1; atomicCAS(a.err, 0, 2); }
+            long g = 0;
+            int tl = 0;
+            for (int t = blockIdx.x; t < a.ntiles && !*abort_flag; t += gridDim.x, tl++) {
+                const int acc = tl & 1, use = tl >> 1;
+                if (use > 0 && !mbar_wait(smem_u32(&aempty[acc]), (uint32_t)((use - 1) & 1), abort_flag)) {
+                    if (!*abort_flag) { *abort_flag = 1; atomicCAS(a.err, 0, 4); }
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t st = smem_u32(smem + (size_t)s * SP_STAGE_BYTES);
-                const uint32_t x1 = st, x2 = st + SP_A_BYTES, y1 = st + 2 * SP_A_BYTES, y2 = y1 + SP_B_BYTES;
+                const uint32_t d = tmem + (uint32_t)(acc * SP_BN);
+                for (int kc = 0; kc < nK; kc++, g++) {
+                    const int s = (int)(g % SP_STAGES);
+                    const long it = g / SP_STAGES;
+                    if (!mbar_wait(smem_u32(&full[s]), (uint32_t)(it & 1), abort_flag)) {
+                        if (!*abort_flag) { *abort_flag = 1; atomicCAS(a.err, 0, 2); }
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t st = smem_u32(smem + (size_t)s * SP_STAGE_BYTES);
+                    const uint32_t x1 = st, x2 = st + SP_A_BYTES, y1 = st + 2 * SP_A_BYTES, y2 = y1 + SP_B_BYTES;
 #pragma unroll
-                for (int kk = 0; kk < SP_BK / 16; kk++) {
-                    const uint32_t o = kk * 32;  // 16 FP16 = 32 bytes along the swizzled row
-                    umma_f16(tmem, umma_desc(x1 + o), umma_desc(y1 + o), (kc | kk) != 0);
-                    umma_f16(tmem, umma_desc(x1 + o), umma_desc(y2 + o), 1);
-                    umma_f16(tmem, umma_desc(x2 + o), umma_desc(y1 + o), 1);
+                    for (int kk = 0; kk < SP_BK / 16; kk++) {
+                        const uint32_t o = kk * 32;  // 16 FP16 = 32 bytes along the swizzled row
+                        umma_f16(d, umma_desc(x1 + o), umma_desc(y1 + o), (kc | kk) != 0);
+                        umma_f16(d, umma_desc(x1 + o), umma_desc(y2 + o), 1);
+                        umma_f16(d, umma_desc(x2 + o), umma_desc(y1 + o), 1);
+                    }
+                    umma_commit(smem_u32(&empty[s]));  // frees the stage when these MMAs finish
                 }
-                umma_commit(smem_u32(&bars[2 + s]));  // frees the stage when these MMAs finish
+                umma_commit(smem_u32(&afull[acc]));  // this tile's accumulator is complete
             }
-            umma_commit(smem_u32(&bars[4]));  // accumulator complete
         }
     } else {
         // epilogue: warps 2..5 own TMEM lanes 32*(warp % 4) .. +31
-        const bool ok = mbar_wait(smem_u32(&bars[4]), 0, abort_flag);
-        if (!ok && !*abort_flag) { *abort_flag = 1; atomicCAS(a.err, 0, 3); }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (ok) {
-            const int lb = (warp & 3) * 32;
+        const int lb = (warp & 3) * 32;
+        int tl = 0;
+        for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x, tl++) {
+            const int acc = tl & 1, use = tl >> 1;
+            const bool ok = mbar_wait(smem_u32(&afull[acc]), (uint32_t)(use & 1), abort_flag);
+            if (!ok) {
+                if (!*abort_flag) { *abort_flag = 1; atomicCAS(a.err, 0, 3); }
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int2 tile = a.tiles[t];
+            const int u0 = tile.x * SP_BM, vt0 = tile.y * SP_BN;
             const int u = u0 + lb + lane;
             const double su = (u < a.U) ? a.sx_inv[u] : 0.0;
             for (int c0 = 0; c0 < SP_BN; c0 += 32) {
                 float v[32];
-                tmem_ld32(tmem + ((uint32_t)lb << 16) + (uint32_t)c0, v);
-#pragma unroll 4
+                tmem_ld32(tmem + ((uint32_t)lb << 16) + (uint32_t)(acc * SP_BN + c0), v);
+#pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const int vt = vt0 + c0 + j;
-                    if (vt >= a.UV) break;
-                    const int2 p = a.vt_pairs[vt];
-                    if (u <= p.x) a.Tsym[a.vt_off[vt] + u] = (float)((double)v[j] * su * a.sy_inv[vt]);
+                    if (vt < a.UV) {
+                        const int2 p = a.vt_pairs[vt];
+                        if (u <= p.x) a.Tsym[a.vt_off[vt] + u] = (float)((double)v[j] * su * a.sy_inv[vt]);
+                    }
                 }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&aempty[acc]));
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 1) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(SP_BN) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(SP_TMEM_COLS) : "memory");
     }
 }
 
@@ -416,7 +457,7 @@ static modal_status get_encode()
     return MODAL_OK;
 }
 
-// 2D FP16 map over [rows][Kpad], box [box_rows][64], 128-byte swizzle.
+// 2D FP16 map over [rows][Kpad], box [box_rows][32], 64-byte swizzle.
 static modal_status make_map(CUtensorMap *m, const void *base, long rows, int Kpad, int box_rows)
 {
     cuuint64_t dims[2] = {(cuuint64_t)Kpad, (cuuint64_t)rows};
@@ -424,7 +465,7 @@ static modal_status make_map(CUtensorMap *m, const void *base, long rows, int Kp
     cuuint32_t box[2] = {(cuuint32_t)SP_BK, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = g_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) { set_error("cuTensorMapEncodeTiled failed (%d)", (int)r); return MODAL_ERR_CUDA; }
     return MODAL_OK;
@@ -444,7 +485,7 @@ modal_status gamma_split_dev(modal_ctx *ctx)
     const int Upad = ceil_div(U, SP_BM) * SP_BM;
     const long UV = (long)U * (U + 1) / 2;
     const long UVpad = (long)ceil_div(UV, SP_BN) * SP_BN;
-    const int Kpad = ceil_div(nmu, SP_BK) * SP_BK;
+    const int Kpad = ceil_div(nmu, SP_KPAD) * SP_KPAD;
     const long long ntsym = (long long)U * (U + 1) * (U + 2) / 6;
 
     // host tables: pairs, pair index, vt pairs and offsets, tile list
@@ -530,6 +571,7 @@ modal_status gamma_split_dev(modal_ctx *ctx)
     MODAL_TRY(make_map(&my2, Y2, UVpad, Kpad, SP_BN));
     LiftArgs la;
     la.tiles = reinterpret_cast<const int2 *>(b + o_tiles);
+    la.ntiles = (int)tiles.size();
     la.nK = Kpad / SP_BK;
     la.U = U;
     la.UV = (int)UV;
@@ -540,8 +582,14 @@ modal_status gamma_split_dev(modal_ctx *ctx)
     la.Tsym = Tsym;
     la.err = err;
     MODAL_CUDA(cudaFuncSetAttribute(k_gamma_lift, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SP_SMEM));
-    k_gamma_lift<<<(unsigned)tiles.size(), 192, SP_SMEM, ctx->stream>>>(mx1, mx2, my1, my2, la);
-    MODAL_TRY(launched(ctx, "gamma_lift"));
+    int nsm = 0;
+    MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int grid = (int)std::min<long>((long)tiles.size(), (long)(nsm > 0 ? nsm : 1));
+    {
+        StageTimer tl(ctx, MODAL_T_LIFT);
+        k_gamma_lift<<<grid, 192, SP_SMEM, ctx->stream>>>(mx1, mx2, my1, my2, la);
+        MODAL_TRY(launched(ctx, "gamma_lift"));
+    }
 
     MODAL_TRY(ensure(ctx->gamma, sizeof(double) * (size_t)N * N));
     size_t gsm = (size_t)U * 8 + (size_t)P * P * 4;

@@ -267,10 +267,17 @@ modal_status cholesky_dev(modal_ctx *ctx, int *fail_row)
     const int big = INT_MAX;
     MODAL_CUDA(cudaFuncSetAttribute(k_trsm_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRI_SMEM));
     MODAL_CUDA(cudaMemcpyAsync(info, &big, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    int h = INT_MAX;
     for (int kb = 0; kb < N; kb += NB) {
         int nb = (N - kb < NB) ? (N - kb) : NB;
         k_potrf_diag<<<1, 256, 0, ctx->stream>>>(A, N, kb, nb, info);
         MODAL_TRY(launched(ctx, "potrf_diag"));
+        // every 4 panels: stop early once a pivot has failed (the PCA branch follows)
+        if ((kb / NB) % 4 == 3) {
+            MODAL_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (h != INT_MAX) break;
+        }
         int rest = N - kb - nb;
         if (rest > 0) {
             k_trsm_panel<<<ceil_div(rest, 64), 64, TRI_SMEM, ctx->stream>>>(A, N, kb, nb);
@@ -280,7 +287,6 @@ modal_status cholesky_dev(modal_ctx *ctx, int *fail_row)
             MODAL_TRY(dgemm(ctx, rest, rest, nb, -1.0, A21, N, false, A21, N, true, 1.0, A22, N, 1));
         }
     }
-    int h = 0;
     MODAL_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
     *fail_row = (h == INT_MAX) ? -1 : h;

@@ -33,7 +33,7 @@ EXPORTS = [
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc",
 ]
 
-TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6}
+TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7}
 
 
 class ModalError(RuntimeError):

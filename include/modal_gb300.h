@@ -174,6 +174,21 @@ modal_status modal_set_spectrum(modal_ctx *ctx, const double *cl);
 modal_status modal_project(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec,
                            double *beta);
 
+/* modify_bispectrum (calculate_modes.c:6-45) on the GPU, in place on the host
+ * array b[size][size][size]: b <- c_i c_j c_k h~^2(l_i,l_j,l_k) (1.55e-8)^2 b on
+ * even-parity triangle triples (l = vec[index]), 0 elsewhere;
+ * c_i = beam_i / ((2 l_i + 1)^{1/6} sqrt(beam_i^2 cl_i + noise_i)) when cl_i != 0
+ * and l_i != 0.  cl, beam, noise, vec: [size], indexed like b. */
+modal_status modal_modify_bispectrum(int size, const int *vec, const double *cl, const double *beam,
+                                     const double *noise, double *b);
+
+/* calculate_modes (calculate_modes.c:47-79) for every mode at once:
+ * beta[r] = sum over i <= j <= k < size of m(i,j,k) plijk_TTT(r,i,j,k) b[i][j][k]
+ * (m = 1, 3, 6 orderings; the array index is the multipole l, as in the
+ * reference).  b: host [size][size][size], typically after
+ * modal_modify_bispectrum.  beta: host [N] or NULL (kept for modal_alpha). */
+modal_status modal_calculate_modes(modal_ctx *ctx, int size, const double *b, double *beta);
+
 /* alpha = lambdal^T lambdal beta and modesR = orthol^T alpha
  * (eigenmodetoday_mpi.c:148-162, 286-316) for S shapes, FP64 on the GPU.
  * beta: host [S][N] or NULL for the device result of modal_project.

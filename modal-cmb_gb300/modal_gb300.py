@@ -30,7 +30,7 @@ EXPORTS = [
     "modal_tetrapyd_count", "modal_set_basis", "modal_set_modes", "modal_set_gl", "modal_init_glint",
     "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_orthol_pair", "modal_orthogonalise",
     "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
-    "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc",
+    "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7}
@@ -86,6 +86,8 @@ def lib():
             "modal_ctx_timer": (i, [vp, i, ctypes.POINTER(d), ctypes.POINTER(l)]),
             "modal_ctx_timer_reset": (i, [vp]),
             "modal_gamma_fp64_noalloc": (i, [i, i, i, vp, i, vp, i, vp, vp, vp, vp]),
+            "modal_modify_bispectrum": (i, [i, vp, vp, vp, vp, vp]),
+            "modal_calculate_modes": (i, [vp, i, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -144,6 +146,18 @@ def tetrapyd_count(lmin, lmax):
     n = ctypes.c_long()
     _check(lib().modal_tetrapyd_count(lmin, lmax, ctypes.byref(n)))
     return n.value
+
+
+def modify_bispectrum(b, vec, cl, beam=None, noise=None):
+    """modify_bispectrum on the GPU; returns the modified copy of b[size][size][size]."""
+    b = np.array(b, dtype=np.float64, order="C", copy=True)
+    size = b.shape[0]
+    vec = np.ascontiguousarray(vec, dtype=np.int32)
+    cl = _f64(cl)
+    beam = np.ones(size) if beam is None else _f64(beam)
+    noise = np.zeros(size) if noise is None else _f64(noise)
+    _check(lib().modal_modify_bispectrum(size, _ptr(vec), _ptr(cl), _ptr(beam), _ptr(noise), _ptr(b)))
+    return b
 
 
 def shapes_to_c(shapes):
@@ -273,6 +287,12 @@ class Context:
         out = np.empty((len(shapes), self.N)) if download else None
         _check(lib().modal_project(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), prec, _ptr(out)))
         del keep
+        return out
+
+    def calculate_modes(self, b):
+        b = _f64(b)
+        out = np.empty(self.N)
+        _check(lib().modal_calculate_modes(self.h, b.shape[0], _ptr(b), _ptr(out)))
         return out
 
     def alpha(self, S, beta=None, download=True):

@@ -455,3 +455,54 @@ int orc_alpha(int N, const double *orthol, const double *lambdal, const double *
     free(orthoinv);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Serial dense form (calculate_modes.c:6-79).                                */
+/* modify_bispectrum: b[i][j][k] <- c_i c_j c_k h~^2(l) (1.55e-8)^2 b on even */
+/* triangle triples of l = vec[index], else 0; c_i = beam_i / ((2l_i+1)^{1/6}  */
+/* sqrt(beam_i^2 cl_i + noise_i)) when cl_i != 0 and vec_i != 0.               */
+/* calculate_modes: beta_r = sum_{i<=j<=k<size, b != 0} m plijk(r,i,j,k) b,    */
+/* m = 1, 3, 6 by coinciding indices; the index is used as l.                 */
+/* ------------------------------------------------------------------------ */
+int orc_modify_bispectrum(int size, const int *vec, const double *cl, const double *beam, const double *noise,
+                          double *b)
+{
+    double *c = malloc(sizeof(double) * (size_t)size);
+    for (int i = 0; i < size; i++) {
+        c[i] = 0;
+        if (cl[i] != 0 && vec[i] != 0)
+            c[i] = beam[i] / (pow(2.0 * vec[i] + 1.0, 1.0 / 6.0) * sqrt(beam[i] * beam[i] * cl[i] + noise[i]));
+    }
+    for (int i = 0; i < size; i++)
+        for (int j = 0; j < size; j++)
+            for (int k = 0; k < size; k++) {
+                int a = vec[i], bb = vec[j], cc = vec[k];
+                double *v = b + ((long)i * size + j) * size + k;
+                if (((a + bb + cc) % 2) == 0 && a + bb >= cc && bb + cc >= a && cc + a >= bb)
+                    *v = c[i] * c[j] * c[k] * orc_geometric(a, bb, cc) * (*v * 1.55e-8 * 1.55e-8);
+                else
+                    *v = 0.0;
+            }
+    free(c);
+    return 0;
+}
+
+int orc_calculate_modes(int lmin, int lmax, int P, const double *basis, int N, const int *triples, int size,
+                        const double *b, double *beta)
+{
+    #pragma omp parallel for schedule(dynamic, 1)
+    for (int r = 0; r < N; r++) {
+        double result = 0.0;
+        for (int i = 0; i < size; i++)
+            for (int j = i; j < size; j++)
+                for (int k = j; k < size; k++) {
+                    double v = b[((long)i * size + j) * size + k];
+                    if (v != 0.0) {
+                        double f = (i == j && j == k) ? 1.0 : ((i == j || j == k) ? 3.0 : 6.0);
+                        result += f * plijk(basis, P, triples + 3 * r, lmin, lmax, i, j, k) * v;
+                    }
+                }
+        beta[r] = result;
+    }
+    return 0;
+}

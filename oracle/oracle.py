@@ -83,6 +83,8 @@ class Oracle:
             ("orc_project", i, [i, i, i, vp, i, vp, vp, i, i, vp, d, d, d, d, i, l, vp]),
             ("orc_ortho_cholesky", l, [i, vp, vp, vp]),
             ("orc_alpha", i, [i, vp, vp, vp, vp, vp]),
+            ("orc_modify_bispectrum", i, [i, vp, vp, vp, vp, vp]),
+            ("orc_calculate_modes", i, [i, i, i, vp, i, vp, i, vp, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -159,6 +161,25 @@ class Oracle:
                            _p(beta))
         return beta
 
+    def modify_bispectrum(self, b, vec, cl, beam=None, noise=None):
+        b = np.array(b, dtype=np.float64, order="C", copy=True)
+        size = b.shape[0]
+        vec = np.ascontiguousarray(vec, dtype=np.int32)
+        beam = np.ones(size) if beam is None else np.ascontiguousarray(beam, dtype=np.float64)
+        noise = np.zeros(size) if noise is None else np.ascontiguousarray(noise, dtype=np.float64)
+        cl = np.ascontiguousarray(cl[:size], dtype=np.float64)
+        self.L.orc_modify_bispectrum(size, _p(vec), _p(cl), _p(beam), _p(noise), _p(b))
+        return b
+
+    def calculate_modes(self, lmin, lmax, q, triples, b):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        triples = np.ascontiguousarray(triples, dtype=np.int32)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        beta = np.empty(triples.shape[0])
+        self.L.orc_calculate_modes(lmin, lmax, q.shape[1], _p(q), triples.shape[0], _p(triples), b.shape[0], _p(b),
+                                   _p(beta))
+        return beta
+
     def ortho_cholesky(self, gamma):
         """Cholesky branch; returns (orthol, lambdal, fail) with fail = -1 or the failing pivot row."""
         g = np.ascontiguousarray(gamma, dtype=np.float64)
@@ -219,6 +240,8 @@ class Ref:
             ("ref_tetrapyd_walk", l, [i, i, l, vp]),
             ("ref_decompose", i, [i, i, i, vp]),
             ("ref_project", i, [i, i, i, vp, d, d, d, d, l, vp]),
+            ("ref_modify_bispectrum", i, [i, vp, vp]),
+            ("ref_calculate_modes", i, [i, vp, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -267,6 +290,19 @@ class Ref:
         with quiet_stdout():
             self.L.ref_decompose(nthreads, lmin, lmax, _p(out))
         return out
+
+    def modify_bispectrum(self, b, vec):
+        b = np.array(b, dtype=np.float64, order="C", copy=True)
+        vec = np.ascontiguousarray(vec, dtype=np.int32)
+        self.L.ref_modify_bispectrum(b.shape[0], _p(vec), _p(b))
+        return b
+
+    def calculate_modes(self, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        beta = np.empty(self.N)
+        with quiet_stdout():
+            self.L.ref_calculate_modes(b.shape[0], _p(b), _p(beta))
+        return beta
 
     def project(self, shape, nthreads=8, max_points=0):
         beta = np.empty(self.N)

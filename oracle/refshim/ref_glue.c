@@ -263,3 +263,37 @@ int ref_project(int nthreads, int kind, int nterms, const double *tab, double c1
     free(b);
     return 0;
 }
+
+/* ---- serial dense form: modify_bispectrum + calculate_modes (calculate_modes.c:6-79) ---- */
+extern void modify_bispectrum(int size, int *vec, double ***bispectrum);
+extern double calculate_modes(int r, int size, double ***bispectrum);
+
+static double ***view3(int size, double *flat)
+{
+    double ***b = malloc(sizeof(double **) * (size_t)size);
+    double **rows = malloc(sizeof(double *) * (size_t)size * size);
+    for (int i = 0; i < size; i++) {
+        b[i] = rows + (size_t)i * size;
+        for (int j = 0; j < size; j++) b[i][j] = flat + ((size_t)i * size + j) * size;
+    }
+    return b;
+}
+
+static void free_view3(double ***b) { free(b[0]); free(b); }
+
+/* In place on flat[size^3]; the spectrum installed by ref_setup is indexed by i. */
+int ref_modify_bispectrum(int size, const int *vec, double *flat)
+{
+    double ***b = view3(size, flat);
+    modify_bispectrum(size, (int *)vec, b);
+    free_view3(b);
+    return 0;
+}
+
+int ref_calculate_modes(int size, double *flat, double *beta)
+{
+    double ***b = view3(size, flat);
+    for (int r = 0; r < g_N; r++) beta[r] = calculate_modes(r, size, b);
+    free_view3(b);
+    return 0;
+}

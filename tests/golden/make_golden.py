@@ -25,6 +25,14 @@ def inputs_digest(q, tr, cl):
     return np.array([q.sum(), (q * q).sum(), tr.sum(), cl.sum()])
 
 
+def dense_input(size):
+    """Seeded-free smooth test bispectrum for the serial dense form (also rebuilt by the tests)."""
+    l = np.arange(size, dtype=np.float64)
+    l[0] = 1.0
+    raw = np.einsum("i,j,k->ijk", l ** -1.2, l ** -0.7, l ** -1.5)
+    return (raw + raw.transpose(1, 2, 0) + raw.transpose(2, 0, 1)) / 3.0
+
+
 def main():
     ref = O.Ref()
     # 1. asy() Gauss-Legendre nodes/weights
@@ -52,7 +60,18 @@ def main():
     np.savez_compressed(os.path.join(OUT, "tetrapyd.npz"), walk=walk[:400], walk_count=n, decompose=dec,
                         **{"count_" + k: v for k, v in counts.items()})
 
-    # 5. Gamma (calculate_orthol over all pairs) and projection beta
+    # 5. serial dense form: modify_bispectrum + calculate_modes at size 41 (l = index),
+    #    basis for l = 2..40, P = 4; input: a seeded smooth bispectrum
+    lmax, P, size = 40, 4, 41
+    q, tr, cl = M.workload(lmax, P)
+    ref.setup(2, lmax, q, tr, cl)
+    raw = dense_input(size)
+    vec = np.arange(size, dtype=np.int32)
+    mod = ref.modify_bispectrum(raw, vec)
+    beta = ref.calculate_modes(mod)
+    np.savez_compressed(os.path.join(OUT, "modes_dense.npz"), modified=mod, beta=beta, lmax=lmax, P=P)
+
+    # 6. Gamma (calculate_orthol over all pairs) and projection beta
     #    small: lmax=60, P=4; config 1: lmax=500, P=10 (220 modes)
     for name, lmax, P, S in [("small", 60, 4, 4), ("cfg1", 500, 10, 4)]:
         q, tr, cl = M.workload(lmax, P)

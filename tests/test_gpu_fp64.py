@@ -289,3 +289,42 @@ def test_full_pipeline_on_device(mg, golden):
         d = a[s] - ref
         assert np.sqrt(abs(d @ G @ d)) <= 1e-8 * np.sqrt(abs(ref @ G @ ref))
     assert n0 > 10
+
+
+# ------------------------------------------------------- serial dense form
+
+def _dense_raw(size):
+    l = np.arange(size, dtype=np.float64)
+    l[0] = 1.0
+    raw = np.einsum("i,j,k->ijk", l ** -1.2, l ** -0.7, l ** -1.5)
+    return (raw + raw.transpose(1, 2, 0) + raw.transpose(2, 0, 1)) / 3.0
+
+
+def test_dense_form_vs_reference(mg, golden):
+    """modify_bispectrum + calculate_modes on the GPU vs the in-place reference (golden)."""
+    g = golden("modes_dense")
+    lmax, P = int(g["lmax"]), int(g["P"])
+    size = g["modified"].shape[0]
+    q, tr, cl = mg.workload(lmax, P)
+    mod = mg.modify_bispectrum(_dense_raw(size), np.arange(size), cl[:size])
+    nz = g["modified"] != 0
+    assert np.array_equal(mod != 0, nz)
+    assert np.max(np.abs(mod[nz] - g["modified"][nz]) / np.abs(g["modified"][nz])) <= 1e-14
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        beta = c.calculate_modes(g["modified"])
+    assert rel_fro(beta, g["beta"]) <= 1e-12
+
+
+def test_dense_form_vs_oracle_larger(mg, orc):
+    """size beyond lmax (indices above lmax contribute nothing) and P = 6."""
+    lmax, P, size = 70, 6, 81
+    q, tr, cl = mg.workload(lmax, P)
+    cl_ext = np.concatenate([cl, np.full(size - cl.size, cl[-1])])
+    mod = mg.modify_bispectrum(_dense_raw(size), np.arange(size), cl_ext)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        beta = c.calculate_modes(mod)
+    assert rel_fro(beta, orc.calculate_modes(2, lmax, q, tr, mod)) <= 1e-12

@@ -165,3 +165,22 @@ def test_alpha_restatement(orc):
     a, mR = orc.alpha(o, lam, beta)
     assert np.allclose(a, np.linalg.solve(G, beta), rtol=1e-10)
     assert np.allclose(mR, lam @ beta, rtol=1e-10, atol=1e-12)
+
+
+def test_dense_form_matches_reference(orc, golden, mg):
+    """modify_bispectrum + calculate_modes (calculate_modes.c:6-79) vs the in-place reference."""
+    import numpy as np
+    g = golden("modes_dense")
+    lmax, P = int(g["lmax"]), int(g["P"])
+    size = g["modified"].shape[0]
+    q, tr, cl = mg.workload(lmax, P)
+    l = np.arange(size, dtype=np.float64)
+    l[0] = 1.0
+    raw = np.einsum("i,j,k->ijk", l ** -1.2, l ** -0.7, l ** -1.5)
+    raw = (raw + raw.transpose(1, 2, 0) + raw.transpose(2, 0, 1)) / 3.0
+    mod = orc.modify_bispectrum(raw, np.arange(size), cl)
+    nz = g["modified"] != 0
+    assert np.array_equal(mod != 0, nz)
+    assert np.max(np.abs(mod[nz] - g["modified"][nz]) / np.abs(g["modified"][nz])) <= 1e-14
+    beta = orc.calculate_modes(2, lmax, q, tr, g["modified"])
+    assert rel_fro(beta, g["beta"]) <= 1e-13

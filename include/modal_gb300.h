@@ -189,6 +189,21 @@ modal_status modal_modify_bispectrum(int size, const int *vec, const double *cl,
  * modal_modify_bispectrum.  beta: host [N] or NULL (kept for modal_alpha). */
 modal_status modal_calculate_modes(modal_ctx *ctx, int size, const double *b, double *beta);
 
+/* Late x primordial transfer Gamma (calculate_gamma.c, default path of
+ * gamma_mpi.c: init_gamma_glint :48-250, precompute_gammaMij_T :254-303,
+ * gamma_2d_pt_TTT :512-555, calculate_gamma_2d :773-842 with
+ * integrate_cubic_spline :845-934).  Install the radial grid xvec[xsize]
+ * (increasing, xsize >= 4), the raw transfer functions
+ * qtilde[xsize][Pp][lmax+1] = q~_p(l, x) (get_qtilde_T(p, l, x)) and the
+ * primordial mode triples prim[Nprim][3] (find_perm_prim). */
+modal_status modal_set_transfer(modal_ctx *ctx, int Pp, int xsize, const double *xvec, const double *qtilde,
+                                int Nprim, const int *prim);
+
+/* gamma_t[m][n] = calculate_gamma_2d(m, n)[0] for every late mode m < N and
+ * primordial mode n < Nprim, with weight (2l+1)^{5/6}/sqrt(C_l + N_l/b_l^2)
+ * from modal_set_spectrum and scale deltaphi^2/(8 pi).  FP64 on the GPU. */
+modal_status modal_gamma_transfer(modal_ctx *ctx, double deltaphi, double *gamma_t);
+
 /* alpha = lambdal^T lambdal beta and modesR = orthol^T alpha
  * (eigenmodetoday_mpi.c:148-162, 286-316) for S shapes, FP64 on the GPU.
  * beta: host [S][N] or NULL for the device result of modal_project.

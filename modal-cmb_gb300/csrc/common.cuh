@@ -61,6 +61,15 @@ struct modal_ctx {
     modal::DevBuf split;       // split-precision Gamma: operand pieces, T table, per-P tables
     int split_P = -1;          // P the per-P tables in `split` were built for
     int gl_n = -1;             // n of the GPU quadrature held in mu/w (-1: none or caller-supplied)
+
+    // late x primordial transfer Gamma
+    int tr_Pp = 0, tr_xsize = 0, tr_Nprim = 0;
+    modal::DevBuf tr_x;        // [xsize] grid, then [xsize] spline weights
+    modal::DevBuf tr_qt;       // [xsize][Pp][lmax+1] transfer functions
+    modal::DevBuf tr_prim;     // [Nprim][3]
+    modal::DevBuf tr_mt;       // [xsize][nmu][Pp][P]
+    modal::DevBuf tr_v;        // [lmax+1] weights
+    modal::DevBuf tr_out;      // [N][Nprim]
     double *h_info = nullptr;  // pinned readback
 
     // profiling: event pairs per stage, summed on read

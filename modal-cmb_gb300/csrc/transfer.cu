@@ -1,0 +1,270 @@
+// transfer.cu -- late x primordial transfer Gamma, FP64 on the GPU.
+//
+// Default path of gamma_mpi.c (calculate_gamma.c):
+//   TTweight_l = (2l+1)^{5/6} b_l / sqrt(b_l^2 C_l + N_l)                     (:76-88)
+//   M[p][q][x][k] = sum_l P_l(mu_k) TTweight_l q~_p(l,x) q_q(l)                (:254-303)
+//   g(m,n,x)      = sum_k w_k perm3(M[p_a][q_b][x][k]), (p) = prim triple of n,
+//                   (q) = late triple of m                                       (:512-555)
+//   y_x = x^2 g(m,n,x), set to 0 at the first 10 grid points when |y| > 1e-18
+//   Gamma_t[m][n] = integrate_cubic_spline(x, y) dphi^2 / (8 pi)                 (:773-934)
+// The spline integral is linear in y for fixed nodes: I(y) = sum_x c_x y_x with
+// c_x the integral of the spline through the unit vector e_x, computed once on
+// the host with the reference's own spline recurrences.  The kernel folds the
+// x loop and that weighted sum into one pass per (m, n) tile.
+// Device layouts: qt[x][p][l] (l = 0..lmax), mt2[x][k][p][q] (mu-major per x).
+#include <cmath>
+#include <vector>
+#include "common.cuh"
+
+namespace modal {
+
+// Integral over [x0, x_{n-1}] of the cubic spline of integrate_cubic_spline
+// (calculate_gamma.c:845-934) through (x, y).
+static double spline_integral(const double *x, const double *y, int n)
+{
+    if (n < 2) return 0.0;
+    std::vector<double> a(n, 0.0), b(n, 0.0), c(n, 0.0);
+    c[0] = x[1] - x[0];
+    b[1] = (y[1] - y[0]) / c[0];
+    for (int i = 1; i < n - 1; i++) {
+        c[i] = x[i + 1] - x[i];
+        a[i] = 2.0 * (c[i - 1] + c[i]);
+        b[i + 1] = (y[i + 1] - y[i]) / c[i];
+        b[i] = b[i + 1] - b[i];
+    }
+    a[0] = -c[0];
+    a[n - 1] = -c[n - 2];
+    b[0] = 0.0;
+    b[n - 1] = 0.0;
+    if (n > 2) {
+        b[0] = b[2] / (x[3] - x[1]) - b[1] / (x[2] - x[0]);
+        b[n - 1] = b[n - 2] / (x[n - 1] - x[n - 3]) - b[n - 3] / (x[n - 2] - x[n - 4]);
+        b[0] = b[0] * c[0] * c[0] / (x[3] - x[0]);
+        b[n - 1] = -b[n - 1] * c[n - 2] * c[n - 2] / (x[n - 1] - x[n - 4]);
+    }
+    for (int i = 1; i < n; i++) {
+        double h = c[i - 1] / a[i - 1];
+        a[i] -= h * c[i - 1];
+        b[i] -= h * b[i - 1];
+    }
+    b[n - 1] /= a[n - 1];
+    for (int i = n - 2; i >= 0; i--) b[i] = (b[i] - c[i] * b[i + 1]) / a[i];
+    for (int i = 0; i < n - 1; i++) {
+        a[i] = (y[i + 1] - y[i]) / c[i] - c[i] * (b[i + 1] + 2.0 * b[i]);
+        c[i] = (b[i + 1] - b[i]) / c[i];
+        b[i] = 3.0 * b[i];
+    }
+    double in = 0.0;
+    for (int i = 0; i < n - 1; i++) {
+        double d = x[i + 1] - x[i];
+        in += d * (y[i] + d * (a[i] / 2.0 + d * (b[i] / 3.0 + d * c[i] / 4.0)));
+    }
+    return in;
+}
+
+// v_l = TTweight_l / (2l+1)^{2/3}: the P_l table on the device carries (2l+1)^{2/3}.
+__global__ void k_transfer_weight(int lmax, const double *__restrict__ cl, double *__restrict__ v)
+{
+    int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l > lmax) return;
+    v[l] = (l > 1) ? pow(2e0 * l + 1e0, 5e0 / 6e0) * (1.0 / sqrt(cl[l])) / pow(2e0 * l + 1e0, 2e0 / 3e0) : 0e0;
+}
+
+// mt2[x][k][p][q] = sum_l pl[l][k] v_l qt[x][p][l] q[l-lmin][q]; tile 64 mu x 32 (p,q), l ascending.
+constexpr int TR_BK = 64, TR_BU = 32, TR_LC = 16;
+
+__global__ void __launch_bounds__(256) k_mij_transfer(int nmu, int lmin, int lmax, int P, int Pp,
+                                                      const double *__restrict__ pl, const double *__restrict__ q,
+                                                      const double *__restrict__ v, const double *__restrict__ qt,
+                                                      double *__restrict__ mt2)
+{
+    __shared__ double sPl[TR_LC][TR_BK];
+    __shared__ double sV[TR_LC][TR_BU];
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int k0 = blockIdx.x * TR_BK, u0 = blockIdx.y * TR_BU, xi = blockIdx.z;
+    const int L = lmax - lmin + 1, nu = Pp * P;
+    const double *qtx = qt + (size_t)xi * Pp * (lmax + 1);
+    double acc[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) acc[r] = 0.0;
+    for (int l0 = 0; l0 < L; l0 += TR_LC) {
+#pragma unroll
+        for (int t = 0; t < (TR_LC * TR_BK) / 256; t++) {
+            int e = tid + 256 * t, lr = e / TR_BK, kc = e % TR_BK;
+            int l = l0 + lr, k = k0 + kc;
+            sPl[lr][kc] = (l < L && k < nmu) ? pl[(size_t)(lmin + l) * nmu + k] : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < (TR_LC * TR_BU) / 256; t++) {
+            int e = tid + 256 * t, lr = e / TR_BU, uc = e % TR_BU;
+            int l = l0 + lr, u = u0 + uc;
+            double val = 0.0;
+            if (l < L && u < nu) {
+                int p = u / P, qq = u - p * P;
+                val = (v[lmin + l] * qtx[(size_t)p * (lmax + 1) + lmin + l]) * q[(size_t)l * P + qq];
+            }
+            sV[lr][uc] = val;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int lr = 0; lr < TR_LC; lr++) {
+            double vv = sV[lr][tx];
+#pragma unroll
+            for (int r = 0; r < 8; r++) acc[r] = fma(sPl[lr][ty + 8 * r], vv, acc[r]);
+        }
+        __syncthreads();
+    }
+    const int u = u0 + tx;
+    if (u >= nu) return;
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        int k = k0 + ty + 8 * r;
+        if (k < nmu) mt2[((size_t)xi * nmu + k) * nu + u] = acc[r];
+    }
+}
+
+// One CTA per 32 (n: primordial) x 32 (m: late) tile; thread (tx, ty) owns
+// n = n0 + tx and m = m0 + ty + 8 r.
+__global__ void __launch_bounds__(256) k_gamma_transfer(int N, int Nprim, int P, int Pp, int nmu, int xsize, int KC,
+                                                        const int *__restrict__ triples, const int *__restrict__ prim,
+                                                        const double *__restrict__ mt2, const double *__restrict__ w,
+                                                        const double *__restrict__ xvec, const double *__restrict__ cx,
+                                                        double scale, double *__restrict__ out)
+{
+    extern __shared__ double smt[];
+    double *sW = smt;        // [KC]
+    double *sA = smt + KC;   // [KC][Pp*P]
+    const int nu = Pp * P;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int n = blockIdx.x * 32 + tx;
+    int po[3] = {0, 0, 0};
+    if (n < Nprim) { po[0] = prim[3 * n] * P; po[1] = prim[3 * n + 1] * P; po[2] = prim[3 * n + 2] * P; }
+    int qm[4][3];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        int m = blockIdx.y * 32 + ty + 8 * r;
+        for (int b = 0; b < 3; b++) qm[r][b] = (m < N) ? triples[3 * m + b] : 0;
+    }
+    double res[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int xi = 0; xi < xsize; xi++) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        const double *src0 = mt2 + (size_t)xi * nmu * nu;
+        for (int k0 = 0; k0 < nmu; k0 += KC) {
+            const int kc = min(KC, nmu - k0);
+            const double *src = src0 + (size_t)k0 * nu;
+            for (int e = tid; e < kc * nu; e += 256) sA[e] = src[e];
+            if (tid < kc) sW[tid] = w[k0 + tid];
+            __syncthreads();
+            for (int kk = 0; kk < kc; kk++) {
+                const double *A = sA + kk * nu;
+                const double wk = sW[kk];
+                const double *r1 = A + po[0], *r2 = A + po[1], *r3 = A + po[2];
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    double a11 = r1[qm[r][0]], a12 = r1[qm[r][1]], a13 = r1[qm[r][2]];
+                    double a21 = r2[qm[r][0]], a22 = r2[qm[r][1]], a23 = r2[qm[r][2]];
+                    double a31 = r3[qm[r][0]], a32 = r3[qm[r][1]], a33 = r3[qm[r][2]];
+                    double t1 = fma(a23, a32, a22 * a33);
+                    double t2 = fma(a23, a31, a21 * a33);
+                    double t3 = fma(a22, a31, a21 * a32);
+                    acc[r] = fma(wk, fma(a13, t3, fma(a12, t2, a11 * t1)), acc[r]);
+                }
+            }
+            __syncthreads();
+        }
+        const double x2 = xvec[xi] * xvec[xi], c = cx[xi];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            double y = x2 * acc[r];
+            if (xi < 10 && fabs(y) > 1e-18) y = 0.0;  // calculate_gamma.c:803-804
+            res[r] = fma(c, y, res[r]);
+        }
+    }
+    if (n >= Nprim) return;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        int m = blockIdx.y * 32 + ty + 8 * r;
+        if (m < N) out[(size_t)m * Nprim + n] = res[r] * scale;
+    }
+}
+
+}  // namespace modal
+
+using namespace modal;
+
+extern "C" modal_status modal_set_transfer(modal_ctx *c, int Pp, int xsize, const double *xvec, const double *qtilde,
+                                           int Nprim, const int *prim)
+{
+    if (!c || !c->have_basis) { set_error("modal_set_transfer: set the basis first"); return MODAL_ERR_STATE; }
+    if (Pp < 1 || Pp > 64 || xsize < 4 || Nprim < 1 || !xvec || !qtilde || !prim) {
+        set_error("modal_set_transfer: Pp=%d xsize=%d (>= 4 points) Nprim=%d", Pp, xsize, Nprim);
+        return MODAL_ERR_ARG;
+    }
+    for (long e = 0; e < 3L * Nprim; e++)
+        if (prim[e] < 0 || prim[e] >= Pp) { set_error("modal_set_transfer: primordial mode index %d outside [0,%d)", prim[e], Pp); return MODAL_ERR_ARG; }
+    for (int i = 1; i < xsize; i++)
+        if (!(xvec[i] > xvec[i - 1])) { set_error("modal_set_transfer: x grid must increase"); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    // spline weights c_x = integral of the reference spline through e_x
+    std::vector<double> cx(xsize), e(xsize, 0.0);
+    for (int i = 0; i < xsize; i++) {
+        e[i] = 1.0;
+        cx[i] = spline_integral(xvec, e.data(), xsize);
+        e[i] = 0.0;
+    }
+    const size_t nq = (size_t)xsize * Pp * (c->lmax + 1);
+    MODAL_TRY(ensure(c->tr_x, sizeof(double) * 2 * xsize));
+    MODAL_TRY(ensure(c->tr_qt, sizeof(double) * nq));
+    MODAL_TRY(ensure(c->tr_prim, sizeof(int) * 3 * (size_t)Nprim));
+    MODAL_CUDA(cudaMemcpyAsync(c->tr_x.ptr, xvec, sizeof(double) * xsize, cudaMemcpyHostToDevice, c->stream));
+    MODAL_CUDA(cudaMemcpyAsync(c->tr_x.as<double>() + xsize, cx.data(), sizeof(double) * xsize, cudaMemcpyHostToDevice,
+                               c->stream));
+    MODAL_CUDA(cudaMemcpyAsync(c->tr_qt.ptr, qtilde, sizeof(double) * nq, cudaMemcpyHostToDevice, c->stream));
+    MODAL_CUDA(cudaMemcpyAsync(c->tr_prim.ptr, prim, sizeof(int) * 3 * Nprim, cudaMemcpyHostToDevice, c->stream));
+    MODAL_CUDA(cudaStreamSynchronize(c->stream));
+    c->tr_Pp = Pp;
+    c->tr_xsize = xsize;
+    c->tr_Nprim = Nprim;
+    return MODAL_OK;
+}
+
+extern "C" modal_status modal_gamma_transfer(modal_ctx *c, double deltaphi, double *gamma_t)
+{
+    if (!c || !c->have_modes || !c->have_spec || c->tr_xsize < 4) {
+        set_error("modal_gamma_transfer: set basis, modes, spectrum and transfer functions first");
+        return MODAL_ERR_STATE;
+    }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    if (!c->have_glint) MODAL_TRY(modal_init_glint(c));
+    const int P = c->P, Pp = c->tr_Pp, xsize = c->tr_xsize, nmu = c->nmu, N = c->N, Nprim = c->tr_Nprim;
+    const int nu = Pp * P;
+    MODAL_TRY(ensure(c->tr_mt, sizeof(double) * (size_t)xsize * nmu * nu));
+    MODAL_TRY(ensure(c->tr_v, sizeof(double) * (c->lmax + 1)));
+    MODAL_TRY(ensure(c->tr_out, sizeof(double) * (size_t)N * Nprim));
+    StageTimer t(c, MODAL_T_GAMMA);
+    k_transfer_weight<<<ceil_div(c->lmax + 1, 256), 256, 0, c->stream>>>(c->lmax, c->cl.as<double>(), c->tr_v.as<double>());
+    MODAL_TRY(launched(c, "transfer_weight"));
+    dim3 gm(ceil_div(nmu, TR_BK), ceil_div(nu, TR_BU), xsize);
+    k_mij_transfer<<<gm, 256, 0, c->stream>>>(nmu, c->lmin, c->lmax, P, Pp, c->pl.as<double>(), c->q.as<double>(),
+                                              c->tr_v.as<double>(), c->tr_qt.as<double>(), c->tr_mt.as<double>());
+    MODAL_TRY(launched(c, "mij_transfer"));
+    int KC = (96 * 1024) / (nu * 8);
+    if (KC < 1) KC = 1;
+    if (KC > 32) KC = 32;
+    const size_t smem = sizeof(double) * ((size_t)KC + (size_t)KC * nu);
+    if (smem > 200 * 1024) { set_error("modal_gamma_transfer: Pp*P=%d too large for the tile", nu); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaFuncSetAttribute(k_gamma_transfer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 gg(ceil_div(Nprim, 32), ceil_div(N, 32));
+    const double scale = deltaphi * deltaphi / (8.0 * 3.14159265358979323846);
+    k_gamma_transfer<<<gg, 256, smem, c->stream>>>(N, Nprim, P, Pp, nmu, xsize, KC, c->triples.as<int>(),
+                                                   c->tr_prim.as<int>(), c->tr_mt.as<double>(), c->w.as<double>(),
+                                                   c->tr_x.as<double>(), c->tr_x.as<double>() + xsize, scale,
+                                                   c->tr_out.as<double>());
+    MODAL_TRY(launched(c, "gamma_transfer"));
+    t.stop();
+    if (gamma_t)
+        MODAL_CUDA(cudaMemcpyAsync(gamma_t, c->tr_out.ptr, sizeof(double) * (size_t)N * Nprim, cudaMemcpyDeviceToHost,
+                                   c->stream));
+    MODAL_CUDA(cudaStreamSynchronize(c->stream));
+    return MODAL_OK;
+}

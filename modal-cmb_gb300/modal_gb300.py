@@ -31,6 +31,7 @@ EXPORTS = [
     "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_orthol_pair", "modal_orthogonalise",
     "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
+    "modal_set_transfer", "modal_gamma_transfer",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7}
@@ -88,6 +89,8 @@ def lib():
             "modal_gamma_fp64_noalloc": (i, [i, i, i, vp, i, vp, i, vp, vp, vp, vp]),
             "modal_modify_bispectrum": (i, [i, vp, vp, vp, vp, vp]),
             "modal_calculate_modes": (i, [vp, i, vp, vp]),
+            "modal_set_transfer": (i, [vp, i, i, vp, vp, i, vp]),
+            "modal_gamma_transfer": (i, [vp, d, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -287,6 +290,18 @@ class Context:
         out = np.empty((len(shapes), self.N)) if download else None
         _check(lib().modal_project(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), prec, _ptr(out)))
         del keep
+        return out
+
+    def set_transfer(self, xvec, qtilde, prim):
+        xvec = _f64(xvec)
+        qt = _f64(qtilde)
+        prim = np.ascontiguousarray(prim, dtype=np.int32).reshape(-1, 3)
+        _check(lib().modal_set_transfer(self.h, qt.shape[1], xvec.size, _ptr(xvec), _ptr(qt), prim.shape[0], _ptr(prim)))
+        self.Nprim = prim.shape[0]
+
+    def gamma_transfer(self, deltaphi):
+        out = np.empty((self.N, self.Nprim))
+        _check(lib().modal_gamma_transfer(self.h, float(deltaphi), _ptr(out)))
         return out
 
     def calculate_modes(self, b):

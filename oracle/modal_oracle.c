@@ -506,3 +506,137 @@ int orc_calculate_modes(int lmin, int lmax, int P, const double *basis, int N, c
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Late x primordial transfer Gamma, default path of gamma_mpi.c:            */
+/* init_gamma_glint + precompute_gammaMij_T + calculate_gamma_2d             */
+/* (calculate_gamma.c:48-303, 512-555, 773-934).                             */
+/* ------------------------------------------------------------------------ */
+
+/* integrate_cubic_spline (calculate_gamma.c:845-934): the integral over
+ * [x0, x_{n-1}] of the reference's cubic spline through (x, y). */
+double orc_integrate_cubic_spline(const double *x, const double *y, int npts)
+{
+    if (npts < 2) return 0.0;
+    double *X = malloc(sizeof(double) * (size_t)npts), *Y = malloc(sizeof(double) * (size_t)npts);
+    double *a = calloc((size_t)npts, sizeof(double)), *b = calloc((size_t)npts, sizeof(double));
+    double *c = calloc((size_t)npts, sizeof(double));
+    for (int i = 0; i < npts; i++) { X[i] = x[i]; Y[i] = y[i]; }
+    c[0] = X[1] - X[0];
+    b[1] = (Y[1] - Y[0]) / c[0];
+    for (int i = 1; i < npts - 1; i++) {
+        c[i] = x[i + 1] - X[i];
+        a[i] = 2.0 * (c[i - 1] + c[i]);
+        b[i + 1] = (Y[i + 1] - Y[i]) / c[i];
+        b[i] = b[i + 1] - b[i];
+    }
+    a[0] = -c[0];
+    a[npts - 1] = -c[npts - 2];
+    b[0] = 0.0;
+    b[npts - 1] = 0.0;
+    if (npts > 2) {
+        b[0] = b[2] / (X[3] - X[1]) - b[1] / (X[2] - X[0]);
+        b[npts - 1] = b[npts - 2] / (X[npts - 1] - X[npts - 3]) - b[npts - 3] / (X[npts - 2] - X[npts - 4]);
+        b[0] = b[0] * c[0] * c[0] / (X[3] - X[0]);
+        b[npts - 1] = -b[npts - 1] * c[npts - 2] * c[npts - 2] / (X[npts - 1] - X[npts - 4]);
+    }
+    for (int i = 1; i < npts; i++) {
+        double h = c[i - 1] / a[i - 1];
+        a[i] = a[i] - h * c[i - 1];
+        b[i] = b[i] - h * b[i - 1];
+    }
+    b[npts - 1] = b[npts - 1] / a[npts - 1];
+    for (int i = npts - 2; i >= 0; i--) b[i] = (b[i] - c[i] * b[i + 1]) / a[i];
+    a[npts - 1] = (Y[npts - 1] - Y[npts - 2]) / c[npts - 2] + c[npts - 2] * (b[npts - 2] + 2.0 * b[npts - 1]);
+    for (int i = 0; i < npts - 1; i++) {
+        a[i] = (Y[i + 1] - Y[i]) / c[i] - c[i] * (b[i + 1] + 2.0 * b[i]);
+        c[i] = (b[i + 1] - b[i]) / c[i];
+        b[i] = 3.0 * b[i];
+    }
+    b[npts - 1] = 3.0 * b[npts - 1];
+    c[npts - 1] = c[npts - 2];
+    double in = 0.0;
+    for (int i = 0; i < npts - 1; i++) {
+        double d = x[i + 1] - x[i];
+        in += d * (Y[i] + d * (a[i] / 2.0 + d * (b[i] / 3.0 + d * c[i] / 4.0)));
+    }
+    free(X); free(Y); free(a); free(b); free(c);
+    return in;
+}
+
+/* qt[x][p][l]: raw transfer functions q~_p(l, x), l = 0..lmax; prim[Nprim][3];
+ * cl[l] = C_l + N_l/b_l^2 (beam 1 folded in); mu, w: n_mu GL nodes (asy());
+ * out[N][Nprim] = calculate_gamma_2d(m, n) for late mode m and primordial n. */
+int orc_gamma_transfer(int lmin, int lmax, int P, const double *basis, int N, const int *triples, const double *cl,
+                       int nmu, const double *mu, const double *w, int xsize, const double *xvec, int Pp,
+                       const double *qt, int Nprim, const int *prim, double dphi, double *out)
+{
+    const int L = lmax - lmin + 1;
+    double *ttw = malloc(sizeof(double) * (size_t)L);
+    for (int i = 0; i < L; i++) {
+        int l = lmin + i;
+        ttw[i] = (l > 1) ? pow(2e0 * l + 1e0, 5e0 / 6e0) * (1.0 / sqrt(cl[l])) : 0e0;  /* :76-88, beam 1 */
+    }
+    /* gl_Pl[k][l] = P_l(mu_k), no (2l+1) factor here (:97-101) */
+    double *pl = malloc(sizeof(double) * (size_t)nmu * (lmax + 1));
+    #pragma omp parallel for
+    for (int k = 0; k < nmu; k++) {
+        double x = mu[k], pm2 = 1.0, pm1 = x;
+        double *row = pl + (long)k * (lmax + 1);
+        for (int l = 0; l <= lmax; l++) {
+            double p;
+            if (l == 0) p = 1.0;
+            else if (l == 1) p = x;
+            else {
+                double pr = (x * (2 * l - 1) * pm1 - (l - 1) * pm2) / l;
+                pm2 = pm1; pm1 = pr;
+                p = (l == 2) ? 0.5 * (3.0 * x * x - 1.0) : (x == 1.0 ? 1.0 : (x == -1.0 ? ((l & 1) ? -1.0 : 1.0) : pr));
+            }
+            row[l] = p;
+        }
+    }
+    /* M[p][q][x][k] = sum_l gl_Pl[k][l+lmin] qtilde_T[x][p][l] basis_T[q][l] (:254-303) */
+    double *M = malloc(sizeof(double) * (size_t)Pp * P * xsize * nmu);
+    #pragma omp parallel for collapse(3)
+    for (int p = 0; p < Pp; p++)
+        for (int q = 0; q < P; q++)
+            for (int xi = 0; xi < xsize; xi++) {
+                double *vec = malloc(sizeof(double) * (size_t)L);
+                for (int l = 0; l < L; l++)
+                    vec[l] = (ttw[l] * qt[((long)xi * Pp + p) * (lmax + 1) + lmin + l]) * basis[(long)l * P + q];
+                for (int k = 0; k < nmu; k++) {
+                    double sum = 0;
+                    const double *row = pl + (long)k * (lmax + 1);
+                    for (int l = 0; l < L; l++) sum += row[l + lmin] * vec[l];
+                    M[(((long)p * P + q) * xsize + xi) * nmu + k] = sum;
+                }
+                free(vec);
+            }
+    /* gamma_2d_pt_TTT (:512-555), calculate_gamma_2d (:773-842) */
+    #pragma omp parallel for collapse(2) schedule(dynamic, 4)
+    for (int m = 0; m < N; m++)
+        for (int n = 0; n < Nprim; n++) {
+            const int *pp = prim + 3 * n, *qq = triples + 3 * m;
+            double *y = malloc(sizeof(double) * (size_t)xsize);
+            for (int xi = 0; xi < xsize; xi++) {
+#define MT(a, b) (M + (((long)pp[a] * P + qq[b]) * xsize + xi) * nmu)
+                const double *m11 = MT(0, 0), *m12 = MT(0, 1), *m13 = MT(0, 2);
+                const double *m21 = MT(1, 0), *m22 = MT(1, 1), *m23 = MT(1, 2);
+                const double *m31 = MT(2, 0), *m32 = MT(2, 1), *m33 = MT(2, 2);
+#undef MT
+                double result = 0.0;
+                for (int j = 0; j < nmu; j++) {
+                    double s1 = m11[j] * m22[j] * m33[j], s2 = m11[j] * m23[j] * m32[j];
+                    double s3 = m12[j] * m21[j] * m33[j], s4 = m12[j] * m23[j] * m31[j];
+                    double s5 = m13[j] * m21[j] * m32[j], s6 = m13[j] * m22[j] * m31[j];
+                    result += w[j] * (s1 + s2 + s3 + s4 + s5 + s6);
+                }
+                y[xi] = xvec[xi] * xvec[xi] * result;
+                if (xi < 10 && fabs(y[xi]) > 1e-18) y[xi] = 0;
+            }
+            out[(long)m * Nprim + n] = orc_integrate_cubic_spline(xvec, y, xsize) * dphi * dphi / (8.0 * ORC_PI);
+            free(y);
+        }
+    free(ttw); free(pl); free(M);
+    return 0;
+}

@@ -85,6 +85,8 @@ class Oracle:
             ("orc_alpha", i, [i, vp, vp, vp, vp, vp]),
             ("orc_modify_bispectrum", i, [i, vp, vp, vp, vp, vp]),
             ("orc_calculate_modes", i, [i, i, i, vp, i, vp, i, vp, vp]),
+            ("orc_integrate_cubic_spline", d, [vp, vp, i]),
+            ("orc_gamma_transfer", i, [i, i, i, vp, i, vp, vp, i, vp, vp, i, vp, i, vp, i, vp, d, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -180,6 +182,24 @@ class Oracle:
                                    _p(beta))
         return beta
 
+    def integrate_cubic_spline(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        return self.L.orc_integrate_cubic_spline(_p(x), _p(y), x.size)
+
+    def gamma_transfer(self, lmin, lmax, q, triples, cl, mu, w, xvec, qt, prim, dphi):
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        triples = np.ascontiguousarray(triples, dtype=np.int32)
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        qt = np.ascontiguousarray(qt, dtype=np.float64)
+        xvec = np.ascontiguousarray(xvec, dtype=np.float64)
+        N, Nprim = triples.shape[0], prim.shape[0]
+        out = np.empty((N, Nprim))
+        self.L.orc_gamma_transfer(lmin, lmax, q.shape[1], _p(q), N, _p(triples), _p(np.ascontiguousarray(cl)), mu.size,
+                                  _p(np.ascontiguousarray(mu)), _p(np.ascontiguousarray(w)), xvec.size, _p(xvec),
+                                  qt.shape[1], _p(qt), Nprim, _p(prim), float(dphi), _p(out))
+        return out
+
     def ortho_cholesky(self, gamma):
         """Cholesky branch; returns (orthol, lambdal, fail) with fail = -1 or the failing pivot row."""
         g = np.ascontiguousarray(gamma, dtype=np.float64)
@@ -242,6 +262,7 @@ class Ref:
             ("ref_project", i, [i, i, i, vp, d, d, d, d, l, vp]),
             ("ref_modify_bispectrum", i, [i, vp, vp]),
             ("ref_calculate_modes", i, [i, vp, vp]),
+            ("ref_gamma_transfer", i, [i, vp, i, vp, i, vp, d, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -303,6 +324,16 @@ class Ref:
         with quiet_stdout():
             self.L.ref_calculate_modes(b.shape[0], _p(b), _p(beta))
         return beta
+
+    def gamma_transfer(self, xvec, qt, prim, dphi):
+        xvec = np.ascontiguousarray(xvec, dtype=np.float64)
+        qt = np.ascontiguousarray(qt, dtype=np.float64)
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        out = np.empty((self.N, prim.shape[0]))
+        with quiet_stdout():
+            self.L.ref_gamma_transfer(xvec.size, _p(xvec), qt.shape[1], _p(qt), prim.shape[0], _p(prim), float(dphi),
+                                      _p(out))
+        return out
 
     def project(self, shape, nthreads=8, max_points=0):
         beta = np.empty(self.N)

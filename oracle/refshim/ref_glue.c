@@ -60,6 +60,15 @@ static int *g_triples;    /* [N][3] */
 static double *g_cl;      /* [lmax+1], C_l + N_l/b_l^2 */
 static orc_shape g_shape;
 
+/* ---- Intel aligned allocation used by calculate_gamma.c ---- */
+void *_mm_malloc(size_t size, size_t align)
+{
+    void *p = NULL;
+    if (align < sizeof(void *)) align = sizeof(void *);
+    return posix_memalign(&p, align, size) == 0 ? p : NULL;
+}
+void _mm_free(void *p) { free(p); }
+
 /* ---- MPI, one rank ---- */
 int MPI_Init(int *argc, char ***argv) { (void)argc; (void)argv; return 0; }
 int MPI_Finalize(void) { return 0; }
@@ -109,8 +118,36 @@ int get_terms_late(void) { return g_N; }
 int get_terms_prim(void) { return g_N; }
 int get_lmax(void) { return eflag_T_lmax; }
 double get_tau0(void) { return 0.0; }
-int get_qtilde_xsize(void) { return 1; }
-int get_qtilde_xvec(double *v) { v[0] = 0.0; return 0; }
+/* radial grid and transfer functions q~_p(l, x) (qtilde, fixed_data.c:2045-2495);
+ * one dummy point unless ref_setup_transfer installed some */
+static int g_xsize = 1, g_Pp = 1, g_Nprim = 0;
+static double g_x0 = 0.0, *g_xvec = &g_x0, *g_qt;  /* g_qt[x][p][l], l = 0..lmax */
+static int *g_prim;                                 /* [Nprim][3] */
+double deltaphi = 1.0;
+double fskyT = 1.0, fskyE = 1.0;
+int get_qtilde_xsize(void) { return g_xsize; }
+int get_qtilde_xvec(double *v) { for (int i = 0; i < g_xsize; i++) v[i] = g_xvec[i]; return 0; }
+double get_qtilde_T(int p, int l, int x) { return g_qt[((long)x * g_Pp + p) * (eflag_T_lmax + 1) + l]; }
+double get_qtilde_E(int p, int l, int x) { return get_qtilde_T(p, l, x); }
+int destroy_qtilde(void) { return 0; }
+int get_pmax_prim(void) { return g_Pp - 1; }
+void find_perm_prim(int r, int *p1, int *p2, int *p3) { *p1 = g_prim[3 * r]; *p2 = g_prim[3 * r + 1]; *p3 = g_prim[3 * r + 2]; }
+double get_beam_EE(int l) { (void)l; return 1.0; }
+double get_beam_TE(int l) { (void)l; return 1.0; }
+double get_cl_TE(int l) { (void)l; return 0.0; }
+double get_cl_EE(int l) { (void)l; return 1.0; }
+double get_cl_TP(int l) { (void)l; return 0.0; }
+double get_noise_TE(int l) { (void)l; return 0.0; }
+double get_noise_EE(int l) { (void)l; return 0.0; }
+/* GSL cubic-spline link stubs (calculate_gamma() is not exercised) */
+#include <stdio.h>
+const struct refshim_interp_type *gsl_interp_cspline = NULL;
+struct refshim_spline *gsl_spline_alloc(const struct refshim_interp_type *T, size_t n) { (void)T; (void)n; fprintf(stderr, "gsl_spline stub called\n"); abort(); }
+int gsl_spline_init(struct refshim_spline *s, const double xa[], const double ya[], size_t n) { (void)s; (void)xa; (void)ya; (void)n; abort(); }
+double gsl_spline_eval_integ(const struct refshim_spline *s, double a, double b, struct refshim_interp_accel *acc) { (void)s; (void)a; (void)b; (void)acc; abort(); }
+struct refshim_interp_accel *gsl_interp_accel_alloc(void) { abort(); }
+void gsl_interp_accel_free(struct refshim_interp_accel *a) { (void)a; }
+void gsl_spline_free(struct refshim_spline *s) { (void)s; }
 int read_eigen(int a, int b, int c) { (void)a; (void)b; (void)c; return 0; }
 double get_eigen(int i) { return i == 0 ? 1.0 : 0.0; }
 double get_cl_TT(int l) { return g_cl[l]; }
@@ -295,5 +332,37 @@ int ref_calculate_modes(int size, double *flat, double *beta)
     double ***b = view3(size, flat);
     for (int r = 0; r < g_N; r++) beta[r] = calculate_modes(r, size, b);
     free_view3(b);
+    return 0;
+}
+
+/* ---- late x primordial transfer Gamma (calculate_gamma.c, default 2D path) ---- */
+extern void init_gamma_glint(void);
+extern void precompute_gammaMij_T(void);
+extern void calculate_gamma_2d(int m, int n, double *result);
+
+/* qt[x][p][l] raw q~_p(l, x) for l = 0..lmax; prim[Nprim][3]; out[N][Nprim]
+ * = calculate_gamma_2d(m, n) (calculate_gamma.c:773-842) after
+ * init_gamma_glint + precompute_gammaMij_T, the gamma_mpi.c default path. */
+int ref_gamma_transfer(int xsize, const double *xvec, int Pp, const double *qt, int Nprim, const int *prim,
+                       double dphi, double *out)
+{
+    g_xsize = xsize; g_Pp = Pp; g_Nprim = Nprim; deltaphi = dphi;
+    g_xvec = malloc(sizeof(double) * (size_t)xsize);
+    memcpy(g_xvec, xvec, sizeof(double) * (size_t)xsize);
+    size_t nq = (size_t)xsize * Pp * (eflag_T_lmax + 1);
+    g_qt = malloc(sizeof(double) * nq);
+    memcpy(g_qt, qt, sizeof(double) * nq);
+    g_prim = malloc(sizeof(int) * 3 * (size_t)Nprim);
+    memcpy(g_prim, prim, sizeof(int) * 3 * (size_t)Nprim);
+    init_gamma_glint();
+    precompute_gammaMij_T();
+    double r[4];
+    for (int m = 0; m < g_N; m++)
+        for (int n = 0; n < Nprim; n++) {
+            calculate_gamma_2d(m, n, r);
+            out[(long)m * Nprim + n] = r[0];
+        }
+    free(g_xvec); g_xvec = &g_x0; g_xsize = 1; g_Pp = 1;
+    free(g_qt); g_qt = NULL; free(g_prim); g_prim = NULL;
     return 0;
 }

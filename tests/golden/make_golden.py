@@ -33,6 +33,17 @@ def dense_input(size):
     return (raw + raw.transpose(1, 2, 0) + raw.transpose(2, 0, 1)) / 3.0
 
 
+def transfer_inputs(lmax, Pp, xsize):
+    """Synthetic radial grid and transfer functions q~_p(l, x) (also rebuilt by the tests)."""
+    xvec = np.linspace(1000.0, 12000.0, xsize)
+    l = np.arange(lmax + 1.0)
+    qt = np.zeros((xsize, Pp, lmax + 1))
+    for xi, x in enumerate(xvec):
+        for p in range(Pp):
+            qt[xi, p] = np.cos((p + 1) * x / 4000.0) * np.sin(0.1 * l * (1 + p) + x / 3000.0) / (1.0 + l)
+    return xvec, qt
+
+
 def main():
     ref = O.Ref()
     # 1. asy() Gauss-Legendre nodes/weights
@@ -71,7 +82,18 @@ def main():
     beta = ref.calculate_modes(mod)
     np.savez_compressed(os.path.join(OUT, "modes_dense.npz"), modified=mod, beta=beta, lmax=lmax, P=P)
 
-    # 6. Gamma (calculate_orthol over all pairs) and projection beta
+    # 6. late x primordial transfer Gamma (calculate_gamma_2d over all (m, n))
+    out = {}
+    for name, lmax, P, Pp, xsize in [("a", 40, 3, 3, 30), ("b", 90, 4, 5, 41)]:
+        q, tr, cl = M.workload(lmax, P)
+        ref.setup(2, lmax, q, tr, cl)
+        xvec, qt = transfer_inputs(lmax, Pp, xsize)
+        prim = M.mode_triples(Pp)
+        out["gamma_" + name] = ref.gamma_transfer(xvec, qt, prim, 0.7)
+        out["dims_" + name] = np.array([lmax, P, Pp, xsize])
+    np.savez_compressed(os.path.join(OUT, "gamma_transfer.npz"), **out)
+
+    # 7. Gamma (calculate_orthol over all pairs) and projection beta
     #    small: lmax=60, P=4; config 1: lmax=500, P=10 (220 modes)
     for name, lmax, P, S in [("small", 60, 4, 4), ("cfg1", 500, 10, 4)]:
         q, tr, cl = M.workload(lmax, P)

@@ -328,3 +328,54 @@ def test_dense_form_vs_oracle_larger(mg, orc):
         c.set_modes(tr)
         beta = c.calculate_modes(mod)
     assert rel_fro(beta, orc.calculate_modes(2, lmax, q, tr, mod)) <= 1e-12
+
+
+# ------------------------------------------------- late x primordial transfer
+
+def _transfer_inputs(lmax, Pp, xsize):
+    xvec = np.linspace(1000.0, 12000.0, xsize)
+    l = np.arange(lmax + 1.0)
+    qt = np.zeros((xsize, Pp, lmax + 1))
+    for xi, x in enumerate(xvec):
+        for p in range(Pp):
+            qt[xi, p] = np.cos((p + 1) * x / 4000.0) * np.sin(0.1 * l * (1 + p) + x / 3000.0) / (1.0 + l)
+    return xvec, qt
+
+
+@pytest.mark.parametrize("name", ["a", "b"])
+def test_transfer_gamma_vs_reference(mg, golden, name):
+    """calculate_gamma_2d over all (m, n) on the GPU vs the in-place reference,
+    with the reference's asy() nodes: 1e-12."""
+    g = golden("gamma_transfer")
+    lmax, P, Pp, xsize = (int(v) for v in g["dims_" + name])
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = _transfer_inputs(lmax, Pp, xsize)
+    nmu = 3 * lmax // 2 + 1
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        gl = golden("gl_asy")
+        if f"x{nmu}" in gl.files:
+            c.set_gl(gl[f"x{nmu}"], gl[f"w{nmu}"])
+        c.set_transfer(xvec, qt, mg.mode_triples(Pp))
+        G = c.gamma_transfer(0.7)
+    tol = 1e-12 if f"x{nmu}" in golden("gl_asy").files else 1e-11
+    assert rel_max(G, g["gamma_" + name]) <= tol
+
+
+def test_transfer_gamma_vs_oracle_wider(mg, orc):
+    """Tile edges: N and Nprim not multiples of 32, Pp != P."""
+    lmax, P, Pp, xsize = 120, 5, 6, 37
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = _transfer_inputs(lmax, Pp, xsize)
+    prim = mg.mode_triples(Pp)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        c.set_transfer(xvec, qt, prim)
+        G = c.gamma_transfer(1.3)
+        x, w = c.get_gl()
+    Go = orc.gamma_transfer(2, lmax, q, tr, cl, x, w, xvec, qt, prim, 1.3)
+    assert rel_max(G, Go) <= 1e-12

@@ -184,3 +184,38 @@ def test_dense_form_matches_reference(orc, golden, mg):
     assert np.max(np.abs(mod[nz] - g["modified"][nz]) / np.abs(g["modified"][nz])) <= 1e-14
     beta = orc.calculate_modes(2, lmax, q, tr, g["modified"])
     assert rel_fro(beta, g["beta"]) <= 1e-13
+
+
+def _transfer_inputs(lmax, Pp, xsize):
+    import numpy as np
+    xvec = np.linspace(1000.0, 12000.0, xsize)
+    l = np.arange(lmax + 1.0)
+    qt = np.zeros((xsize, Pp, lmax + 1))
+    for xi, x in enumerate(xvec):
+        for p in range(Pp):
+            qt[xi, p] = np.cos((p + 1) * x / 4000.0) * np.sin(0.1 * l * (1 + p) + x / 3000.0) / (1.0 + l)
+    return xvec, qt
+
+
+@pytest.mark.parametrize("name", ["a", "b"])
+def test_transfer_gamma_matches_reference(orc, golden, mg, name):
+    """calculate_gamma_2d path of calculate_gamma.c vs the in-place reference."""
+    g = golden("gamma_transfer")
+    lmax, P, Pp, xsize = (int(v) for v in g["dims_" + name])
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = _transfer_inputs(lmax, Pp, xsize)
+    x, w = golden("gl_asy")["x91"], golden("gl_asy")["w91"]
+    nmu = 3 * lmax // 2 + 1
+    if nmu != 91:
+        x, w = orc.gl_nodes(nmu)
+    G = orc.gamma_transfer(2, lmax, q, tr, cl, x, w, xvec, qt, mg.mode_triples(Pp), 0.7)
+    tol = 1e-14 if nmu == 91 else 1e-12  # own nodes vs asy() at n = 136
+    assert rel_max(G, g["gamma_" + name]) <= tol
+
+
+def test_cubic_spline_integral_exact_for_cubics(orc):
+    import numpy as np
+    x = np.sort(np.random.default_rng(2).uniform(0, 3, 25))
+    y = 2 - x + 0.5 * x ** 2 - 0.25 * x ** 3
+    exact = lambda t: 2 * t - t ** 2 / 2 + t ** 3 / 6 - t ** 4 / 16  # noqa: E731
+    assert abs(orc.integrate_cubic_spline(x, y) - (exact(x[-1]) - exact(x[0]))) < 1e-12

@@ -83,7 +83,8 @@ typedef enum {
     MODAL_T_PROJECT = 5,  /* projection of the shapes */
     MODAL_T_ALPHA = 6,    /* alpha solve */
     MODAL_T_LIFT = 7,     /* split form: the tensor-core GEMM of the mu-contraction alone */
-    MODAL_T_COUNT = 8
+    MODAL_T_ADJOINT = 8,  /* gradients with respect to the basis values */
+    MODAL_T_COUNT = 9
 } modal_timer;
 modal_status modal_ctx_profile(modal_ctx *ctx, int enable);
 modal_status modal_ctx_timer(modal_ctx *ctx, int timer, double *ms, long *count);
@@ -209,6 +210,48 @@ modal_status modal_gamma_transfer(modal_ctx *ctx, double deltaphi, double *gamma
  * beta: host [S][N] or NULL for the device result of modal_project.
  * alpha/modesR: host [S][N] or NULL. */
 modal_status modal_alpha(modal_ctx *ctx, int S, const double *beta, double *alpha, double *modesR);
+
+/* ---------------------------------------------------------------- adjoint */
+
+/* Gradients with respect to the basis values q[L][P] of modal_set_basis, FP64
+ * on the GPU.  No counterpart in the reference: its basis optimisation
+ * (basis_optimisation_mpi.c:199-337) prunes modes greedily by the smallest
+ * eigenvalue of leave-one-out Gamma submatrices and has no derivatives; these
+ * entries give the gradient such a search (or a continuous optimiser over
+ * basis coefficients) follows.
+ *
+ * The shape side works in Gamma's own inner product: separable shapes
+ * (MODAL_SHAPE_SEPARABLE only) are weighted per l like the basis,
+ * w_l = (2l+1)^{1/6}/sqrt(C_l + N_l/b_l^2) from modal_set_spectrum
+ * (calculate_mode_3D.c:53-62), and projected through the Gauss-Legendre form
+ * of h^2 (the exact one Gamma uses), so that <S,S> - beta^T Gamma^{-1} beta
+ * is the squared residual of the shape's projection onto the modes. */
+
+/* beta[S][N] = <S_s, Q_n> and norm2[S] = <S_s, S_s> (host, either NULL). */
+modal_status modal_project_gl(modal_ctx *ctx, int S, const modal_shape *shapes, double *beta, double *norm2);
+
+/* dL_dq[L][P] (host) for an upstream dL_dgamma[N][N] (host) through the FP64
+ * Gamma of the current basis/modes/quadrature (modal_gamma, both forms). */
+modal_status modal_gamma_vjp(modal_ctx *ctx, const double *dL_dgamma, double *dL_dq);
+
+/* dL_dq[L][P] for an upstream dL_dbeta[S][N] through modal_project_gl. */
+modal_status modal_project_gl_vjp(modal_ctx *ctx, int S, const modal_shape *shapes, const double *dL_dbeta,
+                                  double *dL_dq);
+
+/* alpha[S][N] = Gamma^{-1} beta = lambdal^T lambdal beta with beta from
+ * modal_project_gl and lambdal from modal_orthogonalise (the alpha solve of
+ * eigenmodetoday_mpi.c:148-162); with dL_dalpha[S][N] also dL_dq[L][P]
+ * (both or neither).  Exact when the orthogonalisation took the Cholesky
+ * branch (lambdal^T lambdal = Gamma^{-1}); on the PCA branch the gradient is
+ * that of the truncated pseudo-inverse with the eigenvectors held fixed. */
+modal_status modal_alpha_gl(modal_ctx *ctx, int S, const modal_shape *shapes, double *alpha, const double *dL_dalpha,
+                            double *dL_dq);
+
+/* Basis-quality objective: the mean relative squared projection residual
+ *   J = (1/S) sum_s (<S_s,S_s> - beta_s^T Gamma^{-1} beta_s) / <S_s,S_s>
+ * (0 when every shape lies in the span of the modes), and dJ_dq[L][P] (host,
+ * NULL to skip).  Needs modal_gamma (FP64) and modal_orthogonalise first. */
+modal_status modal_adjoint_residual(modal_ctx *ctx, int S, const modal_shape *shapes, double *J, double *dJ_dq);
 
 /* ------------------------------------------------- allocation-free Gamma */
 

@@ -70,6 +70,9 @@ struct modal_ctx {
     modal::DevBuf tr_mt;       // [xsize][nmu][Pp][P]
     modal::DevBuf tr_v;        // [lmax+1] weights
     modal::DevBuf tr_out;      // [N][Nprim]
+
+    // adjoint: shape legs and forward products, per-mu adjoints, upstreams
+    modal::DevBuf adj, adj2, adj3;
     double *h_info = nullptr;  // pinned readback
 
     // profiling: event pairs per stage, summed on read

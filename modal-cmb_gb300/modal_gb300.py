@@ -31,10 +31,11 @@ EXPORTS = [
     "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_orthol_pair", "modal_orthogonalise",
     "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
-    "modal_set_transfer", "modal_gamma_transfer",
+    "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
+    "modal_alpha_gl", "modal_adjoint_residual",
 ]
 
-TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7}
+TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8}
 
 
 class ModalError(RuntimeError):
@@ -91,6 +92,11 @@ def lib():
             "modal_calculate_modes": (i, [vp, i, vp, vp]),
             "modal_set_transfer": (i, [vp, i, i, vp, vp, i, vp]),
             "modal_gamma_transfer": (i, [vp, d, vp]),
+            "modal_project_gl": (i, [vp, i, vp, vp, vp]),
+            "modal_gamma_vjp": (i, [vp, vp, vp]),
+            "modal_project_gl_vjp": (i, [vp, i, vp, vp, vp]),
+            "modal_alpha_gl": (i, [vp, i, vp, vp, vp, vp]),
+            "modal_adjoint_residual": (i, [vp, i, vp, ctypes.POINTER(d), vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -310,6 +316,50 @@ class Context:
         _check(lib().modal_calculate_modes(self.h, b.shape[0], _ptr(b), _ptr(out)))
         return out
 
+    # ---- adjoint (gradients with respect to q[L][P])
+
+    def project_gl(self, shapes):
+        """(beta [S][N], <S,S> [S]) in Gamma's Gauss-Legendre inner product."""
+        arr, keep = shapes_to_c(shapes)
+        beta, n2 = np.empty((len(shapes), self.N)), np.empty(len(shapes))
+        _check(lib().modal_project_gl(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), _ptr(beta), _ptr(n2)))
+        del keep
+        return beta, n2
+
+    def gamma_vjp(self, dL_dgamma):
+        g = _f64(dL_dgamma)
+        out = np.empty((self.lmax - self.lmin + 1, self.P))
+        _check(lib().modal_gamma_vjp(self.h, _ptr(g), _ptr(out)))
+        return out
+
+    def project_gl_vjp(self, shapes, dL_dbeta):
+        arr, keep = shapes_to_c(shapes)
+        g = _f64(dL_dbeta)
+        out = np.empty((self.lmax - self.lmin + 1, self.P))
+        _check(lib().modal_project_gl_vjp(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), _ptr(g), _ptr(out)))
+        del keep
+        return out
+
+    def alpha_gl(self, shapes, dL_dalpha=None):
+        """alpha [S][N]; with dL_dalpha also dL/dq [L][P]."""
+        arr, keep = shapes_to_c(shapes)
+        a = np.empty((len(shapes), self.N))
+        g = None if dL_dalpha is None else _f64(dL_dalpha)
+        out = None if g is None else np.empty((self.lmax - self.lmin + 1, self.P))
+        _check(lib().modal_alpha_gl(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), _ptr(a), _ptr(g), _ptr(out)))
+        del keep
+        return a if g is None else (a, out)
+
+    def adjoint_residual(self, shapes, grad=True):
+        """(J, dJ/dq [L][P] or None): mean relative squared projection residual."""
+        arr, keep = shapes_to_c(shapes)
+        J = ctypes.c_double()
+        out = np.empty((self.lmax - self.lmin + 1, self.P)) if grad else None
+        _check(lib().modal_adjoint_residual(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), ctypes.byref(J),
+                                            _ptr(out)))
+        del keep
+        return J.value, out
+
     def alpha(self, S, beta=None, download=True):
         b = None if beta is None else _f64(beta)
         a = np.empty((S, self.N)) if download else None
@@ -392,6 +442,40 @@ def separable_shapes(lmax, S, seed, tmin=1, tmax=2):
     return out
 
 
+def bspline_matrix(lmin, lmax, nb=64, degree=3):
+    """[L][nb] clamped uniform B-splines of the given degree on [lmin, lmax]
+    (Cox-de Boor recursion; input builder for the basis-optimisation workload)."""
+    l = np.arange(lmin, lmax + 1, dtype=np.float64)
+    x = (l - lmin) / (lmax - lmin)
+    inner = np.linspace(0.0, 1.0, nb - degree + 1)
+    t = np.concatenate([np.zeros(degree), inner, np.ones(degree)])
+    B = np.zeros((x.size, len(t) - 1))
+    for i in range(len(t) - 1):
+        B[:, i] = (x >= t[i]) & (x < t[i + 1])
+    B[x >= 1.0, nb - 1] = 1.0  # right end belongs to the last non-empty span
+    for k in range(1, degree + 1):
+        Bn = np.zeros((x.size, len(t) - 1 - k))
+        for i in range(len(t) - 1 - k):
+            a = t[i + k] - t[i]
+            b = t[i + k + 1] - t[i + 1]
+            left = (x - t[i]) / a * B[:, i] if a > 0 else 0.0
+            right = (t[i + k + 1] - x) / b * B[:, i + 1] if b > 0 else 0.0
+            Bn[:, i] = left + right
+        B = Bn
+    return B
+
+
+def bspline_workload(lmax=1000, nfunc=12, nb=64, seed=0, lmin=2):
+    """Basis-optimisation workload: q_p = sum_j C[p][j] B_j(l) with a seeded
+    [nfunc][nb] FP64 coefficient matrix.  Returns (C, Bw, triples, cl) where
+    Bw[l][j] = B_j(l) (2l+1)^{1/6}/sqrt(C_l), so that q~ = Bw C^T."""
+    cl = synthetic_cl(lmax)
+    B = bspline_matrix(lmin, lmax, nb)
+    Bw = weighted_q(B, cl, lmin)
+    C = np.random.default_rng(seed).standard_normal((nfunc, nb))
+    return C, Bw, mode_triples(nfunc), cl
+
+
 def bump_shapes(S, seed):
     """S seeded Gaussian bumps, centre ~ Dirichlet(1,1,1), sigma ~ U[0.05,0.3]."""
     rng = np.random.default_rng(seed)
@@ -407,6 +491,7 @@ CONFIGS = {
     "cfg1": dict(lmax=500, P=10, shapes=("sep", 4, 1, 2)),
     "cfg2": dict(lmax=2000, P=30, shapes=("sep", 16, 1, 2)),
     "cfg3": dict(lmax=2000, P=30, shapes=("mix", 256, 1, 4)),
+    "cfg4": dict(lmax=1000, P=12, shapes=("sep", 32, 1, 2), basis="bspline64"),
     "cfg5": dict(lmax=2500, P=40, shapes=("mix", 512, 1, 4)),
     # mid-size case for kernel captures: operands larger than L2, a few GB at most
     "prof": dict(lmax=1000, P=20, shapes=("sep", 4, 1, 2)),

@@ -84,7 +84,8 @@ typedef enum {
     MODAL_T_ALPHA = 6,    /* alpha solve */
     MODAL_T_LIFT = 7,     /* split form: the tensor-core GEMM of the mu-contraction alone */
     MODAL_T_ADJOINT = 8,  /* gradients with respect to the basis values */
-    MODAL_T_COUNT = 9
+    MODAL_T_PRUNE = 9,    /* greedy basis pruning */
+    MODAL_T_COUNT = 10
 } modal_timer;
 modal_status modal_ctx_profile(modal_ctx *ctx, int enable);
 modal_status modal_ctx_timer(modal_ctx *ctx, int timer, double *ms, long *count);
@@ -252,6 +253,31 @@ modal_status modal_alpha_gl(modal_ctx *ctx, int S, const modal_shape *shapes, do
  * (0 when every shape lies in the span of the modes), and dJ_dq[L][P] (host,
  * NULL to skip).  Needs modal_gamma (FP64) and modal_orthogonalise first. */
 modal_status modal_adjoint_residual(modal_ctx *ctx, int S, const modal_shape *shapes, double *J, double *dJ_dq);
+
+/* ----------------------------------------------------------- basis pruning */
+
+/* Greedy basis pruning of basis_optimisation_mpi.c:184-337.  Over the modes
+ * not in faillist[nfail] (the reference's faillist file, :134-147), Gamma is
+ * normalised to unit diagonal (:184-190); then, while two or more modes are
+ * active, the mode whose removal leaves the normalised Gamma with the largest
+ * smallest eigenvalue is removed (first maximum, :256-312).  order[t] is the
+ * mode removed at step t and lambda_min[t] that largest smallest eigenvalue;
+ * the last entry is the surviving mode with lambda_min = 1, as the reference
+ * prints it (:326-343).  Both arrays are host [N - nfail].  gamma: host
+ * [N][N] (the master Gamma the reference reads, :90-109) or NULL for the
+ * device Gamma of modal_gamma (N must match).  Every leave-one-out smallest
+ * eigenvalue comes from one eigendecomposition per step (FP64, cuSOLVER) and
+ * the secular equation of the minor (see prune.cu), not one eigensolve per
+ * candidate.  Repeated or out-of-range fail-list entries give MODAL_ERR_ARG
+ * (the reference would mis-size its active list). */
+modal_status modal_basis_prune(modal_ctx *ctx, int N, const double *gamma, int nfail, const int *faillist, int *order,
+                               double *lambda_min);
+
+/* The reference's basis-quality figure as an objective: the smallest
+ * eigenvalue of the normalised device Gamma (of modal_gamma), its eigenvector
+ * eigvec[N] (host, or NULL) and the gradient dlam_dq[L][P] (host, or NULL)
+ * with respect to the basis values, through the Gamma adjoint. */
+modal_status modal_lambda_min(modal_ctx *ctx, double *lambda_min, double *eigvec, double *dlam_dq);
 
 /* ------------------------------------------------- allocation-free Gamma */
 

@@ -493,6 +493,8 @@ modal_status adj_ready(modal_ctx *c, const char *who, int S, const modal_shape *
 
 }  // namespace
 
+modal_status gamma_vjp_accum_dev(modal_ctx *c, const double *G, double *dq) { return gamma_vjp_dev(c, G, dq); }
+
 }  // namespace modal
 
 using namespace modal;

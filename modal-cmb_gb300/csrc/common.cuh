@@ -73,6 +73,7 @@ struct modal_ctx {
 
     // adjoint: shape legs and forward products, per-mu adjoints, upstreams
     modal::DevBuf adj, adj2, adj3;
+    modal::DevBuf prune;  // basis pruning: normalised Gamma, minors, eigenvalues, work
     double *h_info = nullptr;  // pinned readback
 
     // profiling: event pairs per stage, summed on read
@@ -140,6 +141,9 @@ modal_status transpose_dev(modal_ctx *ctx, const double *in, double *out, int R,
 modal_status basis_legendre_dev(modal_ctx *ctx, int size, int pmax, double min, double max, const double *d_values,
                                 double *d_out);
 modal_status geometric_dev(modal_ctx *ctx, long npts, const int *d_pts, double *d_out);
+
+// dq[L][P] (device, accumulated) += the Gamma adjoint for an upstream dL/dGamma G[N][N] (device).
+modal_status gamma_vjp_accum_dev(modal_ctx *ctx, const double *G, double *dq);
 
 // FP64 tiled GEMM on the context stream:
 //   C[m][n] = beta*C[m][n] + alpha * sum_k opA(m,k) opB(k,n)

@@ -32,10 +32,10 @@ EXPORTS = [
     "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
     "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
-    "modal_alpha_gl", "modal_adjoint_residual",
+    "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
 ]
 
-TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8}
+TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
 
 
 class ModalError(RuntimeError):
@@ -97,6 +97,8 @@ def lib():
             "modal_project_gl_vjp": (i, [vp, i, vp, vp, vp]),
             "modal_alpha_gl": (i, [vp, i, vp, vp, vp, vp]),
             "modal_adjoint_residual": (i, [vp, i, vp, ctypes.POINTER(d), vp]),
+            "modal_basis_prune": (i, [vp, i, vp, i, vp, vp, vp]),
+            "modal_lambda_min": (i, [vp, ctypes.POINTER(d), vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -359,6 +361,25 @@ class Context:
                                             _ptr(out)))
         del keep
         return J.value, out
+
+    def basis_prune(self, gamma=None, faillist=(), N=None):
+        """(order, lambda_min): greedy pruning order of the active modes."""
+        g = None if gamma is None else _f64(gamma)
+        N = g.shape[0] if g is not None else (N or self.N)
+        fl = np.ascontiguousarray(faillist, dtype=np.int32)
+        n = N - fl.size
+        order, lam = np.empty(max(n, 1), dtype=np.int32), np.empty(max(n, 1))
+        _check(lib().modal_basis_prune(self.h, N, _ptr(g), fl.size, _ptr(fl) if fl.size else None, _ptr(order),
+                                       _ptr(lam)))
+        return order[:n], lam[:n]
+
+    def lambda_min(self, grad=False):
+        """(lambda_min, eigenvector, dlambda/dq or None) of the normalised device Gamma."""
+        lam = ctypes.c_double()
+        v = np.empty(self.N)
+        out = np.empty((self.lmax - self.lmin + 1, self.P)) if grad else None
+        _check(lib().modal_lambda_min(self.h, ctypes.byref(lam), _ptr(v), _ptr(out)))
+        return lam.value, v, out
 
     def alpha(self, S, beta=None, download=True):
         b = None if beta is None else _f64(beta)

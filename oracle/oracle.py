@@ -347,3 +347,63 @@ class Ref:
         with quiet_stdout():
             self.L.ref_project(nthreads, *args, max_points, _p(beta))
         return beta
+
+
+def basis_prune(gamma, faillist=(), steps=None):
+    """Greedy basis pruning of basis_optimisation_mpi.c:184-337, restated with
+    numpy.linalg.eigvalsh (LAPACK, upper triangle) standing in for
+    LAPACKE_dsyevr(..., 'I', 'U', il = iu = 1).  The active modes are those not
+    in faillist; Gamma is normalised as ortho[i][j] / (norm_i norm_j) (:184-190);
+    each step computes the smallest eigenvalue of every leave-one-out minor
+    (:256-281), removes the first maximiser (:287-312).  Returns (order,
+    lambda_min) with the survivor last at lambda 1 (:326-343); `steps` stops
+    early after that many removals (for large N), returning only those."""
+    gamma = np.asarray(gamma, dtype=np.float64)
+    N = gamma.shape[0]
+    norm = np.sqrt(np.diag(gamma))
+    failed = set(int(f) for f in faillist)
+    lst = [i for i in range(N) if i not in failed]
+    arr = gamma[np.ix_(lst, lst)] / np.outer(norm[lst], norm[lst])
+    order, lams = [], []
+    for n in range(len(lst) - 1, 0, -1):
+        if steps is not None and len(order) == steps:
+            return np.array(order), np.array(lams)
+        vals = np.empty(n + 1)
+        for m in range(n + 1):
+            keep = np.r_[0:m, m + 1:n + 1]
+            vals[m] = np.linalg.eigvalsh(arr[np.ix_(keep, keep)], UPLO="U")[0]
+        index = int(np.argmax(vals))  # first maximum, as the strict '>' scan
+        order.append(lst[index])
+        lams.append(vals[index])
+        del lst[index]
+        arr = np.delete(np.delete(arr, index, 0), index, 1)
+    order.append(lst[0])
+    lams.append(1.0)
+    return np.array(order), np.array(lams)
+
+
+REF_PRUNE = os.path.join(HERE, "_ref", "basis_prune_ref")
+
+
+def ref_basis_prune(gamma, faillist=()):
+    """Run the reference's own basis_optimisation_mpi.c main() (compiled in
+    place by `make -C oracle ref`, with its Gamma and fail-list reads redirected
+    to temporary files and a Jacobi stand-in for MKL's dsyevr) and parse its
+    printed elimination order: (order, lambda_min printed with %e)."""
+    import tempfile
+    gamma = np.ascontiguousarray(gamma, dtype=np.float64)
+    N = gamma.shape[0]
+    with tempfile.TemporaryDirectory() as d:
+        gp = os.path.join(d, "gamma.unf")
+        gamma.tofile(gp)
+        env = dict(os.environ, MODAL_PRUNE_N=str(N), MODAL_PRUNE_GAMMA=gp)
+        if len(faillist):
+            fp = os.path.join(d, "fail.txt")
+            with open(fp, "w") as f:
+                f.write("\n".join(str(int(v)) for v in faillist) + "\n")
+            env["MODAL_PRUNE_FAIL"] = fp
+        out = subprocess.run([REF_PRUNE, "unused.ini"], env=env, check=True, capture_output=True, text=True).stdout
+    lines = out.split("starting reduction\n", 1)[1].strip().splitlines()
+    order = np.array([int(l.split("\t")[0]) for l in lines])
+    lam = np.array([float(l.split("\t")[4]) for l in lines])
+    return order, lam

@@ -108,5 +108,27 @@ def main():
         print(name, "done", G.shape, beta.shape)
 
 
+def prune_golden():
+    """8. greedy basis pruning: the reference's basis_optimisation_mpi.c main()
+    (oracle/_ref/basis_prune_ref) on a Gamma of 35 modes with two failed modes,
+    and on a seeded 60 x 60 SPD matrix."""
+    q, tr, cl = M.workload(120, 5)
+    orc = O.Oracle()
+    mu, w = orc.gl_nodes(181)
+    G = orc.gamma(orc.mij(orc.legendre_table(mu, 120), 2, 120, q), w, tr)
+    fail = np.array([3, 7])
+    order_a, lam_a = O.ref_basis_prune(G, fail)
+    X = np.random.default_rng(0).standard_normal((60, 80))
+    R = X @ X.T
+    order_b, lam_b = O.ref_basis_prune(R)
+    np.savez_compressed(os.path.join(OUT, "basis_prune.npz"), gamma_a=G, fail_a=fail, order_a=order_a, lam_a=lam_a,
+                        gamma_b=R, order_b=order_b, lam_b=lam_b)
+    print("basis_prune done", order_a.size, order_b.size)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["prune"]:
+        prune_golden()
+    else:
+        main()
+        prune_golden()

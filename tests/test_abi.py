@@ -53,6 +53,10 @@ def test_argument_errors_without_gpu(built_lib, mg):
     assert L.modal_set_basis(None, 2, 10, 3, None) == 1
     n = ctypes.c_long()
     assert L.modal_tetrapyd_count(5, 2, ctypes.byref(n)) == 1
+    assert L.modal_basis_prune(None, 4, None, 0, None, None, None) == 1
+    assert L.modal_gamma_vjp(None, None, None) == 1
+    assert L.modal_adjoint_residual(None, 1, None, None, None) == 1
+    assert L.modal_lambda_min(None, None, None, None) == 1
 
 
 def test_tetrapyd_count_host_logic(built_lib, mg, orc):

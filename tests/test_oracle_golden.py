@@ -219,3 +219,15 @@ def test_cubic_spline_integral_exact_for_cubics(orc):
     y = 2 - x + 0.5 * x ** 2 - 0.25 * x ** 3
     exact = lambda t: 2 * t - t ** 2 / 2 + t ** 3 / 6 - t ** 4 / 16  # noqa: E731
     assert abs(orc.integrate_cubic_spline(x, y) - (exact(x[-1]) - exact(x[0]))) < 1e-12
+
+
+@pytest.mark.parametrize("case", ["a", "b"])
+def test_basis_prune_matches_reference_driver(golden, case):
+    # basis_optimisation_mpi.c's own main() (in place, Jacobi stand-in for dsyevr)
+    import oracle
+    g = golden("basis_prune")
+    fail = g["fail_a"] if case == "a" else ()
+    order, lam = oracle.basis_prune(g["gamma_" + case], fail)
+    assert np.array_equal(order, g["order_" + case])
+    # the reference prints lambda with %e (7 significant digits)
+    assert np.max(np.abs(lam - g["lam_" + case]) / np.abs(lam)) <= 6e-7

@@ -228,6 +228,20 @@ def run_ours(a, ws, rank, local):
                 "modesR_fro": float(np.linalg.norm(ms_ - m64) / np.linalg.norm(m64)),
             },
         }
+        # alpha with a PCA eigenvalue floor above the split form's Gamma error:
+        # the same FP64 orthogonalisation of each Gamma, keeping eigenvalues > floor * e_max
+        fl = {}
+        for floor in (1e-6, 1e-4):
+            ctx.set_pca_floor(floor)
+            _, _, _, r64 = ctx.orthogonalise(G64, download=False)
+            af64, _ = ctx.alpha(S, b64)
+            _, _, _, rs = ctx.orthogonalise(Gs, download=False)
+            afs, _ = ctx.alpha(S, bs)
+            fl["%g" % floor] = {"kept_fp64": r64, "kept_split": rs,
+                                "alpha_fro": float(np.linalg.norm(afs - af64) / np.linalg.norm(af64)),
+                                "alpha_gamma_norm": float(np.max(gnorm(afs - af64) / gnorm(af64)))}
+        ctx.set_pca_floor(0.0)
+        extra["rel_err_vs_fp64"]["alpha_with_pca_floor"] = fl
 
     # the 256-shape batch at this size (128 separable sums of 1-4 terms + 128
     # Gaussian bumps), split form; the FP64 form is scaled from the timed shapes
@@ -298,7 +312,7 @@ def run_ours(a, ws, rank, local):
     line = {
         "metric": METRIC, "value": go_ms * 1e-3, "unit": "s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == mg.PREC_FP64 else "bf16x3 split, f32 tile acc, f64 sum",
+        "dtype": "f64" if prec == mg.PREC_FP64 else "f16x3 split (hi/lo pieces, 3 products), f32 tile acc, f64 sum",
         "data": "synthetic (seeded shapes; synthetic C_l; shifted Legendre basis)",
         "config": {"workload": f"{a.config}: l=2..{lmax}, P={P}, N={N}, n_mu={nmu}, S={S} shapes",
                    "l2": "flushed (256 MB write between steps)", "parallelism": f"replicas x{ws}",

@@ -206,6 +206,15 @@ modal_status modal_set_transfer(modal_ctx *ctx, int Pp, int xsize, const double 
  * from modal_set_spectrum and scale deltaphi^2/(8 pi).  FP64 on the GPU. */
 modal_status modal_gamma_transfer(modal_ctx *ctx, double deltaphi, double *gamma_t);
 
+/* Eigenvalue floor of the PCA branch: keep the leading eigenvalues of the
+ * normalised Gamma above floor * (largest eigenvalue).  0 (the default) is the
+ * reference's rule, every positive eigenvalue (ortho_late_mpi.c:786-792).  At
+ * cond ~1e16 the smallest kept eigenvalues are rounding noise and alpha
+ * amplifies any perturbation of Gamma or beta by 1/e; a floor above the
+ * relative error of Gamma (about 1e-7 for the split form) makes alpha
+ * reproducible.  Takes effect at the next modal_orthogonalise. */
+modal_status modal_set_pca_floor(modal_ctx *ctx, double floor);
+
 /* alpha = lambdal^T lambdal beta and modesR = orthol^T alpha
  * (eigenmodetoday_mpi.c:148-162, 286-316) for S shapes, FP64 on the GPU.
  * beta: host [S][N] or NULL for the device result of modal_project.

@@ -465,6 +465,14 @@ modal_status modal_orthogonalise(modal_ctx *c, const double *gamma, int pca_flag
     return MODAL_OK;
 }
 
+modal_status modal_set_pca_floor(modal_ctx *c, double floor)
+{
+    if (!c || !(floor >= 0.0 && floor < 1.0)) { set_error("modal_set_pca_floor: floor must be in [0, 1)"); return MODAL_ERR_ARG; }
+    c->pca_floor = floor;
+    c->have_ortho = false;
+    return MODAL_OK;
+}
+
 modal_status modal_set_spectrum(modal_ctx *c, const double *cl)
 {
     MODAL_TRY(need(c, c && c->have_basis, "modal_set_spectrum: set the basis first"));

@@ -33,6 +33,7 @@ struct modal_ctx {
     bool have_glint = false, have_gamma = false, have_spec = false, have_ortho = false;
     bool have_beta = false;
     int ortho_branch = 0, ortho_rank = 0;
+    double pca_floor = 0.0;  // PCA keeps eigenvalues > pca_floor * e_max (0: the reference's > 0)
     int beta_S = 0;
 
     // device state

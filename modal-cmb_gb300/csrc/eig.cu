@@ -14,12 +14,14 @@
 
 namespace modal {
 
-// Count leading positive eigenvalues in descending order (W is ascending).
-__global__ void k_pca_rank(int N, const double *__restrict__ W, int *rank)
+// Count leading eigenvalues above floor * e_max in descending order (W is
+// ascending); floor = 0 is the reference's rule (leading positive ones).
+__global__ void k_pca_rank(int N, const double *__restrict__ W, double floor, int *rank)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double cut = floor > 0.0 ? floor * W[N - 1] : 0.0;
     int r = 0;
-    for (int i = 0; i < N && W[N - 1 - i] > 0.0; i++) r = i + 1;
+    for (int i = 0; i < N && W[N - 1 - i] > cut; i++) r = i + 1;
     *rank = r;
 }
 
@@ -76,7 +78,7 @@ modal_status eig_pca_dev(modal_ctx *ctx)
     MODAL_CUDA(cudaMemcpyAsync(&hinfo, devinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
     if (hinfo != 0) { set_error("syevd info=%d", hinfo); return MODAL_ERR_NOCONV; }
-    k_pca_rank<<<1, 1, 0, ctx->stream>>>(N, W, rank);
+    k_pca_rank<<<1, 1, 0, ctx->stream>>>(N, W, ctx->pca_floor, rank);
     MODAL_TRY(launched(ctx, "pca_rank"));
     size_t NN = (size_t)N * N;
     k_pca_outputs<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, A, W, ctx->norm.as<double>(), rank,

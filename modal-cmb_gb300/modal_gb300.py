@@ -33,6 +33,7 @@ EXPORTS = [
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
     "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
     "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
+    "modal_set_pca_floor",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
@@ -99,6 +100,7 @@ def lib():
             "modal_adjoint_residual": (i, [vp, i, vp, ctypes.POINTER(d), vp]),
             "modal_basis_prune": (i, [vp, i, vp, i, vp, vp, vp]),
             "modal_lambda_min": (i, [vp, ctypes.POINTER(d), vp, vp]),
+            "modal_set_pca_floor": (i, [vp, d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -287,6 +289,9 @@ class Context:
         _check(lib().modal_orthogonalise(self.h, _ptr(g), pca_flag, _ptr(o), _ptr(lam), ctypes.byref(br),
                                          ctypes.byref(rk)))
         return o, lam, br.value, rk.value
+
+    def set_pca_floor(self, floor):
+        _check(lib().modal_set_pca_floor(self.h, float(floor)))
 
     def set_spectrum(self, cl):
         cl = _f64(cl)

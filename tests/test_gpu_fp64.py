@@ -207,6 +207,16 @@ def test_pca_branch_forced_and_on_failure(mg):
                 s = np.sign(np.dot(lam[i], lam_ref[i]))
                 assert np.max(np.abs(lam[i] - s * lam_ref[i])) <= 1e-8 * np.max(np.abs(lam_ref[i]))
             assert np.all(lam[rank:] == 0) and np.all(o[:, rank:] == 0)
+        # eigenvalue floor: rank 40 exactly once the round-off eigenvalues are cut
+        n = np.sqrt(np.diag(G_def))
+        e = np.linalg.eigvalsh(G_def / np.outer(n, n))
+        c.set_pca_floor(1e-10)
+        _, lam, branch, rank = c.orthogonalise(G_def, pca_flag=1)
+        assert branch == 1 and rank == int(np.sum(e > 1e-10 * e[-1])) == 40
+        assert np.all(lam[40:] == 0)
+        c.set_pca_floor(0.0)
+        with pytest.raises(mg.ModalError):
+            c.set_pca_floor(1.0)
 
 
 # ---------------------------------------------------------------- projection

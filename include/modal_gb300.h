@@ -215,6 +215,31 @@ modal_status modal_gamma_transfer(modal_ctx *ctx, double deltaphi, double *gamma
  * reproducible.  Takes effect at the next modal_orthogonalise. */
 modal_status modal_set_pca_floor(modal_ctx *ctx, double floor);
 
+/* Batched projection replayed from a captured CUDA graph.  Same inputs,
+ * result and FP64/FP32 forms as modal_project (beta: host [S][N], required;
+ * it also stays on the device for modal_alpha).  The first call for a batch
+ * layout -- S, and each shape's kind and term count -- captures the device
+ * work (staging copies from pinned buffers, the slab kernel over all shapes,
+ * the reductions, the copy of beta back) into a graph; later calls with the
+ * same layout copy the new values into the pinned staging buffers and launch
+ * the graph once.  A change of layout, basis size or of any buffer the graph
+ * uses is detected and re-captured.  No reference counterpart (the reference
+ * re-walks the tetrapyd per shape, calculate_mode_3D.c:217-264). */
+modal_status modal_project_batch(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec, double *beta);
+/* Number of CUDA graphs this context has captured. */
+long modal_ctx_captures(const modal_ctx *ctx);
+
+/* Launch-configuration tuner.  Times the candidate configurations of the
+ * FP32 projection kernel (shapes per CTA; grid or persistent 1-2 CTAs per SM)
+ * and of the FP64 Gamma kernel (mu steps per shared-memory stage) on this
+ * context's problem, keeps the fastest, and appends them to the text file
+ * cache_path (NULL: no file) keyed by GPU architecture and problem size; a
+ * later call that finds its keys there applies them without timing.  Needs
+ * basis, modes and spectrum.  No reference counterpart. */
+modal_status modal_autotune(modal_ctx *ctx, const char *cache_path);
+/* The configuration in effect (0 = built-in default). */
+modal_status modal_get_tuning(const modal_ctx *ctx, int *proj_sg, int *proj_cpb, int *gamma_kc);
+
 /* alpha = lambdal^T lambdal beta and modesR = orthol^T alpha
  * (eigenmodetoday_mpi.c:148-162, 286-316) for S shapes, FP64 on the GPU.
  * beta: host [S][N] or NULL for the device result of modal_project.

@@ -164,6 +164,7 @@ void modal_ctx_destroy(modal_ctx *c)
                       &c->modesr, &c->scratch, &c->scratch2, &c->shape_tab, &c->shape_desc, &c->slab_order,
                       &c->split, &c->tr_x, &c->tr_qt, &c->tr_prim, &c->tr_mt, &c->tr_v, &c->tr_out,
                       &c->adj, &c->adj2, &c->adj3, &c->prune};
+    batch_release(c);
     for (DevBuf *b : bufs) release(*b);
     timers_clear(c);
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);

@@ -22,6 +22,8 @@ struct DevBuf {
 
 }  // namespace modal
 
+namespace modal { struct BatchGraph; }
+
 struct modal_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -34,6 +36,10 @@ struct modal_ctx {
     bool have_beta = false;
     int ortho_branch = 0, ortho_rank = 0;
     double pca_floor = 0.0;  // PCA keeps eigenvalues > pca_floor * e_max (0: the reference's > 0)
+    modal::BatchGraph *batch = nullptr;  // captured batched-projection graph (batch.cu)
+    long captures = 0;                   // graphs captured so far
+    // tuned launch configurations (0: built-in defaults; set by modal_autotune)
+    int proj_sg = 0, proj_cpb = 0, gamma_kc = 0;
     int beta_S = 0;
 
     // device state
@@ -145,6 +151,32 @@ modal_status geometric_dev(modal_ctx *ctx, long npts, const int *d_pts, double *
 
 // dq[L][P] (device, accumulated) += the Gamma adjoint for an upstream dL/dGamma G[N][N] (device).
 modal_status gamma_vjp_accum_dev(modal_ctx *ctx, const double *G, double *dq);
+
+// Device descriptor of one shape (projection kernels).
+struct DShape {
+    int kind, nterms;
+    long tab_off;
+    double c1, c2, c3, sigma;
+};
+
+// A planned projection: validated descriptors, buffer offsets, launch shape.
+struct ProjPlan {
+    int S = 0;
+    modal_prec prec = MODAL_PREC_FP64;
+    long tab_total = 0;
+    std::vector<DShape> desc;
+    int SG = 8, CPL = 1, cpb = 0, nsm = 0, fpt = 0;
+    size_t smem = 0, o_q = 0, o_v = 0, o_t = 0, o_s = 0, o_F = 0, o_B = 0, o_c = 0;
+};
+// plan: validate, size every buffer, upload the slab schedule (may allocate);
+// stage: copy shape tables/descriptors to the device; record: enqueue the
+// device work only (no allocation, no host round trip: capturable).
+modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec, ProjPlan &pl);
+modal_status proj_stage(modal_ctx *ctx, const ProjPlan &pl, const modal_shape *shapes);
+modal_status proj_record(modal_ctx *ctx, const ProjPlan &pl);
+
+// Frees the captured batched-projection graph and its pinned staging buffers.
+void batch_release(modal_ctx *ctx);
 
 // FP64 tiled GEMM on the context stream:
 //   C[m][n] = beta*C[m][n] + alpha * sum_k opA(m,k) opB(k,n)

@@ -172,6 +172,8 @@ modal_status gamma_fp64_dev(modal_ctx *ctx)
     int KC = (96 * 1024) / (P * P * 8);
     if (KC < 1) KC = 1;
     if (KC > 32) KC = 32;
+    if (ctx->gamma_kc > 0 && sizeof(double) * ((size_t)ctx->gamma_kc * (1 + (size_t)P * P)) <= 200 * 1024)
+        KC = ctx->gamma_kc;  // tuned (modal_autotune)
     size_t smem = sizeof(double) * ((size_t)KC + (size_t)KC * P * P);
     if (smem > 200 * 1024) { set_error("gamma_fp64: P=%d too large for the shared-memory tile", P); return MODAL_ERR_ARG; }
     MODAL_CUDA(cudaFuncSetAttribute(k_gamma_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

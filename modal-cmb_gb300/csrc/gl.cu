@@ -74,17 +74,26 @@ modal_status gl_nodes_dev(modal_ctx *ctx, int n, double *d_mu, double *d_w)
 // orthogonalisation_late.c:47-54, stored l-major so each step of the
 // recurrence is one coalesced row).  P_l as gsl_sf_legendre_Pl: upward
 // recurrence p_l = (x(2l-1)p_{l-1} - (l-1)p_{l-2})/l from P_0 = 1, P_1 = x,
-// P_2 returned in closed form, exact values at x = +-1.  One thread per node.
-// The 1/l and (2l+1)^{2/3} factors come from a per-l table in shared memory.
+// P_2 returned in closed form, exact values at x = +-1.  One thread per node;
+// the (2l+1)^{2/3} factors come from a per-l table.
 // ---------------------------------------------------------------------------
+// pw[l] = (2l+1)^{2/3}
 __global__ void k_pl_factors(int lmax, double *pw)
 {
     int l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l <= lmax) pw[l] = pow(2.0 * l + 1.0, 2.0 / 3.0);
 }
 
-__global__ void k_legendre_table(int nmu, int lmax, const double *__restrict__ mu, const double *__restrict__ pw,
-                                 double *__restrict__ pl)
+// One thread per node and one warp per block, so that the n_mu independent
+// recurrences spread over as many SMs as possible: the recurrence is serial in
+// l and GB300's FP64 rate per SM is low, so the number of SMs in use, not the
+// bytes written, sets the time.  The arithmetic is gsl_sf_legendre_Pl's
+// upward recurrence exactly, (x (2l-1) P_{l-1} - (l-1) P_{l-2}) / l: folding
+// the division into precomputed factors moves the table by ~1e-12 at l = 500
+// (the coefficient roundings accumulate coherently along l), which would
+// show in Gamma's 1e-12 parity with the reference.
+__global__ void __launch_bounds__(32) k_legendre_table(int nmu, int lmax, const double *__restrict__ mu,
+                                                       const double *__restrict__ pw, double *__restrict__ pl)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nmu) return;
@@ -94,7 +103,7 @@ __global__ void k_legendre_table(int nmu, int lmax, const double *__restrict__ m
     if (lmax >= 1) pl[(size_t)nmu + k] = pw[1] * x;
     double pm2 = 1.0, pm1 = x;
     for (int l = 2; l <= lmax; l++) {
-        double pr = (x * (2 * l - 1) * pm1 - (l - 1) * pm2) / l;
+        const double pr = (x * (2 * l - 1) * pm1 - (l - 1) * pm2) / l;
         pm2 = pm1;
         pm1 = pr;
         double p = pr;
@@ -111,7 +120,7 @@ modal_status legendre_table_dev(modal_ctx *ctx, int nmu, int lmax, const double 
     double *pw = ctx->scratch2.as<double>();
     k_pl_factors<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax, pw);
     MODAL_TRY(launched(ctx, "pl_factors"));
-    k_legendre_table<<<ceil_div(nmu, 64), 64, 0, ctx->stream>>>(nmu, lmax, d_mu, pw, d_pl);
+    k_legendre_table<<<ceil_div(nmu, 32), 32, 0, ctx->stream>>>(nmu, lmax, d_mu, pw, d_pl);
     return launched(ctx, "legendre_table");
 }
 

@@ -151,7 +151,7 @@ extern "C" modal_status modal_gamma_fp64_noalloc(int lmin, int lmax, int P, cons
         w = w_s;
     }
     k_pl_factors<<<ceil_div(lmax + 1, 256), 256, 0, s>>>(lmax, pw);
-    k_legendre_table<<<ceil_div(nmu, 64), 64, 0, s>>>(nmu, lmax, mu, pw, pl);
+    k_legendre_table<<<ceil_div(nmu, 32), 32, 0, s>>>(nmu, lmax, mu, pw, pl);
     k_noalloc_pairs<<<1, 1, 0, s>>>(P, pairs, status);
     k_noalloc_triples<<<ceil_div(3L * N, 256), 256, 0, s>>>(N, P, d_triples, triples, status);
     dim3 gm(ceil_div(nmu, NA_MIJ_BK), ceil_div(npair, NA_MIJ_BU));

@@ -22,12 +22,6 @@
 
 namespace modal {
 
-struct DShape {
-    int kind, nterms;
-    long tab_off;
-    double c1, c2, c3, sigma;
-};
-
 __device__ __forceinline__ double d_permsix(int i, int j, int k)
 {
     if (i == k && i == j) return 1.0;
@@ -253,21 +247,39 @@ __device__ __forceinline__ float shape_f(const FShape &s, const float *__restric
     return expf(-a * s.inv2s2);
 }
 
+// Work item w = (slab rank w / G, shape group w % G), slabs heaviest first.
+// counter == NULL: one item per CTA of a (L x G) grid.  counter != NULL: a
+// persistent grid whose CTAs take items from *counter until nitems are done.
 template <int SG, int CPL>
-__global__ void __launch_bounds__(256) k_project_slab_f32(int lmin, int lmax, int P, int S,
+__global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax, int P, int S, int G, int nitems,
+                                                           int *__restrict__ counter,
                                                            const int *__restrict__ slab_order,
                                                            const float *__restrict__ qf, const float *__restrict__ vlf,
                                                            const FShape *__restrict__ shapes,
                                                            const float *__restrict__ tabf, float *__restrict__ Fbuf)
 {
     constexpr int JC = 16, CW = 32 * CPL;
-    __shared__ float fsm[8][2][32][SG];
+    static_assert(SG % 4 == 0, "shape groups are read as float4");
+    __shared__ float4 fsm[8][2][32][SG / 4];  // shape values per (warp, row, k, shape)
     __shared__ float Hs[JC][SG][CW];
     __shared__ FShape sh[SG];
+    __shared__ int item;
     extern __shared__ float Fsm[];  // [SG*P*P] hi, then [SG*P*P] lo
-    const int slab = slab_order[blockIdx.x];
+    for (int pass = 0;; pass++) {
+    int w;
+    if (counter) {
+        __syncthreads();  // the previous item's last reads of Fsm are done
+        if (threadIdx.x == 0) item = atomicAdd(counter, 1);
+        __syncthreads();
+        w = item;
+        if (w >= nitems) return;
+    } else {
+        if (pass > 0) return;
+        w = blockIdx.x * G + blockIdx.y;
+    }
+    const int slab = slab_order[w / G];
     const int i = lmin + slab;
-    const int s0 = blockIdx.y * SG;
+    const int s0 = (w % G) * SG;
     const int sgv = min(SG, S - s0);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int par = i & 1, PP = P * P, L = lmax - lmin + 1, stride = lmax + 1;
@@ -316,7 +328,10 @@ __global__ void __launch_bounds__(256) k_project_slab_f32(int lmin, int lmax, in
                     }
                 }
 #pragma unroll
-                for (int s = 0; s < SG; s++) { fsm[warp][0][lane][s] = fa[s]; fsm[warp][1][lane][s] = fb2[s]; }
+                for (int s4 = 0; s4 < SG / 4; s4++) {
+                    fsm[warp][0][lane][s4] = make_float4(fa[4 * s4], fa[4 * s4 + 1], fa[4 * s4 + 2], fa[4 * s4 + 3]);
+                    fsm[warp][1][lane][s4] = make_float4(fb2[4 * s4], fb2[4 * s4 + 1], fb2[4 * s4 + 2], fb2[4 * s4 + 3]);
+                }
                 __syncwarp();
                 const int nt = min(32, nk - kb);
                 float hA[SG][CPL], hB[SG][CPL];
@@ -331,13 +346,16 @@ __global__ void __launch_bounds__(256) k_project_slab_f32(int lmin, int lmax, in
 #pragma unroll
                     for (int cc = 0; cc < CPL; cc++) qv[cc] = (lane + 32 * cc < P) ? qrow[lane + 32 * cc] : 0.f;
 #pragma unroll
-                    for (int s = 0; s < SG; s++) {
-                        const float a = fsm[warp][0][t][s], b = fsm[warp][1][t][s];
+                    for (int s4 = 0; s4 < SG / 4; s4++) {
+                        const float4 a4 = fsm[warp][0][t][s4], b4 = fsm[warp][1][t][s4];
+                        const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-                        for (int cc = 0; cc < CPL; cc++) {
-                            hA[s][cc] = fmaf(a, qv[cc], hA[s][cc]);
-                            hB[s][cc] = fmaf(b, qv[cc], hB[s][cc]);
-                        }
+                        for (int u = 0; u < 4; u++)
+#pragma unroll
+                            for (int cc = 0; cc < CPL; cc++) {
+                                hA[4 * s4 + u][cc] = fmaf(av[u], qv[cc], hA[4 * s4 + u][cc]);
+                                hB[4 * s4 + u][cc] = fmaf(bv[u], qv[cc], hB[4 * s4 + u][cc]);
+                            }
                     }
                 }
 #pragma unroll
@@ -373,6 +391,7 @@ __global__ void __launch_bounds__(256) k_project_slab_f32(int lmin, int lmax, in
     for (int e = threadIdx.x; e < sgv * PP; e += 256) {
         const int s = e / PP, rem = e - s * PP;
         Fbuf[((size_t)(s0 + s) * L + slab) * PP + rem] = Fhi[e] + Flo[e];
+    }
     }
 }
 
@@ -417,6 +436,15 @@ __global__ void k_fshapes(int S, const DShape *__restrict__ in, FShape *__restri
 }
 
 
+
+// ---------------------------------------------------------------- host side
+//
+// A projection is planned (shapes validated, every device buffer sized, the
+// slab schedule uploaded), its inputs are staged (shape tables and
+// descriptors copied to the device), and its device work is recorded on the
+// context stream.  The record step allocates nothing and makes no host
+// round trip, so modal_project_batch can capture it into a CUDA graph.
+
 static long slab_points(int i, int lmax)
 {
     long n = 0;
@@ -427,133 +455,177 @@ static long slab_points(int i, int lmax)
     return n;
 }
 
-modal_status project_split(modal_ctx *ctx, int S, long tab_total);
+// Tunable launch configuration of the FP32 slab kernel (see autotune.cu).
+static void proj_config(const modal_ctx *ctx, int P, int *SG, int *CPL, int *cpb)
+{
+    *CPL = (P <= 32) ? 1 : 2;
+    *SG = (P <= 32) ? 8 : 4;
+    if (ctx->proj_sg == 4 || (ctx->proj_sg == 8 && P <= 32)) *SG = ctx->proj_sg;
+    *cpb = ctx->proj_cpb > 0 ? ctx->proj_cpb : 0;
+}
 
-modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec)
+modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec, ProjPlan &pl)
 {
     const int lmin = ctx->lmin, lmax = ctx->lmax, L = ctx->L, P = ctx->P, N = ctx->N, PP = P * P;
-    // shapes -> device descriptors + concatenated separable tables
-    std::vector<DShape> ds(S);
+    pl = ProjPlan();
+    pl.S = S;
+    pl.prec = prec;
+    pl.desc.resize(S);
     long tab_total = 0;
     for (int s = 0; s < S; s++) {
         const modal_shape &m = shapes[s];
+        DShape &d = pl.desc[s];
+        d.kind = m.kind;
+        d.nterms = m.nterms;
+        d.tab_off = tab_total;
+        d.c1 = m.c[0]; d.c2 = m.c[1]; d.c3 = m.c[2];
+        d.sigma = m.sigma;
         if (m.kind == MODAL_SHAPE_SEPARABLE) {
             if (m.nterms < 1 || !m.tab) { set_error("shape %d: separable needs nterms >= 1 and a table", s); return MODAL_ERR_ARG; }
             tab_total += (long)m.nterms * 3 * (lmax + 1);
         } else if (m.kind == MODAL_SHAPE_BUMP) {
             if (!(m.sigma > 0.0)) { set_error("shape %d: bump sigma must be > 0", s); return MODAL_ERR_ARG; }
+            d.nterms = 0;
         } else {
             set_error("shape %d: unknown kind %d", s, m.kind);
             return MODAL_ERR_ARG;
         }
     }
+    pl.tab_total = tab_total;
     MODAL_TRY(ensure(ctx->shape_tab, sizeof(double) * (size_t)(tab_total > 0 ? tab_total : 1)));
     MODAL_TRY(ensure(ctx->shape_desc, sizeof(DShape) * (size_t)S));
-    long off = 0;
-    for (int s = 0; s < S; s++) {
-        const modal_shape &m = shapes[s];
-        ds[s].kind = m.kind;
-        ds[s].nterms = m.nterms;
-        ds[s].tab_off = off;
-        ds[s].c1 = m.c[0]; ds[s].c2 = m.c[1]; ds[s].c3 = m.c[2];
-        ds[s].sigma = m.sigma;
-        if (m.kind == MODAL_SHAPE_SEPARABLE) {
-            size_t n = (size_t)m.nterms * 3 * (lmax + 1);
-            MODAL_CUDA(cudaMemcpyAsync(ctx->shape_tab.as<double>() + off, m.tab, sizeof(double) * n,
-                                       cudaMemcpyHostToDevice, ctx->stream));
-            off += (long)n;
-        }
-    }
-    MODAL_CUDA(cudaMemcpyAsync(ctx->shape_desc.ptr, ds.data(), sizeof(DShape) * S, cudaMemcpyHostToDevice, ctx->stream));
     // slab schedule: heaviest slabs first
     std::vector<int> order(L);
     std::vector<long> cnt(L);
-    for (int s = 0; s < L; s++) { order[s] = s; cnt[s] = slab_points(lmin + s, lmax); }
+    for (int q = 0; q < L; q++) { order[q] = q; cnt[q] = slab_points(lmin + q, lmax); }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
     MODAL_TRY(ensure(ctx->slab_order, sizeof(int) * (size_t)L));
     MODAL_CUDA(cudaMemcpyAsync(ctx->slab_order.ptr, order.data(), sizeof(int) * L, cudaMemcpyHostToDevice, ctx->stream));
-
     MODAL_TRY(ensure(ctx->vl, sizeof(double) * (lmax + 1)));
+    MODAL_TRY(ensure(ctx->beta, sizeof(double) * (size_t)S * N));
+    if (prec == MODAL_PREC_SPLIT) {
+        proj_config(ctx, P, &pl.SG, &pl.CPL, &pl.cpb);
+        auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+        size_t o = 0;
+        pl.o_q = o; o += al(sizeof(float) * (size_t)L * P);
+        pl.o_v = o; o += al(sizeof(float) * (lmax + 1));
+        pl.o_t = o; o += al(sizeof(float) * (size_t)(tab_total > 0 ? tab_total : 1));
+        pl.o_s = o; o += al(sizeof(FShape) * (size_t)S);
+        pl.o_F = o; o += al(sizeof(float) * (size_t)S * L * PP);
+        pl.o_B = o; o += al(sizeof(double) * (size_t)S * P * PP);
+        pl.o_c = o; o += al(sizeof(int));
+        MODAL_TRY(ensure(ctx->scratch, o));
+        pl.smem = sizeof(float) * 2 * (size_t)pl.SG * PP;
+        int dev = ctx->device, nsm = 0;
+        MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        pl.nsm = nsm;
+        if (pl.SG == 8) MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_f32<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+        else if (pl.CPL == 1) MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_f32<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+        else MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_f32<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+    } else {
+        const int KMAX = (lmax - lmin) / 2 + 2;
+        pl.smem = sizeof(double) * ((size_t)JC * KMAX + (size_t)JC * P);
+        if (pl.smem > 220 * 1024) { set_error("project: lmax=%d too large for the slab tile", lmax); return MODAL_ERR_ARG; }
+        pl.fpt = ceil_div(PP, 256);
+        if (pl.fpt > 16) { set_error("project: P=%d too large", P); return MODAL_ERR_ARG; }
+        MODAL_TRY(ensure(ctx->scratch, sizeof(double) * ((size_t)S * L * PP + (size_t)S * P * PP)));
+        auto attr = [&](auto kern) -> modal_status {
+            MODAL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+            return MODAL_OK;
+        };
+        if (pl.fpt <= 1) MODAL_TRY(attr(k_project_slab_fp64<1>));
+        else if (pl.fpt <= 4) MODAL_TRY(attr(k_project_slab_fp64<4>));
+        else if (pl.fpt <= 8) MODAL_TRY(attr(k_project_slab_fp64<8>));
+        else MODAL_TRY(attr(k_project_slab_fp64<16>));
+    }
+    return MODAL_OK;
+}
+
+modal_status proj_stage(modal_ctx *ctx, const ProjPlan &pl, const modal_shape *shapes)
+{
+    const int lmax = ctx->lmax;
+    for (int s = 0; s < pl.S; s++) {
+        const modal_shape &m = shapes[s];
+        if (m.kind != MODAL_SHAPE_SEPARABLE) continue;
+        size_t n = (size_t)m.nterms * 3 * (lmax + 1);
+        MODAL_CUDA(cudaMemcpyAsync(ctx->shape_tab.as<double>() + pl.desc[s].tab_off, m.tab, sizeof(double) * n,
+                                   cudaMemcpyHostToDevice, ctx->stream));
+    }
+    MODAL_CUDA(cudaMemcpyAsync(ctx->shape_desc.ptr, pl.desc.data(), sizeof(DShape) * pl.S, cudaMemcpyHostToDevice,
+                               ctx->stream));
+    return MODAL_OK;
+}
+
+modal_status proj_record(modal_ctx *ctx, const ProjPlan &pl)
+{
+    const int lmin = ctx->lmin, lmax = ctx->lmax, L = ctx->L, P = ctx->P, N = ctx->N, PP = P * P, S = pl.S;
     k_vl<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax, ctx->cl.as<double>(), ctx->vl.as<double>());
     MODAL_TRY(launched(ctx, "vl"));
-
-    if (prec == MODAL_PREC_SPLIT) return project_split(ctx, S, tab_total);
-    size_t fbytes = sizeof(double) * (size_t)S * L * PP;
-    size_t bbytes = sizeof(double) * (size_t)S * P * PP;
-    MODAL_TRY(ensure(ctx->scratch, fbytes + bbytes));
+    if (pl.prec == MODAL_PREC_SPLIT) {
+        uint8_t *b = ctx->scratch.as<uint8_t>();
+        float *qf = reinterpret_cast<float *>(b + pl.o_q), *vlf = reinterpret_cast<float *>(b + pl.o_v);
+        float *tabf = reinterpret_cast<float *>(b + pl.o_t), *Fbuf = reinterpret_cast<float *>(b + pl.o_F);
+        FShape *fs = reinterpret_cast<FShape *>(b + pl.o_s);
+        double *B = reinterpret_cast<double *>(b + pl.o_B);
+        int *counter = reinterpret_cast<int *>(b + pl.o_c);
+        k_d2f<<<ceil_div((long)L * P, 256), 256, 0, ctx->stream>>>((long)L * P, ctx->q.as<double>(), qf);
+        MODAL_TRY(launched(ctx, "d2f_q"));
+        k_d2f<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax + 1, ctx->vl.as<double>(), vlf);
+        MODAL_TRY(launched(ctx, "d2f_vl"));
+        if (pl.tab_total > 0) {
+            k_d2f<<<ceil_div(pl.tab_total, 256), 256, 0, ctx->stream>>>(pl.tab_total, ctx->shape_tab.as<double>(), tabf);
+            MODAL_TRY(launched(ctx, "d2f_tab"));
+        }
+        k_fshapes<<<ceil_div(S, 64), 64, 0, ctx->stream>>>(S, ctx->shape_desc.as<DShape>(), fs);
+        MODAL_TRY(launched(ctx, "fshapes"));
+        const int G = ceil_div(S, pl.SG), nitems = L * G;
+        dim3 grid(L, G);
+        int *cnt = nullptr;
+        if (pl.cpb > 0) {
+            MODAL_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), ctx->stream));
+            grid = dim3(std::min(nitems, pl.nsm * pl.cpb), 1);
+            cnt = counter;
+        }
+        auto run = [&](auto kern) -> modal_status {
+            kern<<<grid, 256, pl.smem, ctx->stream>>>(lmin, lmax, P, S, G, nitems, cnt, ctx->slab_order.as<int>(), qf,
+                                                     vlf, fs, tabf, Fbuf);
+            return launched(ctx, "project_slab_f32");
+        };
+        if (pl.SG == 8) MODAL_TRY(run(k_project_slab_f32<8, 1>));
+        else if (pl.CPL == 1) MODAL_TRY(run(k_project_slab_f32<4, 1>));
+        else MODAL_TRY(run(k_project_slab_f32<4, 2>));
+        k_project_B_f32<<<ceil_div((long)S * P * PP, 256), 256, 0, ctx->stream>>>(L, P, S, qf, Fbuf, B);
+        MODAL_TRY(launched(ctx, "project_B_f32"));
+        k_project_beta<<<ceil_div((long)S * N, 256), 256, 0, ctx->stream>>>(N, P, S, ctx->triples.as<int>(), B,
+                                                                              ctx->beta.as<double>());
+        return launched(ctx, "project_beta");
+    }
     double *Fbuf = ctx->scratch.as<double>();
     double *B = Fbuf + (size_t)S * L * PP;
     const int KMAX = (lmax - lmin) / 2 + 2;
-    size_t smem = sizeof(double) * ((size_t)JC * KMAX + (size_t)JC * P);
-    if (smem > 220 * 1024) { set_error("project: lmax=%d too large for the slab tile", lmax); return MODAL_ERR_ARG; }
-    int fpt = ceil_div(PP, 256);
     auto run = [&](auto kern) -> modal_status {
-        MODAL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<L, 256, smem, ctx->stream>>>(lmin, lmax, P, S, KMAX, ctx->slab_order.as<int>(), ctx->q.as<double>(),
-                                            ctx->vl.as<double>(), ctx->shape_desc.as<DShape>(),
-                                            ctx->shape_tab.as<double>(), Fbuf);
+        kern<<<L, 256, pl.smem, ctx->stream>>>(lmin, lmax, P, S, KMAX, ctx->slab_order.as<int>(), ctx->q.as<double>(),
+                                               ctx->vl.as<double>(), ctx->shape_desc.as<DShape>(),
+                                               ctx->shape_tab.as<double>(), Fbuf);
         return launched(ctx, "project_slab_fp64");
     };
-    if (fpt <= 1) MODAL_TRY(run(k_project_slab_fp64<1>));
-    else if (fpt <= 4) MODAL_TRY(run(k_project_slab_fp64<4>));
-    else if (fpt <= 8) MODAL_TRY(run(k_project_slab_fp64<8>));
-    else if (fpt <= 16) MODAL_TRY(run(k_project_slab_fp64<16>));
-    else { set_error("project: P=%d too large", P); return MODAL_ERR_ARG; }
-    size_t nb = (size_t)S * P * PP;
-    k_project_B<<<ceil_div((long)nb, 256), 256, 0, ctx->stream>>>(L, P, S, ctx->q.as<double>(), Fbuf, B);
+    if (pl.fpt <= 1) MODAL_TRY(run(k_project_slab_fp64<1>));
+    else if (pl.fpt <= 4) MODAL_TRY(run(k_project_slab_fp64<4>));
+    else if (pl.fpt <= 8) MODAL_TRY(run(k_project_slab_fp64<8>));
+    else MODAL_TRY(run(k_project_slab_fp64<16>));
+    k_project_B<<<ceil_div((long)S * P * PP, 256), 256, 0, ctx->stream>>>(L, P, S, ctx->q.as<double>(), Fbuf, B);
     MODAL_TRY(launched(ctx, "project_B"));
-    MODAL_TRY(ensure(ctx->beta, sizeof(double) * (size_t)S * N));
     k_project_beta<<<ceil_div((long)S * N, 256), 256, 0, ctx->stream>>>(N, P, S, ctx->triples.as<int>(), B,
                                                                           ctx->beta.as<double>());
     return launched(ctx, "project_beta");
 }
 
-// FP32 path: operands converted once, all shapes in one slab launch.
-modal_status project_split(modal_ctx *ctx, int S, long tab_total)
+modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec)
 {
-    const int lmin = ctx->lmin, lmax = ctx->lmax, L = ctx->L, P = ctx->P, N = ctx->N, PP = P * P;
-    const int CPL = (P <= 32) ? 1 : 2;
-    const int SG = (P <= 32) ? 8 : 4;
-    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    size_t o = 0;
-    const size_t o_q = o; o += al(sizeof(float) * (size_t)L * P);
-    const size_t o_v = o; o += al(sizeof(float) * (lmax + 1));
-    const size_t o_t = o; o += al(sizeof(float) * (size_t)(tab_total > 0 ? tab_total : 1));
-    const size_t o_s = o; o += al(sizeof(FShape) * (size_t)S);
-    const size_t o_F = o; o += al(sizeof(float) * (size_t)S * L * PP);
-    const size_t o_B = o; o += al(sizeof(double) * (size_t)S * P * PP);
-    MODAL_TRY(ensure(ctx->scratch, o));
-    uint8_t *b = ctx->scratch.as<uint8_t>();
-    float *qf = reinterpret_cast<float *>(b + o_q), *vlf = reinterpret_cast<float *>(b + o_v);
-    float *tabf = reinterpret_cast<float *>(b + o_t), *Fbuf = reinterpret_cast<float *>(b + o_F);
-    FShape *fs = reinterpret_cast<FShape *>(b + o_s);
-    double *B = reinterpret_cast<double *>(b + o_B);
-    k_d2f<<<ceil_div((long)L * P, 256), 256, 0, ctx->stream>>>((long)L * P, ctx->q.as<double>(), qf);
-    MODAL_TRY(launched(ctx, "d2f_q"));
-    k_d2f<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax + 1, ctx->vl.as<double>(), vlf);
-    MODAL_TRY(launched(ctx, "d2f_vl"));
-    if (tab_total > 0) {
-        k_d2f<<<ceil_div(tab_total, 256), 256, 0, ctx->stream>>>(tab_total, ctx->shape_tab.as<double>(), tabf);
-        MODAL_TRY(launched(ctx, "d2f_tab"));
-    }
-    k_fshapes<<<ceil_div(S, 64), 64, 0, ctx->stream>>>(S, ctx->shape_desc.as<DShape>(), fs);
-    MODAL_TRY(launched(ctx, "fshapes"));
-    size_t smem = sizeof(float) * 2 * (size_t)SG * PP;
-    dim3 grid(L, ceil_div(S, SG));
-    auto run = [&](auto kern) -> modal_status {
-        MODAL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<grid, 256, smem, ctx->stream>>>(lmin, lmax, P, S, ctx->slab_order.as<int>(), qf, vlf, fs, tabf, Fbuf);
-        return launched(ctx, "project_slab_f32");
-    };
-    if (CPL == 1) MODAL_TRY(run(k_project_slab_f32<8, 1>));
-    else MODAL_TRY(run(k_project_slab_f32<4, 2>));
-    size_t nb = (size_t)S * P * PP;
-    k_project_B_f32<<<ceil_div((long)nb, 256), 256, 0, ctx->stream>>>(L, P, S, qf, Fbuf, B);
-    MODAL_TRY(launched(ctx, "project_B_f32"));
-    MODAL_TRY(ensure(ctx->beta, sizeof(double) * (size_t)S * N));
-    k_project_beta<<<ceil_div((long)S * N, 256), 256, 0, ctx->stream>>>(N, P, S, ctx->triples.as<int>(), B,
-                                                                          ctx->beta.as<double>());
-    return launched(ctx, "project_beta");
+    ProjPlan pl;
+    MODAL_TRY(proj_plan(ctx, S, shapes, prec, pl));
+    MODAL_TRY(proj_stage(ctx, pl, shapes));
+    return proj_record(ctx, pl);
 }
 
 }  // namespace modal

@@ -33,7 +33,7 @@ EXPORTS = [
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
     "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
     "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
-    "modal_set_pca_floor",
+    "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
@@ -101,6 +101,10 @@ def lib():
             "modal_basis_prune": (i, [vp, i, vp, i, vp, vp, vp]),
             "modal_lambda_min": (i, [vp, ctypes.POINTER(d), vp, vp]),
             "modal_set_pca_floor": (i, [vp, d]),
+            "modal_project_batch": (i, [vp, i, vp, i, vp]),
+            "modal_ctx_captures": (l, [vp]),
+            "modal_autotune": (i, [vp, ctypes.c_char_p]),
+            "modal_get_tuning": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -304,6 +308,27 @@ class Context:
         _check(lib().modal_project(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), prec, _ptr(out)))
         del keep
         return out
+
+    def project_batch(self, shapes, prec=PREC_FP64):
+        """beta [S][N] through the captured-graph batch path."""
+        arr, keep = shapes_to_c(shapes)
+        out = np.empty((len(shapes), self.N))
+        _check(lib().modal_project_batch(self.h, len(shapes), ctypes.cast(arr, ctypes.c_void_p), prec, _ptr(out)))
+        del keep
+        return out
+
+    @property
+    def captures(self):
+        return lib().modal_ctx_captures(self.h)
+
+    def autotune(self, cache_path=None):
+        _check(lib().modal_autotune(self.h, None if cache_path is None else os.fsencode(cache_path)))
+        return self.tuning()
+
+    def tuning(self):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().modal_get_tuning(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"proj_sg": a.value, "proj_cpb": b.value, "gamma_kc": c.value}
 
     def set_transfer(self, xvec, qtilde, prim):
         xvec = _f64(xvec)

@@ -57,6 +57,9 @@ def test_argument_errors_without_gpu(built_lib, mg):
     assert L.modal_gamma_vjp(None, None, None) == 1
     assert L.modal_adjoint_residual(None, 1, None, None, None) == 1
     assert L.modal_lambda_min(None, None, None, None) == 1
+    assert L.modal_project_batch(None, 1, None, 0, None) == 1
+    assert L.modal_autotune(None, None) == 1
+    assert L.modal_ctx_captures(None) == 0
 
 
 def test_tetrapyd_count_host_logic(built_lib, mg, orc):

@@ -138,6 +138,8 @@ def run_ours(a, ws, rank, local):
     ctx.profile(True)
     stream = torch.cuda.ExternalStream(ctx.stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    # the library's own launch-configuration tuner, before any timing (cached per machine)
+    tuning = ctx.autotune(os.path.join(tempfile.gettempdir(), f"modal_gb300_tune_{local}.txt"))
 
     split_ok = True
     try:
@@ -244,19 +246,23 @@ def run_ours(a, ws, rank, local):
         extra["rel_err_vs_fp64"]["alpha_with_pca_floor"] = fl
 
     # the 256-shape batch at this size (128 separable sums of 1-4 terms + 128
-    # Gaussian bumps), split form; the FP64 form is scaled from the timed shapes
+    # Gaussian bumps), split form, through the graph-captured batch path (one
+    # graph launch: staging copies, all shapes' slab work, reductions, beta
+    # back to the host); the FP64 form is scaled from the timed shapes
     if split_ok and a.config in ("cfg2", "cfg3"):
         sh256 = mg.config_shapes(lmax, ("mix", 256, 1, 4), seed=rank)
+        b_ref = ctx.project(sh256, mg.PREC_SPLIT)
         for _ in range(2):
-            ctx.project(sh256, mg.PREC_SPLIT, download=False)
+            b256 = ctx.project_batch(sh256, mg.PREC_SPLIT)
+        assert np.array_equal(b256, b_ref)
         torch.cuda.synchronize()
         p_ms = []
-        for _ in range(2):
+        for _ in range(3):
             flush.zero_()
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            ctx.project(sh256, mg.PREC_SPLIT, download=False)
+            ctx.project_batch(sh256, mg.PREC_SPLIT)
             e1.record(stream)
             torch.cuda.synchronize()
             p_ms.append(e0.elapsed_time(e1))
@@ -265,6 +271,7 @@ def run_ours(a, ws, rank, local):
         go64 = extra.get("fp64_gamma_ortho_ms", go_ms)
         gos = extra.get("split_gamma_ortho_ms", go_ms)
         extra["projection_256_shapes"] = {
+            "path": "modal_project_batch (captured CUDA graph, %d captures)" % ctx.captures,
             "split_ms": p256, "split_projections_per_s": 256.0 / (p256 * 1e-3),
             "fp64_ms_scaled_from_%d_shapes" % S: fp64_256,
             "split_vs_fp64_gamma_ortho_plus_256_projections": (go64 + fp64_256) / (gos + p256)}
@@ -309,6 +316,7 @@ def run_ours(a, ws, rank, local):
     if rank == 0 and not a.no_cpu_baseline:
         cpu = cpu_baseline(a.config, lmax, P, q, tr, cl, shapes, samples=1)
     ctx.close()
+    extras = run_extras(mg, local) if rank == 0 and a.config == "cfg2" else None
     line = {
         "metric": METRIC, "value": go_ms * 1e-3, "unit": "s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -318,6 +326,8 @@ def run_ours(a, ws, rank, local):
                    "l2": "flushed (256 MB write between steps)", "parallelism": f"replicas x{ws}",
                    "precision": "fp64" if prec == mg.PREC_FP64 else "split"},
         "projections_per_s": S * ws / (proj_ms * 1e-3),
+        "tuning": tuning,
+        "extras": extras,
         "stage_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in tm.items()},
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -327,6 +337,40 @@ def run_ours(a, ws, rank, local):
     }
     line.update(extra)
     return line
+
+
+def run_extras(mg, local):
+    """The rows next to the path at the basis-optimisation size (lmax 1000, 12 functions
+    of 64 cubic B-splines = 364 modes, n_mu 1501, 32 shapes): one objective + gradient
+    (modal_adjoint_residual) and the full greedy pruning (modal_basis_prune), device
+    time with CUDA events on the context stream."""
+    import torch
+    C, Bw, tri, cl = mg.bspline_workload(1000, 12, 64, seed=4)
+    shapes = mg.separable_shapes(1000, 32, 40, 1, 2)
+    out = {"workload": "lmax 1000, 64 B-splines x 12 functions, N=364, n_mu=1501, 32 shapes"}
+    with mg.Context(local) as c:
+        c.set_basis(2, 1000, Bw @ C.T)
+        c.set_modes(tri)
+        c.set_spectrum(cl)
+        c.init_glint()
+        c.gamma(mg.PREC_FP64, download=False)
+        c.orthogonalise(None, download=False)
+        stream = torch.cuda.ExternalStream(c.stream)
+        c.adjoint_residual(shapes)  # warm-up
+        ts = []
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            J, _ = c.adjoint_residual(shapes)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        out["adjoint_residual_ms"] = float(np.median(ts))
+        out["objective_J"] = J
+        t0 = time.perf_counter()
+        order, lam = c.basis_prune()
+        out["basis_prune_364_s"] = time.perf_counter() - t0
+    return out
 
 
 def run_e2e(ctx, mg, q, tr, cl, shapes, prec, steps):

@@ -149,7 +149,8 @@ modal_status modal_get_gl(modal_ctx *ctx, int *nmu, double *nodes, double *weigh
  * gamma may be NULL: the result stays on the device for the next steps. */
 modal_status modal_gamma(modal_ctx *ctx, modal_prec prec, double *gamma);
 
-/* result[0] = Gamma_mn, the per-pair interface of calculate_orthol
+/* result[0] = Gamma_mn (and result[1..3] = TTE, TEE, EEE after
+ * modal_set_modes_pol), the per-pair interface of calculate_orthol
  * (orthogonalisation_late.c:239; global.h:211).  Computes the whole matrix
  * on first use and answers later pairs from it. */
 modal_status modal_orthol_pair(modal_ctx *ctx, int m, int n, double *result);
@@ -245,6 +246,26 @@ modal_status modal_get_tuning(const modal_ctx *ctx, int *proj_sg, int *proj_cpb,
  * beta: host [S][N] or NULL for the device result of modal_project.
  * alpha/modesR: host [S][N] or NULL. */
 modal_status modal_alpha(modal_ctx *ctx, int S, const double *beta, double *alpha, double *modesR);
+
+/* ----------------------------------------------------------- polarisation */
+
+/* E-mode basis qe[L_E][P_E] (basis_late_E layout, fixed_data.c) on
+ * l = lmin_e..lmax_e: the do_polarisation side of init_orthol_glint
+ * (orthogonalisation_late.c:33-37, 68-95).  With it the quadrature and the
+ * P_l table cover max(lmax_T, lmax_E), and modal_init_glint also builds the E
+ * table (calculate_orthoMij_E, :131-157).  Resets everything derived. */
+modal_status modal_set_basis_e(modal_ctx *ctx, int lmin_e, int lmax_e, int P_e, const double *qe);
+
+/* Mode triples of the polarised lists, N each (N of modal_set_modes), in the
+ * conventions of find_perm_late_TTE/TEE/EEE (fixed_data.c): tte[n] = (T,T,E),
+ * tee[n] = (T,E,E), eee[n] = (E,E,E) basis indices.  With them
+ * modal_orthol_pair also fills result[1..3]. */
+modal_status modal_set_modes_pol(modal_ctx *ctx, const int *tte, const int *tee, const int *eee);
+
+/* Gamma_TTE, Gamma_TEE, Gamma_EEE [N][N] (host, each may be NULL): results
+ * [1], [2], [3] of calculate_orthol with do_polarisation
+ * (orthogonalisation_late.c:293-320) over every pair, FP64 on the GPU. */
+modal_status modal_gamma_pol(modal_ctx *ctx, double *gamma_tte, double *gamma_tee, double *gamma_eee);
 
 /* ---------------------------------------------------------------- adjoint */
 

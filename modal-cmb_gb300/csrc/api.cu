@@ -3,6 +3,7 @@
 #include <cstdarg>
 #include <cstdlib>
 #include <vector>
+#include <algorithm>
 #include "common.cuh"
 
 namespace modal {
@@ -163,7 +164,7 @@ void modal_ctx_destroy(modal_ctx *c)
                       &c->orthol, &c->lambdal, &c->norm, &c->info, &c->cl, &c->vl, &c->beta, &c->alpha,
                       &c->modesr, &c->scratch, &c->scratch2, &c->shape_tab, &c->shape_desc, &c->slab_order,
                       &c->split, &c->tr_x, &c->tr_qt, &c->tr_prim, &c->tr_mt, &c->tr_v, &c->tr_out,
-                      &c->adj, &c->adj2, &c->adj3, &c->prune};
+                      &c->adj, &c->adj2, &c->adj3, &c->prune, &c->qe, &c->me, &c->tri_pol, &c->gamma_pol};
     batch_release(c);
     for (DevBuf *b : bufs) release(*b);
     timers_clear(c);
@@ -319,6 +320,7 @@ modal_status modal_set_basis(modal_ctx *c, int lmin, int lmax, int P, const doub
     MODAL_TRY(sync(c));
     c->have_basis = true;
     c->have_glint = c->have_gamma = c->have_ortho = c->have_beta = false;
+    c->have_pol = c->have_gamma_pol = false;  // polarised modes are re-set after the bases
     if (c->have_modes) {
         // re-validate the mode list against the new basis size
         std::vector<int> tr(3 * (size_t)c->N);
@@ -345,6 +347,7 @@ modal_status modal_set_modes(modal_ctx *c, int N, const int *triples)
     MODAL_TRY(sync(c));
     c->have_modes = true;
     c->have_gamma = c->have_ortho = c->have_beta = false;
+    c->have_pol = c->have_gamma_pol = false;
     return MODAL_OK;
 }
 
@@ -367,8 +370,11 @@ modal_status modal_init_glint(modal_ctx *c)
 {
     MODAL_TRY(need(c, c && c->have_basis, "modal_init_glint: set the basis first"));
     MODAL_CUDA(cudaSetDevice(c->device));
+    // with an E basis the quadrature and the P_l table cover max(lmax_T, lmax_E)
+    // (orthogonalisation_late.c:33-37)
+    const int lmax_all = c->have_basis_e ? std::max(c->lmax, c->lmax_e) : c->lmax;
     if (!c->have_user_gl) {
-        c->nmu = 3 * c->lmax / 2 + 1;  // orthogonalisation_late.c:37
+        c->nmu = 3 * lmax_all / 2 + 1;  // orthogonalisation_late.c:37
         if (c->gl_n != c->nmu) {      // the nodes depend on n only: computed once per n
             MODAL_TRY(ensure(c->mu, sizeof(double) * c->nmu));
             MODAL_TRY(ensure(c->w, sizeof(double) * c->nmu));
@@ -377,18 +383,20 @@ modal_status modal_init_glint(modal_ctx *c)
             c->gl_n = c->nmu;
         }
     }
-    MODAL_TRY(ensure(c->pl, sizeof(double) * (size_t)(c->lmax + 1) * c->nmu));
+    MODAL_TRY(ensure(c->pl, sizeof(double) * (size_t)(lmax_all + 1) * c->nmu));
     {
         StageTimer t(c, MODAL_T_PL);
-        MODAL_TRY(legendre_table_dev(c, c->nmu, c->lmax, c->mu.as<double>(), c->pl.as<double>()));
+        MODAL_TRY(legendre_table_dev(c, c->nmu, lmax_all, c->mu.as<double>(), c->pl.as<double>()));
     }
     {
         StageTimer t(c, MODAL_T_MIJ);
         MODAL_TRY(mij_dev(c));
+        if (c->have_basis_e)  // calculate_orthoMij_E (orthogonalisation_late.c:131-157)
+            MODAL_TRY(mij_table_dev(c, c->qe.as<double>(), c->lmin_e, c->lmax_e, c->P_e, c->me));
     }
     MODAL_TRY(sync(c));
     c->have_glint = true;
-    c->have_gamma = c->have_ortho = false;
+    c->have_gamma = c->have_ortho = c->have_gamma_pol = false;
     return MODAL_OK;
 }
 
@@ -439,6 +447,12 @@ modal_status modal_orthol_pair(modal_ctx *c, int m, int n, double *result)
     MODAL_CUDA(cudaSetDevice(c->device));
     if (!c->have_gamma) MODAL_TRY(modal_gamma(c, MODAL_PREC_FP64, nullptr));
     MODAL_TRY(d2h(c, result, c->gamma.as<double>() + (size_t)m * c->N + n, sizeof(double)));
+    if (c->have_pol) {  // result[1..3] = TTE, TEE, EEE as with do_polarisation
+        if (!c->have_gamma_pol) MODAL_TRY(modal_gamma_pol(c, nullptr, nullptr, nullptr));
+        const size_t NN = (size_t)c->N * c->N;
+        for (int f = 0; f < 3; f++)
+            MODAL_TRY(d2h(c, result + 1 + f, c->gamma_pol.as<double>() + f * NN + (size_t)m * c->N + n, sizeof(double)));
+    }
     return sync(c);
 }
 

@@ -81,6 +81,14 @@ struct modal_ctx {
     // adjoint: shape legs and forward products, per-mu adjoints, upstreams
     modal::DevBuf adj, adj2, adj3;
     modal::DevBuf prune;  // basis pruning: normalised Gamma, minors, eigenvalues, work
+
+    // polarisation: E basis, E-mode M table, TTE/TEE/EEE triples, their Gammas
+    bool have_basis_e = false, have_pol = false, have_gamma_pol = false;
+    int lmin_e = 0, lmax_e = 0, L_e = 0, P_e = 0;
+    modal::DevBuf qe;         // [L_e][P_e]
+    modal::DevBuf me;         // [nmu][P_e][P_e]
+    modal::DevBuf tri_pol;    // [3][N][3]: TTE (T,T,E), TEE (T,E,E), EEE (E,E,E)
+    modal::DevBuf gamma_pol;  // [3][N][N]
     double *h_info = nullptr;  // pinned readback
 
     // profiling: event pairs per stage, summed on read
@@ -139,6 +147,7 @@ struct StageTimer {
 modal_status gl_nodes_dev(modal_ctx *ctx, int n, double *d_mu, double *d_w);
 modal_status legendre_table_dev(modal_ctx *ctx, int nmu, int lmax, const double *d_mu, double *d_pl);
 modal_status mij_dev(modal_ctx *ctx);
+modal_status mij_table_dev(modal_ctx *ctx, const double *q, int lmin, int lmax, int P, DevBuf &out);
 modal_status gamma_fp64_dev(modal_ctx *ctx);
 modal_status gamma_split_dev(modal_ctx *ctx);
 modal_status ortho_dev(modal_ctx *ctx, int pca_flag);

@@ -73,10 +73,11 @@ __global__ void __launch_bounds__(256) k_mij_fp64(int nmu, int lmin, int lmax, i
     }
 }
 
-modal_status mij_dev(modal_ctx *ctx)
+// M table [nmu][P][P] of a basis q[L][P] on lmin..lmax (T or E) into out.
+modal_status mij_table_dev(modal_ctx *ctx, const double *q, int lmin, int lmax, int P, DevBuf &out)
 {
-    const int P = ctx->P, npair = P * (P + 1) / 2;
-    MODAL_TRY(ensure(ctx->mt, sizeof(double) * (size_t)ctx->nmu * P * P));
+    const int npair = P * (P + 1) / 2;
+    MODAL_TRY(ensure(out, sizeof(double) * (size_t)ctx->nmu * P * P));
     MODAL_TRY(ensure(ctx->scratch, sizeof(int2) * npair));
     int2 *h = new int2[npair];
     int u = 0;
@@ -87,9 +88,14 @@ modal_status mij_dev(modal_ctx *ctx)
     delete[] h;
     if (e != cudaSuccess) { set_error("mij pairs: %s", cudaGetErrorString(e)); return MODAL_ERR_CUDA; }
     dim3 grid(ceil_div(ctx->nmu, MIJ_BK), ceil_div(npair, MIJ_BU));
-    k_mij_fp64<<<grid, 256, 0, ctx->stream>>>(ctx->nmu, ctx->lmin, ctx->lmax, P, npair, ctx->pl.as<double>(),
-                                              ctx->q.as<double>(), ctx->scratch.as<int2>(), ctx->mt.as<double>());
+    k_mij_fp64<<<grid, 256, 0, ctx->stream>>>(ctx->nmu, lmin, lmax, P, npair, ctx->pl.as<double>(), q,
+                                              ctx->scratch.as<int2>(), out.as<double>());
     return launched(ctx, "mij_fp64");
+}
+
+modal_status mij_dev(modal_ctx *ctx)
+{
+    return mij_table_dev(ctx, ctx->q.as<double>(), ctx->lmin, ctx->lmax, ctx->P, ctx->mt);
 }
 
 // --------------------------------------------------------------------------

@@ -34,6 +34,7 @@ EXPORTS = [
     "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
     "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
+    "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
@@ -105,6 +106,9 @@ def lib():
             "modal_ctx_captures": (l, [vp]),
             "modal_autotune": (i, [vp, ctypes.c_char_p]),
             "modal_get_tuning": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
+            "modal_set_basis_e": (i, [vp, i, i, i, vp]),
+            "modal_set_modes_pol": (i, [vp, vp, vp, vp]),
+            "modal_gamma_pol": (i, [vp, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -280,10 +284,24 @@ class Context:
         _check(lib().modal_gamma(self.h, prec, _ptr(out)))
         return out
 
-    def orthol_pair(self, m, n):
+    def orthol_pair(self, m, n, all_four=False):
         r = np.zeros(4)
         _check(lib().modal_orthol_pair(self.h, m, n, _ptr(r)))
-        return r[0]
+        return r if all_four else r[0]
+
+    def set_basis_e(self, lmin, lmax, qe):
+        qe = _f64(qe)
+        assert qe.shape[0] == lmax - lmin + 1
+        _check(lib().modal_set_basis_e(self.h, lmin, lmax, qe.shape[1], _ptr(qe)))
+
+    def set_modes_pol(self, tte, tee, eee):
+        t = [np.ascontiguousarray(x, dtype=np.int32).reshape(-1, 3) for x in (tte, tee, eee)]
+        _check(lib().modal_set_modes_pol(self.h, _ptr(t[0]), _ptr(t[1]), _ptr(t[2])))
+
+    def gamma_pol(self):
+        outs = [np.empty((self.N, self.N)) for _ in range(3)]
+        _check(lib().modal_gamma_pol(self.h, _ptr(outs[0]), _ptr(outs[1]), _ptr(outs[2])))
+        return tuple(outs)
 
     def orthogonalise(self, gamma=None, pca_flag=1, download=True):
         g = None if gamma is None else _f64(gamma)

@@ -199,6 +199,45 @@ int orc_gamma(int N, const int *triples, int P, int nmu, const double *M, const 
     return 0;
 }
 
+/* Polarised Gamma, results[1..3] of calculate_orthol with do_polarisation
+ * (orthogonalisation_late.c:293-320).  M tables as Mij_T / Mij_E
+ * [P][P][nmu]; mode triples in the find_perm_late_XXX conventions:
+ * tte[n] = (T, T, E), tee[n] = (T, E, E), eee[n] = (E, E, E).
+ *   TTE: sum_k w_k/(16 pi) (MT[a0][b0] MT[a1][b1] + MT[a1][b0] MT[a0][b1]) ME[a2][b2]
+ *   TEE: sum_k w_k/(16 pi) MT[a0][b0] (ME[a1][b1] ME[a2][b2] + ME[a2][b1] ME[a1][b2])
+ *   EEE: as TTT with ME and w_k/(48 pi).
+ * Any output may be NULL. */
+int orc_gamma_pol(int N, const int *tte, const int *tee, const int *eee, int PT, int PE, int nmu, const double *MT,
+                  const double *ME, const double *w, double *g_tte, double *g_tee, double *g_eee)
+{
+#define ORC_MT(a, b, k) MT[((long)(a) * PT + (b)) * nmu + (k)]
+#define ORC_ME(a, b, k) ME[((long)(a) * PE + (b)) * nmu + (k)]
+    #pragma omp parallel for schedule(dynamic, 4)
+    for (int m = 0; m < N; m++)
+        for (int n = m; n < N; n++) {
+            double r2 = 0.0, r3 = 0.0;
+            const int *a = tte + 3 * m, *b = tte + 3 * n, *c = tee + 3 * m, *d = tee + 3 * n;
+            for (int k = 0; k < nmu; k++) {
+                const double wgt2 = w[k] / (16e0 * ORC_PI);
+                double s1 = ORC_MT(a[0], b[0], k) * ORC_MT(a[1], b[1], k) * ORC_ME(a[2], b[2], k);
+                double s2 = ORC_MT(a[1], b[0], k) * ORC_MT(a[0], b[1], k) * ORC_ME(a[2], b[2], k);
+                r2 += wgt2 * (s1 + s2);
+                s1 = ORC_MT(c[0], d[0], k) * ORC_ME(c[1], d[1], k) * ORC_ME(c[2], d[2], k);
+                s2 = ORC_MT(c[0], d[0], k) * ORC_ME(c[2], d[1], k) * ORC_ME(c[1], d[2], k);
+                r3 += wgt2 * (s1 + s2);
+            }
+            if (g_tte) g_tte[(long)m * N + n] = g_tte[(long)n * N + m] = r2;
+            if (g_tee) g_tee[(long)m * N + n] = g_tee[(long)n * N + m] = r3;
+            if (g_eee) {
+                double g = orthol_pair(PE, nmu, ME, w, eee + 3 * m, eee + 3 * n);
+                g_eee[(long)m * N + n] = g_eee[(long)n * N + m] = g;
+            }
+        }
+#undef ORC_MT
+#undef ORC_ME
+    return 0;
+}
+
 /* Gamma for the first `npairs` upper-triangle pairs (row-major order) only,
  * for bounded CPU timing samples; returns the number of pairs done. */
 long orc_gamma_sample(int N, const int *triples, int P, int nmu, const double *M, const double *w, int nthreads,

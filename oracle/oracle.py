@@ -87,6 +87,7 @@ class Oracle:
             ("orc_calculate_modes", i, [i, i, i, vp, i, vp, i, vp, vp]),
             ("orc_integrate_cubic_spline", d, [vp, vp, i]),
             ("orc_gamma_transfer", i, [i, i, i, vp, i, vp, vp, i, vp, vp, i, vp, i, vp, i, vp, d, vp]),
+            ("orc_gamma_pol", i, [i, vp, vp, vp, i, i, i, vp, vp, vp, vp, vp, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -200,6 +201,17 @@ class Oracle:
                                   qt.shape[1], _p(qt), Nprim, _p(prim), float(dphi), _p(out))
         return out
 
+    def gamma_pol(self, MT, ME, w, tte, tee, eee):
+        """(Gamma_TTE, Gamma_TEE, Gamma_EEE) from Mij_T / Mij_E [P][P][nmu]."""
+        MT, ME = np.ascontiguousarray(MT), np.ascontiguousarray(ME)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        t = [np.ascontiguousarray(x, dtype=np.int32) for x in (tte, tee, eee)]
+        N = t[0].shape[0]
+        outs = [np.empty((N, N)) for _ in range(3)]
+        self.L.orc_gamma_pol(N, _p(t[0]), _p(t[1]), _p(t[2]), MT.shape[0], ME.shape[0], MT.shape[2], _p(MT), _p(ME),
+                             _p(w), _p(outs[0]), _p(outs[1]), _p(outs[2]))
+        return tuple(outs)
+
     def ortho_cholesky(self, gamma):
         """Cholesky branch; returns (orthol, lambdal, fail) with fail = -1 or the failing pivot row."""
         g = np.ascontiguousarray(gamma, dtype=np.float64)
@@ -263,6 +275,8 @@ class Ref:
             ("ref_modify_bispectrum", i, [i, vp, vp]),
             ("ref_calculate_modes", i, [i, vp, vp]),
             ("ref_gamma_transfer", i, [i, vp, i, vp, i, vp, d, vp]),
+            ("ref_setup_pol", i, [i, i, i, vp, vp, vp, vp]),
+            ("ref_gamma_pol", i, [vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -290,6 +304,19 @@ class Ref:
 
     def init_gamma(self):
         self.L.ref_init_gamma()
+
+    def setup_pol(self, lminE, lmaxE, qE, tte, tee, eee):
+        """After setup(): E basis [L_E][P_E] and TTE/TEE/EEE triples (find_perm conventions)."""
+        qE = np.ascontiguousarray(qE, dtype=np.float64)
+        t = [np.ascontiguousarray(x, dtype=np.int32) for x in (tte, tee, eee)]
+        self._keep_pol = (qE, t)
+        self.L.ref_setup_pol(lminE, lmaxE, qE.shape[1], _p(qE), _p(t[0]), _p(t[1]), _p(t[2]))
+
+    def gamma_pol(self):
+        """[4][N][N]: TTT, TTE, TEE, EEE from calculate_orthol over every pair."""
+        out = np.zeros((4, self.N, self.N))
+        self.L.ref_gamma_pol(_p(out))
+        return out
 
     def orthol_pair(self, m, n):
         r = np.zeros(4)

@@ -39,6 +39,7 @@ int offload_target = 0;
 extern int asy(double *nodes, double *weights, unsigned long n);
 extern double init_orthol_glint(void);
 extern void calculate_orthoMij_T(int i, int j);
+extern void calculate_orthoMij_E(int i, int j);
 extern void sync_orthoMij(void);
 extern int calculate_orthol(int m, int n, double *result);
 extern double plijk_TTT(int r, int i, int j, int k);
@@ -57,6 +58,11 @@ extern void calculate_mode_3D(int min, int max, ref_tetrapyd_limits *block, doub
 static int g_P, g_N, g_L;
 static double *g_basis;   /* [L][P] */
 static int *g_triples;    /* [N][3] */
+/* polarisation (ref_setup_pol): E basis [L_E][P_E], TTE/TEE/EEE triples in
+ * the find_perm_late_XXX conventions (T,T,E), (T,E,E), (E,E,E) */
+static int g_PE;
+static double *g_basisE;
+static int *g_tte, *g_tee, *g_eee;
 static double *g_cl;      /* [lmax+1], C_l + N_l/b_l^2 */
 static orc_shape g_shape;
 
@@ -106,14 +112,15 @@ double gsl_sf_legendre_Pl(int l, double x)
 
 /* ---- fixed_data.c accessors ---- */
 int get_pmax_late_T(void) { return g_P - 1; }
-int get_pmax_late_E(void) { return g_P - 1; }
+int get_pmax_late_E(void) { return do_polarisation ? g_PE - 1 : g_P - 1; }
 double get_basis_late_T(int i, int j) { return g_basis[(long)i * g_P + j]; }
-double get_basis_late_E(int i, int j) { return g_basis[(long)i * g_P + j]; }
+double get_basis_late_E(int i, int j) { return do_polarisation ? g_basisE[(long)i * g_PE + j] : g_basis[(long)i * g_P + j]; }
 static void perm_of(int r, int *p1, int *p2, int *p3) { *p1 = g_triples[3 * r]; *p2 = g_triples[3 * r + 1]; *p3 = g_triples[3 * r + 2]; }
 void find_perm_late_TTT(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
-void find_perm_late_TTE(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
-void find_perm_late_TEE(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
-void find_perm_late_EEE(int r, int *p1, int *p2, int *p3) { perm_of(r, p1, p2, p3); }
+static void perm_in(const int *t, int r, int *p1, int *p2, int *p3) { *p1 = t[3 * r]; *p2 = t[3 * r + 1]; *p3 = t[3 * r + 2]; }
+void find_perm_late_TTE(int r, int *p1, int *p2, int *p3) { if (do_polarisation) perm_in(g_tte, r, p1, p2, p3); else perm_of(r, p1, p2, p3); }
+void find_perm_late_TEE(int r, int *p1, int *p2, int *p3) { if (do_polarisation) perm_in(g_tee, r, p1, p2, p3); else perm_of(r, p1, p2, p3); }
+void find_perm_late_EEE(int r, int *p1, int *p2, int *p3) { if (do_polarisation) perm_in(g_eee, r, p1, p2, p3); else perm_of(r, p1, p2, p3); }
 int get_terms_late(void) { return g_N; }
 int get_terms_prim(void) { return g_N; }
 int get_lmax(void) { return eflag_T_lmax; }
@@ -177,6 +184,7 @@ double get_modesR_TTT(int i) { (void)i; return 0.0; }
 int ref_setup(int lmin, int lmax, int P, const double *basis, int N, const int *triples, const double *cl)
 {
     g_P = P; g_N = N; g_L = lmax - lmin + 1;
+    do_polarisation = 0;
     eflag_T_lmin = eflag_E_lmin = lmin;
     eflag_T_lmax = eflag_E_lmax = lmax;
     free(g_basis); free(g_triples); free(g_cl);
@@ -209,7 +217,46 @@ int ref_init_gamma(void)
     init_orthol_glint();
     for (int i = 0; i < g_P; i++)
         for (int j = 0; j < g_P; j++) calculate_orthoMij_T(i, j);
+    if (do_polarisation)
+        for (int i = 0; i < g_PE; i++)
+            for (int j = 0; j < g_PE; j++) calculate_orthoMij_E(i, j);
     sync_orthoMij();
+    return 0;
+}
+
+/* Switch on polarisation after ref_setup: the E basis [lmaxE-lminE+1][PE]
+ * (basis_late_E layout) and the TTE/TEE/EEE mode triples [N][3] as
+ * find_perm_late_XXX returns them. */
+int ref_setup_pol(int lminE, int lmaxE, int PE, const double *basisE, const int *tte, const int *tee, const int *eee)
+{
+    const int LE = lmaxE - lminE + 1;
+    eflag_E_lmin = lminE;
+    eflag_E_lmax = lmaxE;
+    g_PE = PE;
+    free(g_basisE); free(g_tte); free(g_tee); free(g_eee);
+    g_basisE = malloc(sizeof(double) * (size_t)LE * PE);
+    g_tte = malloc(sizeof(int) * 3 * (size_t)g_N);
+    g_tee = malloc(sizeof(int) * 3 * (size_t)g_N);
+    g_eee = malloc(sizeof(int) * 3 * (size_t)g_N);
+    memcpy(g_basisE, basisE, sizeof(double) * (size_t)LE * PE);
+    memcpy(g_tte, tte, sizeof(int) * 3 * (size_t)g_N);
+    memcpy(g_tee, tee, sizeof(int) * 3 * (size_t)g_N);
+    memcpy(g_eee, eee, sizeof(int) * 3 * (size_t)g_N);
+    do_polarisation = 1;
+    return 0;
+}
+
+/* All four matrices of calculate_orthol (TTT, TTE, TEE, EEE) over every
+ * pair, out[4][N][N] (ortho_late_mpi.c:261-287 fills ortho_XXX the same way). */
+int ref_gamma_pol(double *out)
+{
+    const long N = g_N, NN = N * N;
+    for (long i = 0; i < N; i++)
+        for (long j = i; j < N; j++) {
+            double r[4];
+            calculate_orthol((int)i, (int)j, r);
+            for (int c = 0; c < 4; c++) out[c * NN + i * N + j] = out[c * NN + j * N + i] = r[c];
+        }
     return 0;
 }
 

@@ -126,9 +126,43 @@ def prune_golden():
     print("basis_prune done", order_a.size, order_b.size)
 
 
+def pol_inputs(lmaxT=50, lmaxE=60, lminE=3, PT=4, PE=4):
+    """Polarised case: T basis on 2..lmaxT, E basis on lminE..lmaxE with its own
+    weight, TTE/TEE/EEE triples in the find_perm_late_XXX conventions."""
+    cl = M.synthetic_cl(max(lmaxT, lmaxE))
+    qT = M.weighted_q(M.legendre_q(2, lmaxT, PT), cl, 2)
+    qE = M.weighted_q(M.legendre_q(lminE, lmaxE, PE), cl * 2.0, lminE)
+    ttt = M.mode_triples(PT)
+    N = len(ttt)
+    tte = np.array([(p, r, s) for p in range(PT) for r in range(p, PT) for s in range(PE)][:N], dtype=np.int32)
+    tee = np.array([(t, a, b) for t in range(PT) for a in range(PE) for b in range(a, PE)][:N], dtype=np.int32)
+    eee = M.mode_triples(PE)[:N]
+    return cl, qT, qE, ttt, tte, tee, eee
+
+
+def pol_golden():
+    """9. polarised Gamma: calculate_orthol's four results with do_polarisation."""
+    lmaxT, lmaxE, lminE = 50, 60, 3
+    cl, qT, qE, ttt, tte, tee, eee = pol_inputs(lmaxT, lmaxE, lminE)
+    ref = O.Ref()
+    ref.setup(2, lmaxT, qT, ttt, cl)
+    ref.setup_pol(lminE, lmaxE, qE, tte, tee, eee)
+    with O.quiet_stdout():
+        ref.init_gamma()
+    G = ref.gamma_pol()
+    nmu = 3 * max(lmaxT, lmaxE) // 2 + 1
+    x, w = ref.asy(nmu)
+    np.savez_compressed(os.path.join(OUT, "gamma_pol.npz"), gamma=G, nodes=x, weights=w,
+                        dims=np.array([lmaxT, lmaxE, lminE]))
+    print("gamma_pol done", G.shape)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["prune"]:
         prune_golden()
+    elif sys.argv[1:] == ["pol"]:
+        pol_golden()
     else:
         main()
         prune_golden()
+        pol_golden()

@@ -231,3 +231,20 @@ def test_basis_prune_matches_reference_driver(golden, case):
     assert np.array_equal(order, g["order_" + case])
     # the reference prints lambda with %e (7 significant digits)
     assert np.max(np.abs(lam - g["lam_" + case]) / np.abs(lam)) <= 6e-7
+
+
+def test_polarised_gamma_oracle_vs_reference(orc, golden):
+    # calculate_orthol with do_polarisation: TTT, TTE, TEE, EEE (the reference in place)
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden import pol_inputs
+    g = golden("gamma_pol")
+    lmaxT, lmaxE, lminE = (int(v) for v in g["dims"])
+    cl, qT, qE, ttt, tte, tee, eee = pol_inputs(lmaxT, lmaxE, lminE)
+    pl = orc.legendre_table(g["nodes"], max(lmaxT, lmaxE))
+    MT = orc.mij(np.ascontiguousarray(pl[:, :lmaxT + 1]), 2, lmaxT, qT)
+    ME = orc.mij(pl, lminE, lmaxE, qE)
+    gT = orc.gamma(MT, g["weights"], ttt)
+    g1, g2, g3 = orc.gamma_pol(MT, ME, g["weights"], tte, tee, eee)
+    for got, want in zip((gT, g1, g2, g3), g["gamma"]):
+        assert rel_max(got, want) <= 1e-14

@@ -267,6 +267,34 @@ modal_status modal_set_modes_pol(modal_ctx *ctx, const int *tte, const int *tee,
  * (orthogonalisation_late.c:293-320) over every pair, FP64 on the GPU. */
 modal_status modal_gamma_pol(modal_ctx *ctx, double *gamma_tte, double *gamma_tee, double *gamma_eee);
 
+/* Spectra for the E side of the transfer Gamma, arrays over l = 0..lmax_T:
+ * signal C_l, beams b_l and noise N_l of TT, TE and EE, and the sky
+ * fractions (get_cl_XX, get_beam_XX, get_noise_XX, fskyT/fskyE of the
+ * reference's fixed_data.c / parameter.c). */
+typedef struct {
+    const double *cl_tt, *cl_te, *cl_ee;
+    const double *beam_tt, *beam_te, *beam_ee;
+    const double *noise_tt, *noise_te, *noise_ee;
+    double fsky_t, fsky_e;
+} modal_pol_spectra;
+
+/* E transfer functions qtilde_e[xsize][Pp][lmax_T+1] (get_qtilde_E, same grid
+ * and primordial basis as modal_set_transfer) and the spectra of the E weights
+ * (calculate_gamma.c:142-183):
+ *   EEweight_l = (2l+1)^{5/6} b_E / sqrt(s_TT (s_TT s_EE - s_TE^2)),
+ *   q~_E' = EEweight (s_TT q~_E - (sqrt(fsky_E/fsky_T) b_TE^2 C_TE + N_TE) q~_T),
+ *   s_XY = b_X b_Y C_XY + N_XY.
+ * Needs modal_set_transfer, modal_set_basis_e (lmax_E <= lmax_T) and
+ * modal_set_modes_pol.  The TT weight keeps using modal_set_spectrum's
+ * C_l + N_l/b_l^2, which must equal (b_TT^2 C_TT + N_TT)/b_TT^2 here. */
+modal_status modal_set_transfer_pol(modal_ctx *ctx, const double *qtilde_e, const modal_pol_spectra *spectra);
+
+/* Gamma_t TTE, TEE, EEE [N][Nprim] (host, each may be NULL): results [1..3]
+ * of calculate_gamma_2d with do_polarisation (calculate_gamma.c:558-687,
+ * 773-842), scale deltaphi^2/(8 pi), FP64 on the GPU. */
+modal_status modal_gamma_transfer_pol(modal_ctx *ctx, double deltaphi, double *gamma_tte, double *gamma_tee,
+                                      double *gamma_eee);
+
 /* ---------------------------------------------------------------- adjoint */
 
 /* Gradients with respect to the basis values q[L][P] of modal_set_basis, FP64

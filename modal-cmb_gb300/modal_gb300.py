@@ -34,7 +34,8 @@ EXPORTS = [
     "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
     "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
-    "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol",
+    "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol", "modal_set_transfer_pol",
+    "modal_gamma_transfer_pol",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
@@ -44,6 +45,12 @@ class ModalError(RuntimeError):
     def __init__(self, status, msg):
         self.status = status
         super().__init__(f"{STATUS.get(status, status)}: {msg}")
+
+
+class CPolSpectra(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("cl_tt", "cl_te", "cl_ee", "beam_tt", "beam_te", "beam_ee",
+                                                 "noise_tt", "noise_te", "noise_ee")] + \
+               [("fsky_t", ctypes.c_double), ("fsky_e", ctypes.c_double)]
 
 
 class CShape(ctypes.Structure):
@@ -109,6 +116,8 @@ def lib():
             "modal_set_basis_e": (i, [vp, i, i, i, vp]),
             "modal_set_modes_pol": (i, [vp, vp, vp, vp]),
             "modal_gamma_pol": (i, [vp, vp, vp, vp]),
+            "modal_set_transfer_pol": (i, [vp, vp, vp]),
+            "modal_gamma_transfer_pol": (i, [vp, d, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -359,6 +368,18 @@ class Context:
         out = np.empty((self.N, self.Nprim))
         _check(lib().modal_gamma_transfer(self.h, float(deltaphi), _ptr(out)))
         return out
+
+    def set_transfer_pol(self, qtilde_e, spec9, fsky_t, fsky_e):
+        """spec9: cl_tt, cl_te, cl_ee, beam_tt, beam_te, beam_ee, noise_tt, noise_te, noise_ee over l."""
+        qe = _f64(qtilde_e)
+        arrs = [_f64(a) for a in spec9]
+        sp = CPolSpectra(*[a.ctypes.data for a in arrs], float(fsky_t), float(fsky_e))
+        _check(lib().modal_set_transfer_pol(self.h, _ptr(qe), ctypes.byref(sp)))
+
+    def gamma_transfer_pol(self, deltaphi):
+        outs = [np.empty((self.N, self.Nprim)) for _ in range(3)]
+        _check(lib().modal_gamma_transfer_pol(self.h, float(deltaphi), _ptr(outs[0]), _ptr(outs[1]), _ptr(outs[2])))
+        return tuple(outs)
 
     def calculate_modes(self, b):
         b = _f64(b)

@@ -679,3 +679,119 @@ int orc_gamma_transfer(int lmin, int lmax, int P, const double *basis, int N, co
     free(ttw); free(pl); free(M);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Polarised late x primordial transfer Gamma: results[1..3] of             */
+/* calculate_gamma_2d with do_polarisation (calculate_gamma.c).             */
+/*   TTweight_l = (2l+1)^{5/6} b_T / sqrt(s_TT),  s_TT = b_T^2 C_TT + N_TT    */
+/*   EEweight_l = (2l+1)^{5/6} b_E / sqrt(s_TT (s_TT s_EE - s_TE^2))         */
+/*     s_TE = b_T b_E C_TE + N_TE, s_EE = b_E^2 C_EE + N_EE      (:142-157)   */
+/*   q~_E'[x][p][l] = EEweight (s_TT q~_E - (sqrt(fE/fT) b_TE^2 C_TE + N_TE) */
+/*                    q~_T)                                      (:170-181)   */
+/*   M_T = sum_l P_l TTweight q~_T basis_T, M_E = sum_l P_l q~_E' basis_E    */
+/*   TTE/TEE/EEE points: perm3 of [M_{type(b)}[p_a][q_b]] with the late      */
+/*   legs' types (T,T,E), (T,E,E), (E,E,E)                  (:558-687)       */
+/* then the same x^2, zero rule, spline and dphi^2/(8 pi) as TTT.           */
+/* Spectra arrays cover l = 0..max(lmax, lmaxE); lmaxE <= lmax.             */
+/* ------------------------------------------------------------------------ */
+int orc_gamma_transfer_pol(int lmin, int lmax, int P, const double *basisT, int lminE, int lmaxE, int PE,
+                           const double *basisE, int N, const int *tte, const int *tee, const int *eee,
+                           const double *cl_tt, const double *cl_te, const double *cl_ee, const double *b_tt,
+                           const double *b_te, const double *b_ee, const double *n_tt, const double *n_te,
+                           const double *n_ee, double fsky_t, double fsky_e, int nmu, const double *mu,
+                           const double *w, int xsize, const double *xvec, int Pp, const double *qtT,
+                           const double *qtE, int Nprim, const int *prim, double dphi, double *out /*[3][N][Nprim]*/)
+{
+    const int L = lmax - lmin + 1, LE = lmaxE - lminE + 1, lstride = lmax + 1;
+    double *ttw = malloc(sizeof(double) * (size_t)L), *eew = malloc(sizeof(double) * (size_t)LE);
+    for (int i = 0; i < L; i++) {
+        int l = lmin + i;
+        double s2 = b_tt[l] * b_tt[l] * cl_tt[l] + n_tt[l];
+        ttw[i] = (l > 1) ? pow(2e0 * l + 1e0, 5e0 / 6e0) * (b_tt[l] / sqrt(s2)) : 0e0;
+    }
+    for (int i = 0; i < LE; i++) {
+        int l = lminE + i;
+        double s2 = b_tt[l] * b_tt[l] * cl_tt[l] + n_tt[l];
+        double s3 = b_tt[l] * b_ee[l] * cl_te[l] + n_te[l];
+        double s4 = b_ee[l] * b_ee[l] * cl_ee[l] + n_ee[l];
+        eew[i] = (l > 1) ? pow(2e0 * l + 1e0, 5e0 / 6e0) * (b_ee[l] / sqrt(s2 * (s2 * s4 - s3 * s3))) : 0e0;
+    }
+    double *pl = malloc(sizeof(double) * (size_t)nmu * lstride);
+    #pragma omp parallel for
+    for (int k = 0; k < nmu; k++) {
+        double x = mu[k], pm2 = 1.0, pm1 = x;
+        double *row = pl + (long)k * lstride;
+        for (int l = 0; l <= lmax; l++) {
+            double p;
+            if (l == 0) p = 1.0;
+            else if (l == 1) p = x;
+            else {
+                double pr = (x * (2 * l - 1) * pm1 - (l - 1) * pm2) / l;
+                pm2 = pm1; pm1 = pr;
+                p = (l == 2) ? 0.5 * (3.0 * x * x - 1.0) : (x == 1.0 ? 1.0 : (x == -1.0 ? ((l & 1) ? -1.0 : 1.0) : pr));
+            }
+            row[l] = p;
+        }
+    }
+    double *MT = malloc(sizeof(double) * (size_t)Pp * P * xsize * nmu);
+    double *ME = malloc(sizeof(double) * (size_t)Pp * PE * xsize * nmu);
+    #pragma omp parallel for collapse(3)
+    for (int p = 0; p < Pp; p++)
+        for (int xi = 0; xi < xsize; xi++)
+            for (int q = 0; q < (P > PE ? P : PE); q++) {
+                double *vec = malloc(sizeof(double) * (size_t)(L > LE ? L : LE));
+                if (q < P) {
+                    for (int l = 0; l < L; l++)
+                        vec[l] = (ttw[l] * qtT[((long)xi * Pp + p) * lstride + lmin + l]) * basisT[(long)l * P + q];
+                    for (int k = 0; k < nmu; k++) {
+                        double sum = 0;
+                        for (int l = 0; l < L; l++) sum += pl[(long)k * lstride + l + lmin] * vec[l];
+                        MT[(((long)p * P + q) * xsize + xi) * nmu + k] = sum;
+                    }
+                }
+                if (q < PE) {
+                    for (int i = 0; i < LE; i++) {
+                        int l = lminE + i;
+                        double s1 = b_tt[l] * b_tt[l] * cl_tt[l] + n_tt[l];
+                        double s2 = sqrt(fsky_e / fsky_t) * b_te[l] * b_te[l] * cl_te[l] + n_te[l];
+                        double qe = eew[i] * (s1 * qtE[((long)xi * Pp + p) * lstride + l] - s2 * qtT[((long)xi * Pp + p) * lstride + l]);
+                        vec[i] = qe * basisE[(long)i * PE + q];
+                    }
+                    for (int k = 0; k < nmu; k++) {
+                        double sum = 0;
+                        for (int i = 0; i < LE; i++) sum += pl[(long)k * lstride + i + lminE] * vec[i];
+                        ME[(((long)p * PE + q) * xsize + xi) * nmu + k] = sum;
+                    }
+                }
+                free(vec);
+            }
+    const int *lists[3] = {tte, tee, eee};
+    const int nT[3] = {2, 1, 0};
+    #pragma omp parallel for collapse(3) schedule(dynamic, 4)
+    for (int f = 0; f < 3; f++)
+        for (int m = 0; m < N; m++)
+            for (int n = 0; n < Nprim; n++) {
+                const int *pp = prim + 3 * n, *qq = lists[f] + 3 * m;
+                double *y = malloc(sizeof(double) * (size_t)xsize);
+                for (int xi = 0; xi < xsize; xi++) {
+                    const double *c[3][3];
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 3; b++)
+                            c[a][b] = (b < nT[f]) ? MT + (((long)pp[a] * P + qq[b]) * xsize + xi) * nmu
+                                                  : ME + (((long)pp[a] * PE + qq[b]) * xsize + xi) * nmu;
+                    double result = 0.0;
+                    for (int j = 0; j < nmu; j++) {
+                        double s1 = c[0][0][j] * c[1][1][j] * c[2][2][j], s2 = c[0][0][j] * c[1][2][j] * c[2][1][j];
+                        double s3 = c[0][1][j] * c[1][0][j] * c[2][2][j], s4 = c[0][1][j] * c[1][2][j] * c[2][0][j];
+                        double s5 = c[0][2][j] * c[1][0][j] * c[2][1][j], s6 = c[0][2][j] * c[1][1][j] * c[2][0][j];
+                        result += w[j] * (s1 + s2 + s3 + s4 + s5 + s6);
+                    }
+                    y[xi] = xvec[xi] * xvec[xi] * result;
+                    if (xi < 10 && fabs(y[xi]) > 1e-18) y[xi] = 0;
+                }
+                out[((long)f * N + m) * Nprim + n] = orc_integrate_cubic_spline(xvec, y, xsize) * dphi * dphi / (8.0 * ORC_PI);
+                free(y);
+            }
+    free(ttw); free(eew); free(pl); free(MT); free(ME);
+    return 0;
+}

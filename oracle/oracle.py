@@ -88,6 +88,8 @@ class Oracle:
             ("orc_integrate_cubic_spline", d, [vp, vp, i]),
             ("orc_gamma_transfer", i, [i, i, i, vp, i, vp, vp, i, vp, vp, i, vp, i, vp, i, vp, d, vp]),
             ("orc_gamma_pol", i, [i, vp, vp, vp, i, i, i, vp, vp, vp, vp, vp, vp]),
+            ("orc_gamma_transfer_pol", i, [i, i, i, vp, i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                           vp, vp, d, d, i, vp, vp, i, vp, i, vp, vp, i, vp, d, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -212,6 +214,24 @@ class Oracle:
                              _p(w), _p(outs[0]), _p(outs[1]), _p(outs[2]))
         return tuple(outs)
 
+    def gamma_transfer_pol(self, lmin, lmax, qT, lminE, lmaxE, qE, tte, tee, eee, spec9, fsky_t, fsky_e, mu, w,
+                           xvec, qtT, qtE, prim, dphi):
+        """[3][N][Nprim]: TTE, TEE, EEE transfer Gamma (spec9 = cl_tt, cl_te, cl_ee, b_tt, b_te, b_ee,
+        n_tt, n_te, n_ee over l = 0..lmax)."""
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
+        ii = lambda a: np.ascontiguousarray(a, dtype=np.int32)  # noqa: E731
+        qT, qE, spec9, mu, w, xvec, qtT, qtE = map(f, (qT, qE, spec9, mu, w, xvec, qtT, qtE))
+        tte, tee, eee, prim = map(ii, (tte, tee, eee, prim))
+        N, Nprim = tte.shape[0], prim.shape[0]
+        out = np.empty((3, N, Nprim))
+        sp = [spec9[i] for i in range(9)]
+        sp = [np.ascontiguousarray(x) for x in sp]
+        self.L.orc_gamma_transfer_pol(lmin, lmax, qT.shape[1], _p(qT), lminE, lmaxE, qE.shape[1], _p(qE), N, _p(tte),
+                                      _p(tee), _p(eee), *[_p(x) for x in sp], float(fsky_t), float(fsky_e), mu.size,
+                                      _p(mu), _p(w), xvec.size, _p(xvec), qtT.shape[1], _p(qtT), _p(qtE), Nprim,
+                                      _p(prim), float(dphi), _p(out))
+        return out
+
     def ortho_cholesky(self, gamma):
         """Cholesky branch; returns (orthol, lambdal, fail) with fail = -1 or the failing pivot row."""
         g = np.ascontiguousarray(gamma, dtype=np.float64)
@@ -277,6 +297,8 @@ class Ref:
             ("ref_gamma_transfer", i, [i, vp, i, vp, i, vp, d, vp]),
             ("ref_setup_pol", i, [i, i, i, vp, vp, vp, vp]),
             ("ref_gamma_pol", i, [vp]),
+            ("ref_setup_pol_spectra", i, [i, vp, d, d]),
+            ("ref_gamma_transfer_pol", i, [i, vp, i, vp, vp, i, vp, d, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -311,6 +333,17 @@ class Ref:
         t = [np.ascontiguousarray(x, dtype=np.int32) for x in (tte, tee, eee)]
         self._keep_pol = (qE, t)
         self.L.ref_setup_pol(lminE, lmaxE, qE.shape[1], _p(qE), _p(t[0]), _p(t[1]), _p(t[2]))
+
+    def gamma_transfer_pol(self, spec9, fsky_t, fsky_e, xvec, qtT, qtE, prim, dphi):
+        """[4][N][Nprim]: calculate_gamma_2d's TTT, TTE, TEE, EEE with polarisation."""
+        spec9 = np.ascontiguousarray(spec9, dtype=np.float64)
+        xvec, qtT, qtE = (np.ascontiguousarray(a, dtype=np.float64) for a in (xvec, qtT, qtE))
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        self.L.ref_setup_pol_spectra(spec9.shape[1], _p(spec9), float(fsky_t), float(fsky_e))
+        out = np.zeros((4, self.N, prim.shape[0]))
+        self.L.ref_gamma_transfer_pol(xvec.size, _p(xvec), qtT.shape[1], _p(qtT), _p(qtE), prim.shape[0], _p(prim),
+                                      float(dphi), _p(out))
+        return out
 
     def gamma_pol(self):
         """[4][N][N]: TTT, TTE, TEE, EEE from calculate_orthol over every pair."""

@@ -135,17 +135,23 @@ double fskyT = 1.0, fskyE = 1.0;
 int get_qtilde_xsize(void) { return g_xsize; }
 int get_qtilde_xvec(double *v) { for (int i = 0; i < g_xsize; i++) v[i] = g_xvec[i]; return 0; }
 double get_qtilde_T(int p, int l, int x) { return g_qt[((long)x * g_Pp + p) * (eflag_T_lmax + 1) + l]; }
-double get_qtilde_E(int p, int l, int x) { return get_qtilde_T(p, l, x); }
+static double *g_qtE;                               /* polarised runs: g_qtE[x][p][l] */
+double get_qtilde_E(int p, int l, int x)
+{ return g_qtE ? g_qtE[((long)x * g_Pp + p) * (eflag_T_lmax + 1) + l] : get_qtilde_T(p, l, x); }
+/* polarised spectra (ref_setup_pol_spectra): TT, TE, EE signal, beams, noise */
+static double *g_spec;  /* [9][lmax+1]: cl_tt, cl_te, cl_ee, b_tt, b_te, b_ee, n_tt, n_te, n_ee */
+static int g_spec_n;
+#define SPEC(i, l) g_spec[(long)(i) * g_spec_n + (l)]
 int destroy_qtilde(void) { return 0; }
 int get_pmax_prim(void) { return g_Pp - 1; }
 void find_perm_prim(int r, int *p1, int *p2, int *p3) { *p1 = g_prim[3 * r]; *p2 = g_prim[3 * r + 1]; *p3 = g_prim[3 * r + 2]; }
-double get_beam_EE(int l) { (void)l; return 1.0; }
-double get_beam_TE(int l) { (void)l; return 1.0; }
-double get_cl_TE(int l) { (void)l; return 0.0; }
-double get_cl_EE(int l) { (void)l; return 1.0; }
+double get_beam_EE(int l) { return g_spec ? SPEC(5, l) : 1.0; }
+double get_beam_TE(int l) { return g_spec ? SPEC(4, l) : 1.0; }
+double get_cl_TE(int l) { return g_spec ? SPEC(1, l) : 0.0; }
+double get_cl_EE(int l) { return g_spec ? SPEC(2, l) : 1.0; }
 double get_cl_TP(int l) { (void)l; return 0.0; }
-double get_noise_TE(int l) { (void)l; return 0.0; }
-double get_noise_EE(int l) { (void)l; return 0.0; }
+double get_noise_TE(int l) { return g_spec ? SPEC(7, l) : 0.0; }
+double get_noise_EE(int l) { return g_spec ? SPEC(8, l) : 0.0; }
 /* GSL cubic-spline link stubs (calculate_gamma() is not exercised) */
 #include <stdio.h>
 const struct refshim_interp_type *gsl_interp_cspline = NULL;
@@ -157,9 +163,9 @@ void gsl_interp_accel_free(struct refshim_interp_accel *a) { (void)a; }
 void gsl_spline_free(struct refshim_spline *s) { (void)s; }
 int read_eigen(int a, int b, int c) { (void)a; (void)b; (void)c; return 0; }
 double get_eigen(int i) { return i == 0 ? 1.0 : 0.0; }
-double get_cl_TT(int l) { return g_cl[l]; }
-double get_noise_TT(int l) { (void)l; return 0.0; }
-double get_beam_TT(int l) { (void)l; return 1.0; }
+double get_cl_TT(int l) { return g_spec ? SPEC(0, l) : g_cl[l]; }
+double get_noise_TT(int l) { return g_spec ? SPEC(6, l) : 0.0; }
+double get_beam_TT(int l) { return g_spec ? SPEC(3, l) : 1.0; }
 double calculate_ISW_bispectrum(int i, int j, int k) { (void)i; (void)j; (void)k; return 0.0; }
 double calculate_xint_TTT(int a, int b, int c, int n, int xsize, double *xvec)
 { (void)xsize; (void)xvec; return n == 0 ? orc_shape_eval(&g_shape, a, b, c) : 0.0; }
@@ -185,6 +191,7 @@ int ref_setup(int lmin, int lmax, int P, const double *basis, int N, const int *
 {
     g_P = P; g_N = N; g_L = lmax - lmin + 1;
     do_polarisation = 0;
+    free(g_spec); g_spec = NULL; fskyT = fskyE = 1.0;
     eflag_T_lmin = eflag_E_lmin = lmin;
     eflag_T_lmax = eflag_E_lmax = lmax;
     free(g_basis); free(g_triples); free(g_cl);
@@ -411,5 +418,51 @@ int ref_gamma_transfer(int xsize, const double *xvec, int Pp, const double *qt, 
         }
     free(g_xvec); g_xvec = &g_x0; g_xsize = 1; g_Pp = 1;
     free(g_qt); g_qt = NULL; free(g_prim); g_prim = NULL;
+    return 0;
+}
+
+/* Polarised spectra for calculate_gamma's E weights (calculate_gamma.c:76-88,
+ * 142-183): nine arrays over l = 0..n-1 in the order cl_tt, cl_te, cl_ee,
+ * b_tt, b_te, b_ee, n_tt, n_te, n_ee. */
+int ref_setup_pol_spectra(int n, const double *spec9, double fsky_t, double fsky_e)
+{
+    free(g_spec);
+    g_spec = malloc(sizeof(double) * 9 * (size_t)n);
+    memcpy(g_spec, spec9, sizeof(double) * 9 * (size_t)n);
+    g_spec_n = n;
+    fskyT = fsky_t;
+    fskyE = fsky_e;
+    return 0;
+}
+
+extern void precompute_gammaMij_E(void);
+
+/* calculate_gamma_2d for every (late m, primordial n) with do_polarisation:
+ * out[4][N][Nprim] = TTT, TTE, TEE, EEE.  qtT, qtE: [xsize][Pp][lmax_T+1]. */
+int ref_gamma_transfer_pol(int xsize, const double *xvec, int Pp, const double *qtT, const double *qtE, int Nprim,
+                           const int *prim, double dphi, double *out)
+{
+    g_xsize = xsize; g_Pp = Pp; g_Nprim = Nprim; deltaphi = dphi;
+    g_xvec = malloc(sizeof(double) * (size_t)xsize);
+    memcpy(g_xvec, xvec, sizeof(double) * (size_t)xsize);
+    size_t nq = (size_t)xsize * Pp * (eflag_T_lmax + 1);
+    g_qt = malloc(sizeof(double) * nq);
+    g_qtE = malloc(sizeof(double) * nq);
+    memcpy(g_qt, qtT, sizeof(double) * nq);
+    memcpy(g_qtE, qtE, sizeof(double) * nq);
+    g_prim = malloc(sizeof(int) * 3 * (size_t)Nprim);
+    memcpy(g_prim, prim, sizeof(int) * 3 * (size_t)Nprim);
+    init_gamma_glint();
+    precompute_gammaMij_T();
+    precompute_gammaMij_E();
+    const long NP = (long)g_N * Nprim;
+    double r[4];
+    for (int m = 0; m < g_N; m++)
+        for (int n = 0; n < Nprim; n++) {
+            calculate_gamma_2d(m, n, r);
+            for (int c = 0; c < 4; c++) out[c * NP + (long)m * Nprim + n] = r[c];
+        }
+    free(g_xvec); g_xvec = &g_x0; g_xsize = 1; g_Pp = 1;
+    free(g_qt); g_qt = NULL; free(g_qtE); g_qtE = NULL; free(g_prim); g_prim = NULL;
     return 0;
 }

@@ -140,6 +140,49 @@ def pol_inputs(lmaxT=50, lmaxE=60, lminE=3, PT=4, PE=4):
     return cl, qT, qE, ttt, tte, tee, eee
 
 
+def pol_transfer_inputs(lmax=40, lmaxE=34, lminE=2, P=3, PE=3, Pp=3, xsize=30):
+    """Polarised transfer case: T and E bases, TTE/TEE/EEE late triples, synthetic
+    TT/TE/EE spectra with beams, noise and sky fractions, T and E transfer
+    functions on one radial grid.  lmaxE <= lmax."""
+    l = np.arange(lmax + 1.0)
+    ls = np.maximum(l, 2.0)
+    cl_tt = 1e3 / (ls * (ls + 1)) * np.exp(-(l / 1500.0) ** 2)
+    cl_ee = 0.05 * cl_tt
+    cl_te = 0.3 * np.sqrt(cl_tt * cl_ee) * np.cos(l / 7.0)
+    b_tt = np.exp(-l * (l + 1) * 1e-5)
+    b_ee = np.exp(-l * (l + 1) * 2e-5)
+    b_te = np.sqrt(b_tt * b_ee)
+    n_tt, n_ee, n_te = 1e-4 * np.ones_like(l), 3e-4 * np.ones_like(l), 1e-6 * np.ones_like(l)
+    spec9 = np.stack([cl_tt, cl_te, cl_ee, b_tt, b_te, b_ee, n_tt, n_te, n_ee])
+    cl_total = (b_tt ** 2 * cl_tt + n_tt) / b_tt ** 2  # the TT weight's C_l + N_l/b_l^2
+    qT = M.legendre_q(2, lmax, P)
+    qE = M.legendre_q(lminE, lmaxE, PE) * 0.7
+    ttt = M.mode_triples(P)
+    N = len(ttt)
+    tte = np.array([(p, r, s) for p in range(P) for r in range(p, P) for s in range(PE)][:N], dtype=np.int32)
+    tee = np.array([(t, a, b) for t in range(P) for a in range(PE) for b in range(a, PE)][:N], dtype=np.int32)
+    eee = M.mode_triples(PE)[:N]
+    xvec, qtT = transfer_inputs(lmax, Pp, xsize)
+    _, qtE = transfer_inputs(lmax, Pp, xsize)
+    qtE = qtE * 0.5 + 0.1 * np.roll(qtT, 1, axis=1)
+    prim = M.mode_triples(Pp)
+    return dict(lmax=lmax, lmaxE=lmaxE, lminE=lminE, spec9=spec9, cl_total=cl_total, qT=qT, qE=qE, ttt=ttt, tte=tte,
+                tee=tee, eee=eee, xvec=xvec, qtT=qtT, qtE=qtE, prim=prim, fsky_t=0.7, fsky_e=0.5, dphi=0.7)
+
+
+def pol_transfer_golden():
+    """10. polarised transfer Gamma: calculate_gamma_2d's four results."""
+    d = pol_transfer_inputs()
+    ref = O.Ref()
+    ref.setup(2, d["lmax"], d["qT"], d["ttt"], d["cl_total"])
+    ref.setup_pol(d["lminE"], d["lmaxE"], d["qE"], d["tte"], d["tee"], d["eee"])
+    G = ref.gamma_transfer_pol(d["spec9"], d["fsky_t"], d["fsky_e"], d["xvec"], d["qtT"], d["qtE"], d["prim"], d["dphi"])
+    nmu = 3 * d["lmax"] // 2 + 1
+    x, w = ref.asy(nmu)
+    np.savez_compressed(os.path.join(OUT, "gamma_transfer_pol.npz"), gamma=G, nodes=x, weights=w)
+    print("gamma_transfer_pol done", G.shape)
+
+
 def pol_golden():
     """9. polarised Gamma: calculate_orthol's four results with do_polarisation."""
     lmaxT, lmaxE, lminE = 50, 60, 3
@@ -162,7 +205,9 @@ if __name__ == "__main__":
         prune_golden()
     elif sys.argv[1:] == ["pol"]:
         pol_golden()
+        pol_transfer_golden()
     else:
         main()
         prune_golden()
         pol_golden()
+        pol_transfer_golden()

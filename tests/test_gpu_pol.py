@@ -64,3 +64,23 @@ def test_pol_argument_checks(mg):
         c.set_modes(ttt)  # a new TTT list drops the polarised one
         with pytest.raises(mg.ModalError):
             c.gamma_pol()
+
+
+def test_pol_transfer_gamma_vs_reference(mg, golden):
+    from make_golden import pol_transfer_inputs
+    g = golden("gamma_transfer_pol")
+    d = pol_transfer_inputs()
+    with mg.Context(0) as c:
+        c.set_basis(2, d["lmax"], d["qT"])
+        c.set_modes(d["ttt"])
+        c.set_spectrum(d["cl_total"])
+        c.set_basis_e(d["lminE"], d["lmaxE"], d["qE"])
+        c.set_modes_pol(d["tte"], d["tee"], d["eee"])
+        c.set_gl(g["nodes"], g["weights"])
+        c.set_transfer(d["xvec"], d["qtT"], d["prim"])
+        c.set_transfer_pol(d["qtE"], d["spec9"], d["fsky_t"], d["fsky_e"])
+        ttt = c.gamma_transfer(d["dphi"])
+        got = c.gamma_transfer_pol(d["dphi"])
+    assert rel_max(ttt, g["gamma"][0]) <= 1e-12
+    for f in range(3):
+        assert rel_fro(got[f], g["gamma"][f + 1]) <= 1e-12 and rel_max(got[f], g["gamma"][f + 1]) <= 1e-12

@@ -248,3 +248,17 @@ def test_polarised_gamma_oracle_vs_reference(orc, golden):
     g1, g2, g3 = orc.gamma_pol(MT, ME, g["weights"], tte, tee, eee)
     for got, want in zip((gT, g1, g2, g3), g["gamma"]):
         assert rel_max(got, want) <= 1e-14
+
+
+def test_polarised_transfer_oracle_vs_reference(orc, golden):
+    # calculate_gamma_2d with do_polarisation (E weights, calculate_gamma.c:142-183)
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden import pol_transfer_inputs
+    g = golden("gamma_transfer_pol")
+    d = pol_transfer_inputs()
+    out = orc.gamma_transfer_pol(2, d["lmax"], d["qT"], d["lminE"], d["lmaxE"], d["qE"], d["tte"], d["tee"], d["eee"],
+                                 d["spec9"], d["fsky_t"], d["fsky_e"], g["nodes"], g["weights"], d["xvec"], d["qtT"],
+                                 d["qtE"], d["prim"], d["dphi"])
+    for f in range(3):
+        assert rel_max(out[f], g["gamma"][f + 1]) <= 1e-14

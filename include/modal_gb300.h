@@ -295,6 +295,33 @@ modal_status modal_set_transfer_pol(modal_ctx *ctx, const double *qtilde_e, cons
 modal_status modal_gamma_transfer_pol(modal_ctx *ctx, double deltaphi, double *gamma_tte, double *gamma_tee,
                                       double *gamma_eee);
 
+/* ------------------------------------------------- primordial k-space side */
+
+/* Points of the primordial k-grid tetrapyd in the order of get_ijk_next_prim
+ * from (min,min,min) (tetrapyd_tools.c:416-550): min <= i < max, i <= j <= max,
+ * j <= k <= min(max, i+j+2), then the end point (max,max,max) that
+ * decompose_tetrapyd_prim also counts.  *npts = their number; pts[npts][3]
+ * (host, or NULL for the count only) enumerated on the current GPU. */
+modal_status modal_prim_points(int min, int max, long *npts, int *pts);
+
+/* Gram matrix of the primordial modes on that grid, calculate_ortho
+ * (orthogonalisation.c:14-86): sum over points of
+ *   calculate_weight(min,max,i,j,k) dk^3 / (dk (i+j+k)) pijk_r pijk_s,
+ * dk = kmax/max, pijk the symmetrised product of basis[l][p] (get_basis_prim,
+ * basis [max+1][P] on grid indices), modes prim[N][3] (find_perm_prim).
+ * ortho: host [N(N+1)/2], the reference's packed upper triangle (r <= s,
+ * row by row).  FP64 on the GPU. */
+modal_status modal_prim_ortho(modal_ctx *ctx, int min, int max, double kmax, int P, const double *basis, int N,
+                              const int *prim, double *ortho);
+
+/* Projection of S primordial shapes onto the modes, calculate_eigen
+ * (calculate_eigen.c:86-144): alpha[s][r] = sum over points of the same weight
+ * times S_s pijk_r, and norm2[s] = sum weight S_s^2 (integrate_template2,
+ * :13-84; NULL to skip).  Shapes as modal_shape with separable tables over
+ * grid indices 0..max; min >= 1.  FP64 on the GPU. */
+modal_status modal_prim_eigen(modal_ctx *ctx, int min, int max, double kmax, int P, const double *basis, int N,
+                              const int *prim, int S, const modal_shape *shapes, double *alpha, double *norm2);
+
 /* ---------------------------------------------------------------- adjoint */
 
 /* Gradients with respect to the basis values q[L][P] of modal_set_basis, FP64

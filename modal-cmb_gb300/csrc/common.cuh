@@ -93,6 +93,9 @@ struct modal_ctx {
     modal::DevBuf me;         // [nmu][P_e][P_e]
     modal::DevBuf tri_pol;    // [3][N][3]: TTE (T,T,E), TEE (T,E,E), EEE (E,E,E)
     modal::DevBuf gamma_pol;  // [3][N][N]
+
+    // primordial k-space side (prim.cu): grid offsets, basis, chunk buffers
+    modal::DevBuf prim;
     double *h_info = nullptr;  // pinned readback
 
     // profiling: event pairs per stage, summed on read

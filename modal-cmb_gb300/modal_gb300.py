@@ -35,7 +35,7 @@ EXPORTS = [
     "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
     "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol", "modal_set_transfer_pol",
-    "modal_gamma_transfer_pol",
+    "modal_gamma_transfer_pol", "modal_prim_points", "modal_prim_ortho", "modal_prim_eigen",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
@@ -118,6 +118,9 @@ def lib():
             "modal_gamma_pol": (i, [vp, vp, vp, vp]),
             "modal_set_transfer_pol": (i, [vp, vp, vp]),
             "modal_gamma_transfer_pol": (i, [vp, d, vp, vp, vp]),
+            "modal_prim_points": (i, [i, i, ctypes.POINTER(l), vp]),
+            "modal_prim_ortho": (i, [vp, i, i, d, i, vp, i, vp, vp]),
+            "modal_prim_eigen": (i, [vp, i, i, d, i, vp, i, vp, i, vp, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -381,6 +384,27 @@ class Context:
         _check(lib().modal_gamma_transfer_pol(self.h, float(deltaphi), _ptr(outs[0]), _ptr(outs[1]), _ptr(outs[2])))
         return tuple(outs)
 
+    def prim_ortho(self, kmin, kmax_i, kmax, basis, prim):
+        """Packed upper triangle [N(N+1)/2] of the primordial k-grid Gram matrix."""
+        basis = _f64(basis)
+        prim = np.ascontiguousarray(prim, dtype=np.int32).reshape(-1, 3)
+        N = prim.shape[0]
+        out = np.empty(N * (N + 1) // 2)
+        _check(lib().modal_prim_ortho(self.h, kmin, kmax_i, float(kmax), basis.shape[1], _ptr(basis), N, _ptr(prim),
+                                      _ptr(out)))
+        return out
+
+    def prim_eigen(self, kmin, kmax_i, kmax, basis, prim, shapes):
+        """(alpha [S][N], <S,S> [S]) of primordial shapes on the k-grid."""
+        basis = _f64(basis)
+        prim = np.ascontiguousarray(prim, dtype=np.int32).reshape(-1, 3)
+        arr, keep = shapes_to_c(shapes)
+        a, n2 = np.empty((len(shapes), prim.shape[0])), np.empty(len(shapes))
+        _check(lib().modal_prim_eigen(self.h, kmin, kmax_i, float(kmax), basis.shape[1], _ptr(basis), prim.shape[0],
+                                      _ptr(prim), len(shapes), ctypes.cast(arr, ctypes.c_void_p), _ptr(a), _ptr(n2)))
+        del keep
+        return a, n2
+
     def calculate_modes(self, b):
         b = _f64(b)
         out = np.empty(self.N)
@@ -459,6 +483,15 @@ class Context:
 
 
 # ----------------------------------------------------------- synthetic inputs
+
+def prim_points(kmin, kmax_i):
+    """[npts][3] points of the primordial k-grid tetrapyd, enumerated on the GPU."""
+    n = ctypes.c_long()
+    _check(lib().modal_prim_points(kmin, kmax_i, ctypes.byref(n), None))
+    pts = np.empty((n.value, 3), dtype=np.int32)
+    _check(lib().modal_prim_points(kmin, kmax_i, ctypes.byref(n), _ptr(pts)))
+    return pts
+
 
 def synthetic_cl(lmax):
     """C_l = 1e3/(l(l+1)) exp(-(l/1500)^2) + 1e-4 (noise, beam 1); l < 2 set to 1."""

@@ -795,3 +795,153 @@ int orc_gamma_transfer_pol(int lmin, int lmax, int P, const double *basisT, int 
     free(ttw); free(eew); free(pl); free(MT); free(ME);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Primordial k-space side: the grid tetrapyd of get_ijk_next_prim           */
+/* (tetrapyd_tools.c:485-517, start check_ijk_min_prim :519-550), the cell   */
+/* weights of calculate_weight (calculate_volume.c:12-133) and the Gram      */
+/* matrix / projection sums of calculate_ortho (orthogonalisation.c:14-86)   */
+/* and calculate_eigen / integrate_template2 (calculate_eigen.c:13-144).     */
+/* ------------------------------------------------------------------------ */
+static double cell1(double a, double b, double c, double d, double e, double f, double g, double h)
+{ (void)0; return (11 * (a + b + c + e) + 17 * (d + g + f) + 25 * h) / 240.0; }
+static double cell2(double a, double b, double c, double d, double e, double f, double g, double h)
+{ return (47 * a + 19 * (b + c + e) + 5 * (d + f + g) + h) / 720.0; }
+static double cell3(double a, double b, double c, double d, double e, double f, double g, double h)
+{ return (40 * (b + c) + 35 * (a + d) + 26 * (f + g) + 19 * (e + h)) / 360.0; }
+static double cell4(double a, double b, double c, double d, double e, double f, double g, double h)
+{ return (89 * a + 85 * (b + c + e) + 71 * (d + f + g) + 43 * h) / 720.0; }
+
+double orc_prim_weight(int min, int max, int i, int j, int k)
+{
+    int grid[3][3][3], sum = 0;
+    for (int l = 0; l < 3; l++)
+        for (int m = 0; m < 3; m++)
+            for (int n = 0; n < 3; n++) {
+                const int i0 = i + l - 1, j0 = j + m - 1, k0 = k + n - 1;
+                if (i0 < min || i0 > max || j0 < min || j0 > max || k0 < min || k0 > max) grid[l][m][n] = -8;
+                else if (i0 > j0 + k0 || j0 > i0 + k0 || k0 > i0 + j0) grid[l][m][n] = 0;
+                else { grid[l][m][n] = 1; sum++; }
+            }
+    double weight = 0.0;
+    if (sum == 27) {
+        weight = 1.0;
+    } else {
+        double pt[3][3][3] = {{{0}}};
+        pt[1][1][1] = 1.0;
+        for (int s1 = 0; s1 < 2; s1++)
+            for (int s2 = 0; s2 < 2; s2++)
+                for (int s3 = 0; s3 < 2; s3++) {
+                    int su = 0;
+                    for (int l = 0; l < 2; l++)
+                        for (int m = 0; m < 2; m++)
+                            for (int n = 0; n < 2; n++) su += grid[l + s1][m + s2][n + s3];
+                    const double a = pt[s1][s2][s3], b = pt[s1 + 1][s2][s3], c = pt[s1][s2 + 1][s3],
+                                 d = pt[s1 + 1][s2 + 1][s3], e = pt[s1][s2][s3 + 1], f = pt[s1 + 1][s2][s3 + 1],
+                                 g = pt[s1][s2 + 1][s3 + 1], h = pt[s1 + 1][s2 + 1][s3 + 1];
+                    if (su == 4) {
+                        if (grid[1 + s1][0 + s2][1 + s3] == 1) weight += cell2(f, e, h, g, b, a, d, c);
+                        if (grid[1 + s1][1 + s2][0 + s3] == 1) weight += cell2(d, c, b, a, h, g, f, e);
+                        if (grid[0 + s1][1 + s2][1 + s3] == 1) weight += cell2(g, h, e, f, c, d, a, b);
+                    } else if (su == 5) {
+                        weight += cell1(a, b, c, d, e, f, g, h);
+                    } else if (su == 6) {
+                        if (grid[0 + s1][0 + s2][1 + s3] == 1) weight += cell3(g, h, e, f, c, d, a, b);
+                        if (grid[1 + s1][0 + s2][0 + s3] == 1) weight += cell3(f, h, b, d, e, g, a, c);
+                        if (grid[0 + s1][1 + s2][0 + s3] == 1) weight += cell3(d, h, c, g, b, f, a, e);
+                    } else if (su == 7) {
+                        if (grid[0 + s1][1 + s2][0 + s3] == 0) weight += cell4(f, e, h, g, b, a, d, c);
+                        if (grid[0 + s1][0 + s2][1 + s3] == 0) weight += cell4(d, c, b, a, h, g, f, e);
+                        if (grid[1 + s1][0 + s2][0 + s3] == 0) weight += cell4(g, h, e, f, c, d, a, b);
+                    } else if (su == 8) {
+                        weight += 1.0 / 8.0;
+                    }
+                }
+    }
+    if (i != k) weight *= (i == j || j == k) ? 3.0 : 6.0;
+    return weight;
+}
+
+/* Walk of get_ijk_next_prim from the start of check_ijk_min_prim: writes up
+ * to cap points (i,j,k) and returns how many decompose_tetrapyd_prim counts
+ * (all the points with i < max, then the end point (max,max,max)). */
+long orc_prim_walk(int min, int max, long cap, int *pts)
+{
+    int i = min, j = min, k = min;
+    if (i + j + 2 < k) k = i + j + 2;
+    long n = 0;
+    for (;;) {
+        if (n < cap) { pts[3 * n] = i; pts[3 * n + 1] = j; pts[3 * n + 2] = k; }
+        n++;
+        if (j == max) { i++; j = i; k = j; }
+        else if (k == max || k >= i + j + 2) { j++; k = j; }
+        else k++;
+        if (i >= max) {
+            if (n < cap) { pts[3 * n] = max; pts[3 * n + 1] = max; pts[3 * n + 2] = max; }
+            return n + 1;
+        }
+    }
+}
+
+static double prim_pijk(const double *basis, int P, const int *tr, int i, int j, int k)
+{
+#define BP(l, p) basis[(long)(l) * P + (p)]
+    const int p1 = tr[0], p2 = tr[1], p3 = tr[2];
+    double b1 = BP(i, p1) * BP(j, p2) * BP(k, p3), b2 = BP(i, p2) * BP(j, p3) * BP(k, p1);
+    double b3 = BP(i, p3) * BP(j, p1) * BP(k, p2), b4 = BP(i, p3) * BP(j, p2) * BP(k, p1);
+    double b5 = BP(i, p2) * BP(j, p1) * BP(k, p3), b6 = BP(i, p1) * BP(j, p3) * BP(k, p2);
+#undef BP
+    return (b1 + b2 + b3 + b4 + b5 + b6) / 6.0;
+}
+
+static double prim_point_weight(int min, int max, double kmax, int i, int j, int k)
+{
+    const double factor = kmax * (1e0 / (double)max), cube = factor * factor * factor;
+    double x = orc_prim_weight(min, max, i, j, k) * cube;
+    double ksum = factor * i + factor * j + factor * k;
+    if (ksum > 1e-10) ksum = 1e0 / ksum;
+    return x * ksum;
+}
+
+int orc_prim_ortho(int min, int max, double kmax, int P, const double *basis, int N, const int *prim, double *out)
+{
+    long npts = orc_prim_walk(min, max, 0, NULL);
+    int *pts = malloc(sizeof(int) * 3 * (size_t)npts);
+    orc_prim_walk(min, max, npts, pts);
+    const long vsize = (long)N * (N + 1) / 2;
+    for (long v = 0; v < vsize; v++) out[v] = 0.0;
+    double *b = malloc(sizeof(double) * (size_t)N);
+    for (long n = 0; n < npts; n++) {
+        const int i = pts[3 * n], j = pts[3 * n + 1], k = pts[3 * n + 2];
+        const double x = prim_point_weight(min, max, kmax, i, j, k);
+        for (int r = 0; r < N; r++) b[r] = prim_pijk(basis, P, prim + 3 * r, i, j, k);
+        long m = 0;
+        for (int r = 0; r < N; r++)
+            for (int s = r; s < N; s++) out[m++] += x * b[r] * b[s];
+    }
+    free(b);
+    free(pts);
+    return 0;
+}
+
+int orc_prim_eigen(int min, int max, double kmax, int P, const double *basis, int N, const int *prim, int kind,
+                   int nterms, const double *tab, double c1, double c2, double c3, double sigma, double *alpha,
+                   double *norm2)
+{
+    orc_shape sh = {kind, nterms, max, tab, c1, c2, c3, sigma};
+    long npts = orc_prim_walk(min, max, 0, NULL);
+    int *pts = malloc(sizeof(int) * 3 * (size_t)npts);
+    orc_prim_walk(min, max, npts, pts);
+    for (int r = 0; r < N; r++) alpha[r] = 0.0;
+    double y = 0.0;
+    for (long n = 0; n < npts; n++) {
+        const int i = pts[3 * n], j = pts[3 * n + 1], k = pts[3 * n + 2];
+        const double x = prim_point_weight(min, max, kmax, i, j, k);
+        const double s = orc_shape_eval(&sh, i, j, k);
+        for (int r = 0; r < N; r++) alpha[r] += (x * s) * prim_pijk(basis, P, prim + 3 * r, i, j, k);
+        y += x * (s * s);
+    }
+    *norm2 = y;
+    free(pts);
+    return 0;
+}

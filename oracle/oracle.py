@@ -25,6 +25,15 @@ REF_SO = os.path.join(HERE, "_ref", "libmodalref.so")
 REFERENCE_DIR = "/root/reference"
 
 
+def _shape_args(shape):
+    """(kind, nterms, tab, centre, sigma) of a shape dict for the C drivers."""
+    if shape["kind"] == 0:
+        tab = np.ascontiguousarray(shape["tab"], dtype=np.float64)
+        return 0, tab.shape[0], tab, (0.0, 0.0, 0.0), 1.0
+    c = shape["c"]
+    return 1, 0, None, (float(c[0]), float(c[1]), float(c[2])), float(shape["sigma"])
+
+
 def build_oracle():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     return ORACLE_SO
@@ -90,6 +99,10 @@ class Oracle:
             ("orc_gamma_pol", i, [i, vp, vp, vp, i, i, i, vp, vp, vp, vp, vp, vp]),
             ("orc_gamma_transfer_pol", i, [i, i, i, vp, i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                            vp, vp, d, d, i, vp, vp, i, vp, i, vp, vp, i, vp, d, vp]),
+            ("orc_prim_weight", d, [i, i, i, i, i]),
+            ("orc_prim_walk", l, [i, i, l, vp]),
+            ("orc_prim_ortho", i, [i, i, d, i, vp, i, vp, vp]),
+            ("orc_prim_eigen", i, [i, i, d, i, vp, i, vp, i, i, vp, d, d, d, d, vp, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -232,6 +245,32 @@ class Oracle:
                                       _p(prim), float(dphi), _p(out))
         return out
 
+    def prim_walk(self, kmin, kmax_i):
+        n = self.L.orc_prim_walk(kmin, kmax_i, 0, None)
+        pts = np.empty((n, 3), dtype=np.int32)
+        self.L.orc_prim_walk(kmin, kmax_i, n, _p(pts))
+        return pts
+
+    def prim_ortho(self, kmin, kmax_i, kmax, basis, prim):
+        """calculate_ortho: packed upper triangle [N(N+1)/2] of the k-grid Gram matrix."""
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        N = prim.shape[0]
+        out = np.empty(N * (N + 1) // 2)
+        self.L.orc_prim_ortho(kmin, kmax_i, float(kmax), basis.shape[1], _p(basis), N, _p(prim), _p(out))
+        return out
+
+    def prim_eigen(self, kmin, kmax_i, kmax, basis, prim, shape):
+        """calculate_eigen + integrate_template2 for one shape: (alpha[N], <S,S>)."""
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        N = prim.shape[0]
+        a, n2 = np.empty(N), np.empty(1)
+        kind, nterms, tab, c, sigma = _shape_args(shape)
+        self.L.orc_prim_eigen(kmin, kmax_i, float(kmax), basis.shape[1], _p(basis), N, _p(prim), kind, nterms,
+                              _p(tab), c[0], c[1], c[2], sigma, _p(a), _p(n2))
+        return a, n2[0]
+
     def ortho_cholesky(self, gamma):
         """Cholesky branch; returns (orthol, lambdal, fail) with fail = -1 or the failing pivot row."""
         g = np.ascontiguousarray(gamma, dtype=np.float64)
@@ -299,6 +338,8 @@ class Ref:
             ("ref_gamma_pol", i, [vp]),
             ("ref_setup_pol_spectra", i, [i, vp, d, d]),
             ("ref_gamma_transfer_pol", i, [i, vp, i, vp, vp, i, vp, d, vp]),
+            ("ref_prim_ortho", i, [i, i, d, i, vp, i, vp, vp]),
+            ("ref_prim_eigen", i, [i, i, d, i, vp, i, vp, i, i, vp, d, d, d, d, vp, vp]),
         ]:
             fn = getattr(L, name)
             fn.restype = res
@@ -344,6 +385,24 @@ class Ref:
         self.L.ref_gamma_transfer_pol(xvec.size, _p(xvec), qtT.shape[1], _p(qtT), _p(qtE), prim.shape[0], _p(prim),
                                       float(dphi), _p(out))
         return out
+
+    def prim_ortho(self, kmin, kmax_i, kmax, basis, prim):
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        N = prim.shape[0]
+        out = np.empty(N * (N + 1) // 2)
+        self.L.ref_prim_ortho(kmin, kmax_i, float(kmax), basis.shape[1], _p(basis), N, _p(prim), _p(out))
+        return out
+
+    def prim_eigen(self, kmin, kmax_i, kmax, basis, prim, shape):
+        basis = np.ascontiguousarray(basis, dtype=np.float64)
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        N = prim.shape[0]
+        a, n2 = np.empty(N), np.empty(1)
+        kind, nterms, tab, c, sigma = _shape_args(shape)
+        self.L.ref_prim_eigen(kmin, kmax_i, float(kmax), basis.shape[1], _p(basis), N, _p(prim), kind, nterms,
+                              _p(tab), c[0], c[1], c[2], sigma, _p(a), _p(n2))
+        return a, n2[0]
 
     def gamma_pol(self):
         """[4][N][N]: TTT, TTE, TEE, EEE from calculate_orthol over every pair."""

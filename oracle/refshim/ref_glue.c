@@ -466,3 +466,98 @@ int ref_gamma_transfer_pol(int xsize, const double *xvec, int Pp, const double *
     free(g_qt); g_qt = NULL; free(g_qtE); g_qtE = NULL; free(g_prim); g_prim = NULL;
     return 0;
 }
+
+/* ===================== primordial k-space side ===================== */
+/* orthogonalisation.c (calculate_ortho), calculate_volume.c (calculate_weight),
+ * calculate_eigen.c (calculate_eigen, integrate_template2) on the k-grid
+ * tetrapyd: basis_prim[max+1][P] values on grid index i (get_basis_prim),
+ * kmax (get_kmax), the primordial triples (find_perm_prim, g_prim). */
+int alpha_points = 0;
+static double *g_bprim;
+static int g_Pprim, g_kgrid_max;
+static double g_kmax = 1.0;
+double get_basis_prim(int i, int j) { return g_bprim[(long)i * g_Pprim + j]; }
+double get_kmax(void) { return g_kmax; }
+double get_lambda(int i, int j) { (void)i; (void)j; return 0.0; }
+int quad(int i, int j, int k, int l) { (void)i; (void)j; (void)k; (void)l; abort(); }
+/* primordial template stand-in: the synthetic shape of ref_prim_eigen on the
+ * grid index k/dk (separable tables are tabulated on grid indices; the bump
+ * uses k/(k1+k2+k3), which the grid spacing cancels) */
+typedef struct { double a1, a2, a3; } ref_shape_params; /* global.h:32-36 */
+double shape3(double k1, double k2, double k3, ref_shape_params params)
+{
+    (void)params;
+    const double dk = g_kmax / g_kgrid_max;
+    return orc_shape_eval(&g_shape, (int)lround(k1 / dk), (int)lround(k2 / dk), (int)lround(k3 / dk));
+}
+/* Monte Carlo integration link stubs (calculate_ortho_mc is not exercised) */
+struct refshim_rng_type;
+struct refshim_rng;
+struct refshim_monte_plain;
+const struct refshim_rng_type *gsl_rng_default = NULL;
+const struct refshim_rng_type *gsl_rng_env_setup(void) { abort(); }
+struct refshim_rng *gsl_rng_alloc(const struct refshim_rng_type *T) { (void)T; abort(); }
+void gsl_rng_free(struct refshim_rng *r) { (void)r; }
+struct refshim_monte_plain *gsl_monte_plain_alloc(size_t dim) { (void)dim; abort(); }
+int gsl_monte_plain_integrate(const void *f, const double xl[], const double xu[], size_t dim, size_t calls,
+                              struct refshim_rng *r, struct refshim_monte_plain *st, double *res, double *err)
+{ (void)f; (void)xl; (void)xu; (void)dim; (void)calls; (void)r; (void)st; (void)res; (void)err; abort(); }
+void gsl_monte_plain_free(struct refshim_monte_plain *s) { (void)s; }
+
+extern void calculate_ortho(int min, int max, ref_tetrapyd_limits *block, double *ortho);
+extern void calculate_eigen(int min, int max, ref_shape_params params, ref_tetrapyd_limits *block, double *alpha);
+extern void integrate_template2(int min, int max, ref_shape_params params, ref_tetrapyd_limits *block, double *res);
+extern void decompose_tetrapyd_prim(ref_tetrapyd_limits *block, int rank, int nranks, int nthreads, int min, int max);
+
+static void prim_install(int max, double kmax, int P, const double *basis, int N, const int *prim)
+{
+    g_kgrid_max = max;
+    g_kmax = kmax;
+    g_Pprim = P;
+    free(g_bprim);
+    g_bprim = malloc(sizeof(double) * (size_t)(max + 1) * P);
+    memcpy(g_bprim, basis, sizeof(double) * (size_t)(max + 1) * P);
+    g_Nprim = N;
+    g_N = N;
+    free(g_prim);
+    g_prim = malloc(sizeof(int) * 3 * (size_t)N);
+    memcpy(g_prim, prim, sizeof(int) * 3 * (size_t)N);
+}
+
+/* calculate_ortho over the whole k-grid tetrapyd on one rank and one thread:
+ * out[N(N+1)/2], the packed upper triangle r <= s. */
+int ref_prim_ortho(int min, int max, double kmax, int P, const double *basis, int N, const int *prim, double *out)
+{
+    prim_install(max, kmax, P, basis, N, prim);
+    ref_tetrapyd_limits block[1];
+    decompose_tetrapyd_prim(block, 0, 1, 1, min, max);
+    for (long i = 0; i < (long)N * (N + 1) / 2; i++) out[i] = 0.0;
+    calculate_ortho(min, max, block, out);
+    return 0;
+}
+
+/* calculate_eigen and integrate_template2 for one synthetic shape (same
+ * kinds as ref_project): alpha[N] and <S,S>. */
+int ref_prim_eigen(int min, int max, double kmax, int P, const double *basis, int N, const int *prim, int kind,
+                   int nterms, const double *tab, double c1, double c2, double c3, double sigma, double *alpha,
+                   double *norm2)
+{
+    prim_install(max, kmax, P, basis, N, prim);
+    g_shape.kind = kind;
+    g_shape.nterms = nterms;
+    g_shape.tab = tab;
+    g_shape.lmax = max;
+    g_shape.c1 = c1; g_shape.c2 = c2; g_shape.c3 = c3;
+    g_shape.sigma = sigma;
+    ref_tetrapyd_limits block[1];
+    decompose_tetrapyd_prim(block, 0, 1, 1, min, max);
+    ref_shape_params params = {0.0, 0.0, 0.0};
+    for (int r = 0; r < N; r++) alpha[r] = 0.0;
+    const int nt = omp_get_max_threads();
+    omp_set_num_threads(1);  /* the block decomposition above is for one thread */
+    calculate_eigen(min, max, params, block, alpha);
+    *norm2 = 0.0;
+    integrate_template2(min, max, params, block, norm2);
+    omp_set_num_threads(nt);
+    return 0;
+}

@@ -183,6 +183,36 @@ def pol_transfer_golden():
     print("gamma_transfer_pol done", G.shape)
 
 
+def prim_inputs(kmax_i=40, Pp=4):
+    """Primordial k-grid case: cosine basis on grid indices 0..kmax_i, all
+    p <= r <= s < Pp triples, two shapes (one separable, one bump)."""
+    x = np.arange(kmax_i + 1) / kmax_i
+    basis = np.stack([np.cos(np.pi * p * x) + 0.1 * p * x for p in range(Pp)], axis=1)
+    prim = M.mode_triples(Pp)
+    shapes = M.separable_shapes(kmax_i, 1, 3, 1, 2) + M.bump_shapes(1, 4)
+    for sh in shapes:  # tables on grid indices 1..kmax_i (index 0 unused with kmin = 1)
+        if sh["kind"] == 0:
+            sh["tab"][:, :, 0] = 0.0
+    return basis, prim, shapes
+
+
+def prim_golden():
+    """11. primordial k-space side: calculate_ortho, calculate_eigen and
+    integrate_template2 on the grid tetrapyd (reference in place)."""
+    ref = O.Ref()
+    out = {}
+    for name, kmin, kmax_i, kmax in [("a", 1, 40, 0.2), ("b", 3, 57, 1.5)]:
+        basis, prim, shapes = prim_inputs(kmax_i)
+        out["ortho_" + name] = ref.prim_ortho(kmin, kmax_i, kmax, basis, prim)
+        for n, sh in enumerate(shapes):
+            a, n2 = ref.prim_eigen(kmin, kmax_i, kmax, basis, prim, sh)
+            out[f"alpha_{name}{n}"] = a
+            out[f"norm2_{name}{n}"] = np.array([n2])
+        out["grid_" + name] = np.array([kmin, kmax_i, kmax])
+    np.savez_compressed(os.path.join(OUT, "prim.npz"), **out)
+    print("prim done")
+
+
 def pol_golden():
     """9. polarised Gamma: calculate_orthol's four results with do_polarisation."""
     lmaxT, lmaxE, lminE = 50, 60, 3
@@ -206,8 +236,11 @@ if __name__ == "__main__":
     elif sys.argv[1:] == ["pol"]:
         pol_golden()
         pol_transfer_golden()
+    elif sys.argv[1:] == ["prim"]:
+        prim_golden()
     else:
         main()
         prune_golden()
         pol_golden()
         pol_transfer_golden()
+        prim_golden()

@@ -62,6 +62,8 @@ def test_argument_errors_without_gpu(built_lib, mg):
     assert L.modal_ctx_captures(None) == 0
     assert L.modal_set_basis_e(None, 2, 10, 3, None) == 1
     assert L.modal_gamma_pol(None, None, None, None) == 1
+    assert L.modal_prim_points(5, 2, None, None) == 1
+    assert L.modal_prim_ortho(None, 1, 10, 1.0, 3, None, 1, None, None) == 1
 
 
 def test_tetrapyd_count_host_logic(built_lib, mg, orc):

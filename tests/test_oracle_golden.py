@@ -262,3 +262,34 @@ def test_polarised_transfer_oracle_vs_reference(orc, golden):
                                  d["qtE"], d["prim"], d["dphi"])
     for f in range(3):
         assert rel_max(out[f], g["gamma"][f + 1]) <= 1e-14
+
+
+def _prim_inputs(kmax_i):
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    from make_golden import prim_inputs
+    return prim_inputs(kmax_i)
+
+
+@pytest.mark.parametrize("name", ["a", "b"])
+def test_prim_oracle_vs_reference(orc, golden, name):
+    # calculate_ortho / calculate_eigen / integrate_template2 (the reference in place)
+    g = golden("prim")
+    kmin, kmax_i, kmax = g["grid_" + name]
+    kmin, kmax_i = int(kmin), int(kmax_i)
+    basis, prim, shapes = _prim_inputs(kmax_i)
+    assert rel_max(orc.prim_ortho(kmin, kmax_i, kmax, basis, prim), g["ortho_" + name]) <= 1e-15
+    for n, sh in enumerate(shapes):
+        a, n2 = orc.prim_eigen(kmin, kmax_i, kmax, basis, prim, sh)
+        assert rel_max(a, g[f"alpha_{name}{n}"]) <= 1e-14
+        assert abs(n2 - g[f"norm2_{name}{n}"][0]) <= 1e-14 * abs(n2)
+
+
+def test_prim_walk_closed_form(orc):
+    # the walk of get_ijk_next_prim covers min <= i < max, i <= j <= max,
+    # j <= k <= min(max, i+j+2), then the end point (max, max, max)
+    for kmin, kmax_i in [(1, 12), (0, 9), (3, 20), (2, 3)]:
+        walk = orc.prim_walk(kmin, kmax_i)
+        pts = [(i, j, k) for i in range(kmin, kmax_i) for j in range(i, kmax_i + 1)
+               for k in range(j, min(kmax_i, i + j + 2) + 1)] + [(kmax_i,) * 3]
+        assert [tuple(p) for p in walk] == pts

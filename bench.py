@@ -120,6 +120,19 @@ class Clocks:
 
 # -------------------------------------------------------------- our GPU arm
 
+def max_over_ranks(vals, ws, device="cpu"):
+    """Element-wise maximum of per-rank timings after a barrier (replicas: the
+    job takes as long as its slowest rank); the identity for one rank."""
+    if ws <= 1:
+        return [float(v) for v in vals]
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
+    td.barrier()
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return t.tolist()
+
+
 def run_ours(a, ws, rank, local):
     import torch
     import modal_gb300 as mg
@@ -195,10 +208,7 @@ def run_ours(a, ws, rank, local):
     go_ms = float(np.median(times[:, 0]))
     proj_ms = float(np.median(times[:, 1]))
     step_ms = float(np.median(times.sum(axis=1)))
-    if ws > 1:  # max over ranks
-        t = torch.tensor([go_ms, proj_ms, step_ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        go_ms, proj_ms, step_ms = t.tolist()
+    go_ms, proj_ms, step_ms = max_over_ranks([go_ms, proj_ms, step_ms], ws, f"cuda:{local}")
 
     # the other precision, for the split-vs-FP64 ratio and the error against FP64
     extra = {}

@@ -162,16 +162,23 @@ def run_ours(a, ws, rank, local):
         split_ok = False
     prec = {"auto": mg.PREC_SPLIT if split_ok else mg.PREC_FP64, "fp64": mg.PREC_FP64, "split": mg.PREC_SPLIT}[a.prec]
 
-    def step(pr):
+    # the comparison pass in the other precision projects at most 16 shapes
+    # (FP64 projection of 512 shapes at l <= 2500 would take minutes); its
+    # projection time is scaled to S shapes
+    S_cmp = min(S, 16)
+    shapes_cmp = shapes[:S_cmp]
+
+    def step(pr, sh=None):
+        sh = shapes if sh is None else sh
         e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
         e[0].record(stream)
         ctx.init_glint()
         ctx.gamma(pr, download=False)
         ctx.orthogonalise(None, download=False)
         e[1].record(stream)
-        ctx.project(shapes, pr, download=False)
+        ctx.project(sh, pr, download=False)
         e[2].record(stream)
-        ctx.alpha(S, download=False)
+        ctx.alpha(len(sh), download=False)
         e[3].record(stream)
         return e
 
@@ -179,9 +186,9 @@ def run_ours(a, ws, rank, local):
         if ws > 1:
             torch.distributed.barrier()
 
-    def run(pr, steps, warm):
+    def run(pr, steps, warm, sh=None):
         for _ in range(warm):
-            step(pr)
+            step(pr, sh)
             flush.zero_()
             torch.cuda.synchronize()
         ctx.timer_reset()
@@ -192,7 +199,7 @@ def run_ours(a, ws, rank, local):
         clk = Clocks(local) if pr == prec else None
         t0 = time.perf_counter()
         for _ in range(steps):
-            ev = step(pr)
+            ev = step(pr, sh)
             torch.cuda.synchronize()
             times.append([ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2]), ev[2].elapsed_time(ev[3])])
             flush.zero_()  # L2 flush between steps (outside the events)
@@ -216,20 +223,23 @@ def run_ours(a, ws, rank, local):
     ctx.gamma(mg.PREC_FP64, download=False)
     G64 = ctx.gamma(mg.PREC_FP64)
     ctx.orthogonalise(None, download=False)
-    b64 = ctx.project(shapes, mg.PREC_FP64)
-    a64, m64 = ctx.alpha(S)
+    b64 = ctx.project(shapes_cmp, mg.PREC_FP64)
+    a64, m64 = ctx.alpha(S_cmp)
     if split_ok:
         other = mg.PREC_FP64 if prec == mg.PREC_SPLIT else mg.PREC_SPLIT
-        t2, _, _, tm2, _ = run(other, max(1, min(a.steps, 2)), 1 if other == mg.PREC_FP64 else 3)
+        t2, _, _, tm2, _ = run(other, max(1, min(a.steps, 2)), 1 if other == mg.PREC_FP64 else 3, shapes_cmp)
+        t2 = t2.copy()
+        t2[:, 1] *= S / S_cmp  # projection time scaled to the S shapes of the timed steps
         Gs = ctx.gamma(mg.PREC_SPLIT)
         ctx.orthogonalise(None, download=False)
-        bs = ctx.project(shapes, mg.PREC_SPLIT)
-        as_, ms_ = ctx.alpha(S)
+        bs = ctx.project(shapes_cmp, mg.PREC_SPLIT)
+        as_, ms_ = ctx.alpha(S_cmp)
         fp = t2 if other == mg.PREC_FP64 else times
         sp = times if other == mg.PREC_FP64 else t2
         d = as_ - a64
         gnorm = lambda v: np.sqrt(np.abs(np.einsum("si,ij,sj->s", v, G64, v)))  # noqa: E731
         extra = {
+            "comparison_shapes": S_cmp,
             "fp64_gamma_ortho_ms": float(np.median(fp[:, 0])), "split_gamma_ortho_ms": float(np.median(sp[:, 0])),
             "fp64_projection_ms": float(np.median(fp[:, 1])), "split_projection_ms": float(np.median(sp[:, 1])),
             "split_vs_fp64_gamma_ortho_projection": float(np.median(fp[:, :2].sum(1)) / np.median(sp[:, :2].sum(1))),
@@ -246,9 +256,9 @@ def run_ours(a, ws, rank, local):
         for floor in (1e-6, 1e-4):
             ctx.set_pca_floor(floor)
             _, _, _, r64 = ctx.orthogonalise(G64, download=False)
-            af64, _ = ctx.alpha(S, b64)
+            af64, _ = ctx.alpha(S_cmp, b64)
             _, _, _, rs = ctx.orthogonalise(Gs, download=False)
-            afs, _ = ctx.alpha(S, bs)
+            afs, _ = ctx.alpha(S_cmp, bs)
             fl["%g" % floor] = {"kept_fp64": r64, "kept_split": rs,
                                 "alpha_fro": float(np.linalg.norm(afs - af64) / np.linalg.norm(af64)),
                                 "alpha_gamma_norm": float(np.max(gnorm(afs - af64) / gnorm(af64)))}
@@ -384,22 +394,28 @@ def run_extras(mg, local):
 
 
 def run_e2e(ctx, mg, q, tr, cl, shapes, prec, steps):
-    """Gamma + ortho through the public C ABI from host inputs to host outputs."""
+    """Gamma + ortho through the public C ABI from host inputs to host outputs
+    (inputs and outputs in pinned host memory)."""
+    import torch
     ts = []
     N = len(tr)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    qp, trp = pin(q), pin(tr.astype(np.int32))
+    G, o, lam = (torch.empty((N, N), dtype=torch.float64).pin_memory().numpy() for _ in range(3))
     for _ in range(max(1, steps)):
         t0 = time.perf_counter()
-        ctx.set_basis(2, q.shape[0] + 1, q)
-        ctx.set_modes(tr)
+        ctx.set_basis(2, q.shape[0] + 1, qp)
+        ctx.set_modes(trp)
         ctx.init_glint()
-        G = ctx.gamma(prec)
-        o, lam, _, _ = ctx.orthogonalise(None)
+        ctx.gamma(prec, out=G)
+        ctx.orthogonalise(None, out=(o, lam))
         ts.append(time.perf_counter() - t0)
     ctx.set_spectrum(cl)
     h2d = q.nbytes + tr.astype(np.int32).nbytes
     d2h = G.nbytes + o.nbytes + lam.nbytes
     return {"value": float(np.median(ts)), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "what": "set_basis/set_modes (H2D) + init_glint + gamma (D2H Gamma) + orthogonalise (D2H orthol, lambdal)",
+            "what": "set_basis/set_modes (H2D) + init_glint + gamma (D2H Gamma) + orthogonalise (D2H orthol, lambdal); "
+                    "pinned host buffers",
             "N": N}
 
 

@@ -247,6 +247,36 @@ __device__ __forceinline__ float shape_f(const FShape &s, const float *__restric
     return expf(-a * s.inv2s2);
 }
 
+// A separable shape on a fixed row (i, j): sym sum_t f_t g_t h_t at (i, j, k) is
+//   sum_t (al_t h_t(k) + be_t g_t(k) + ga_t f_t(k)) / 6,
+//   al_t = f_t(i) g_t(j) + f_t(j) g_t(i), be_t = f_t(i) h_t(j) + f_t(j) h_t(i),
+//   ga_t = g_t(i) h_t(j) + g_t(j) h_t(i),
+// so the per-point work is three table reads and three FMAs per term.
+constexpr int PJ_TCOEF = 8;  // terms per shape with precomputed row coefficients
+
+__device__ __forceinline__ float3 sep_row_coef(const FShape &s, const float *__restrict__ tab, int stride, int t, int i,
+                                               int j)
+{
+    const float *f = tab + s.tab_off + (long)t * 3 * stride, *g = f + stride, *h = g + stride;
+    const float fi = f[i], fj = f[j], gi = g[i], gj = g[j], hi = h[i], hj = h[j];
+    return make_float3(fi * gj + fj * gi, fi * hj + fj * hi, gi * hj + gj * hi);
+}
+
+__device__ __forceinline__ float shape_row_f(const FShape &s, const float3 *__restrict__ coef,
+                                             const float *__restrict__ tab, int stride, int i, int j, int k)
+{
+    if (s.kind == MODAL_SHAPE_SEPARABLE && s.nterms <= PJ_TCOEF) {
+        float acc = 0.f;
+        for (int t = 0; t < s.nterms; t++) {
+            const float *f = tab + s.tab_off + (long)t * 3 * stride, *g = f + stride, *h = g + stride;
+            const float3 c = coef[t];
+            acc += fmaf(c.x, h[k], fmaf(c.y, g[k], c.z * f[k])) * (1.f / 6.f);
+        }
+        return acc;
+    }
+    return shape_f(s, tab, stride, i, j, k);
+}
+
 // Work item w = (slab rank w / G, shape group w % G), slabs heaviest first.
 // counter == NULL: one item per CTA of a (L x G) grid.  counter != NULL: a
 // persistent grid whose CTAs take items from *counter until nitems are done.
@@ -261,8 +291,10 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
     constexpr int JC = 16, CW = 32 * CPL;
     static_assert(SG % 4 == 0, "shape groups are read as float4");
     __shared__ float4 fsm[8][2][32][SG / 4];  // shape values per (warp, row, k, shape)
-    __shared__ float Hs[JC][SG][CW];
+    __shared__ __align__(16) float Hs[JC][SG][CW];
+    __shared__ __align__(16) float Qs[JC][CW];  // q_b(j) of the chunk's rows, zero beyond P and lmax
     __shared__ FShape sh[SG];
+    __shared__ float3 coef[8][2][SG][PJ_TCOEF];  // row coefficients of separable shapes per (warp, row)
     __shared__ int item;
     extern __shared__ float Fsm[];  // [SG*P*P] hi, then [SG*P*P] lo
     for (int pass = 0;; pass++) {
@@ -307,6 +339,16 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
             const int kend = max(kendA, kendB);
             const int nk = (kend >= kstart) ? (kend - kstart) / 2 + 1 : 0;
             const float vA = vi * vlf[jA], vB = hasB ? vi * vlf[jB] : 0.f;
+            for (int e = lane; e < 2 * SG * PJ_TCOEF; e += 32) {
+                const int row = e / (SG * PJ_TCOEF), rem = e - row * (SG * PJ_TCOEF);
+                const int sx = rem / PJ_TCOEF, t = rem - sx * PJ_TCOEF;
+                const int j = row ? jB : jA;
+                float3 cv = make_float3(0.f, 0.f, 0.f);
+                if (sx < sgv && sh[sx].kind == MODAL_SHAPE_SEPARABLE && t < sh[sx].nterms && j <= lmax)
+                    cv = sep_row_coef(sh[sx], tabf, stride, t, i, j);
+                coef[warp][row][sx][t] = cv;
+            }
+            __syncwarp();
             for (int kb = 0; kb < nk; kb += 32) {
                 const int kk = kb + lane, k = kstart + 2 * kk;
                 float fa[SG], fb2[SG];
@@ -318,13 +360,13 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                         float g = permsix_f(i, jA, k) * geo_f(i, jA, k) * vA * vk;
 #pragma unroll
                         for (int s = 0; s < SG; s++)
-                            if (s < sgv) fa[s] = g * shape_f(sh[s], tabf, stride, i, jA, k);
+                            if (s < sgv) fa[s] = g * shape_row_f(sh[s], coef[warp][0][s], tabf, stride, i, jA, k);
                     }
                     if (hasB && k >= jB + par && k <= kendB) {
                         float g = permsix_f(i, jB, k) * geo_f(i, jB, k) * vB * vk;
 #pragma unroll
                         for (int s = 0; s < SG; s++)
-                            if (s < sgv) fb2[s] = g * shape_f(sh[s], tabf, stride, i, jB, k);
+                            if (s < sgv) fb2[s] = g * shape_row_f(sh[s], coef[warp][1][s], tabf, stride, i, jB, k);
                     }
                 }
 #pragma unroll
@@ -339,6 +381,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                 for (int s = 0; s < SG; s++)
 #pragma unroll
                     for (int cc = 0; cc < CPL; cc++) hA[s][cc] = hB[s][cc] = 0.f;
+#pragma unroll 4
                 for (int t = 0; t < nt; t++) {
                     const int kt = kstart + 2 * (kb + t);
                     const float *qrow = qf + (size_t)(kt - lmin) * P;
@@ -375,16 +418,43 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                 Hs[jo][s][lane + 32 * cc] = HAh[s][cc] + HAl[s][cc];
                 Hs[jo + 2][s][lane + 32 * cc] = HBh[s][cc] + HBl[s][cc];
             }
+        for (int e = threadIdx.x; e < JC * CW; e += 256) {
+            const int r = e / CW, b = e - r * CW, j = j0 + r;
+            Qs[r][b] = (j <= lmax && b < P) ? qf[(size_t)(j - lmin) * P + b] : 0.f;
+        }
         __syncthreads();
-        for (int e = threadIdx.x; e < sgv * PP; e += 256) {
-            const int s = e / PP, rem = e - s * PP, b = rem / P, c = rem - b * P;
-            float acc = 0.f;
+        // F_s[b][c] += sum_r q_b(j0+r) H_s[r][c] as 4 x 4 register tiles (two
+        // vector loads per 16 FMAs), then one compensated add per element
+        {
+            const int nb4 = (P + 3) >> 2, ntile = sgv * nb4 * nb4;
+            for (int ti = threadIdx.x; ti < ntile; ti += 256) {
+                const int sx = ti / (nb4 * nb4), rem = ti - sx * nb4 * nb4, bt = rem / nb4, ct = rem - bt * nb4;
+                float acc[4][4];
+#pragma unroll
+                for (int x = 0; x < 4; x++)
+#pragma unroll
+                    for (int y = 0; y < 4; y++) acc[x][y] = 0.f;
 #pragma unroll 4
-            for (int r = 0; r < JC; r++) {
-                const int j = j0 + r;
-                if (j <= lmax) acc = fmaf(qf[(size_t)(j - lmin) * P + b], Hs[r][s][c], acc);
+                for (int r = 0; r < JC; r++) {
+                    const float4 qv = *reinterpret_cast<const float4 *>(&Qs[r][bt * 4]);
+                    const float4 hv = *reinterpret_cast<const float4 *>(&Hs[r][sx][ct * 4]);
+                    const float qa[4] = {qv.x, qv.y, qv.z, qv.w}, ha[4] = {hv.x, hv.y, hv.z, hv.w};
+#pragma unroll
+                    for (int x = 0; x < 4; x++)
+#pragma unroll
+                        for (int y = 0; y < 4; y++) acc[x][y] = fmaf(qa[x], ha[y], acc[x][y]);
+                }
+#pragma unroll
+                for (int x = 0; x < 4; x++)
+#pragma unroll
+                    for (int y = 0; y < 4; y++) {
+                        const int b = bt * 4 + x, c = ct * 4 + y;
+                        if (b < P && c < P) {
+                            const int e = sx * PP + b * P + c;
+                            kahan_add(Fhi[e], Flo[e], acc[x][y]);
+                        }
+                    }
             }
-            kahan_add(Fhi[e], Flo[e], acc);
         }
         __syncthreads();
     }

@@ -291,8 +291,12 @@ class Context:
         _check(lib().modal_get_mij(self.h, _ptr(out)))
         return out
 
-    def gamma(self, prec=PREC_FP64, download=True):
-        out = np.empty((self.N, self.N)) if (download and self.N) else None
+    def gamma(self, prec=PREC_FP64, download=True, out=None):
+        """Gamma [N][N]; `out` may be a caller array (e.g. a view of pinned memory)."""
+        if out is None:
+            out = np.empty((self.N, self.N)) if (download and self.N) else None
+        else:
+            assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.N * self.N
         _check(lib().modal_gamma(self.h, prec, _ptr(out)))
         return out
 
@@ -315,10 +319,14 @@ class Context:
         _check(lib().modal_gamma_pol(self.h, _ptr(outs[0]), _ptr(outs[1]), _ptr(outs[2])))
         return tuple(outs)
 
-    def orthogonalise(self, gamma=None, pca_flag=1, download=True):
+    def orthogonalise(self, gamma=None, pca_flag=1, download=True, out=None):
+        """(orthol, lambdal, branch, rank); `out` = (orthol, lambdal) caller arrays."""
         g = None if gamma is None else _f64(gamma)
-        o = np.empty((self.N, self.N)) if download else None
-        lam = np.empty((self.N, self.N)) if download else None
+        if out is not None:
+            o, lam = out
+        else:
+            o = np.empty((self.N, self.N)) if download else None
+            lam = np.empty((self.N, self.N)) if download else None
         br, rk = ctypes.c_int(), ctypes.c_int()
         _check(lib().modal_orthogonalise(self.h, _ptr(g), pca_flag, _ptr(o), _ptr(lam), ctypes.byref(br),
                                          ctypes.byref(rk)))

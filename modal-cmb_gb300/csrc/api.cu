@@ -167,6 +167,7 @@ void modal_ctx_destroy(modal_ctx *c)
                       &c->adj, &c->adj2, &c->adj3, &c->prune, &c->qe, &c->me, &c->tri_pol, &c->gamma_pol,
                       &c->tr_qte, &c->tr_we, &c->tr_mte, &c->prim};
     batch_release(c);
+    solver_release(c);
     for (DevBuf *b : bufs) release(*b);
     timers_clear(c);
     for (cudaEvent_t e : c->event_pool) cudaEventDestroy(e);

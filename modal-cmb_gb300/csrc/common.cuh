@@ -97,6 +97,7 @@ struct modal_ctx {
     // primordial k-space side (prim.cu): grid offsets, basis, chunk buffers
     modal::DevBuf prim;
     double *h_info = nullptr;  // pinned readback
+    void *solver = nullptr;    // cusolverDn handle on `stream`, made on first use (eig.cu)
 
     // profiling: event pairs per stage, summed on read
     bool profile = false;
@@ -109,6 +110,8 @@ namespace modal {
 
 modal_status ensure(DevBuf &b, size_t bytes);
 void release(DevBuf &b);
+modal_status solver_handle(modal_ctx *ctx, void **h);  // eig.cu
+void solver_release(modal_ctx *ctx);
 
 #define MODAL_CUDA(call)                                                                  \
     do {                                                                                  \

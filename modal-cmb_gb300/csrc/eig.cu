@@ -49,30 +49,53 @@ __global__ void k_pca_outputs(int N, const double *__restrict__ V_rm, const doub
     orthol[e] = inv;
 }
 
+// One cuSOLVER handle per context, bound to the context's stream.  Creating a
+// handle sets up the library's state on the device; keeping it saves that cost
+// on every orthogonalisation and pruning call.
+modal_status solver_handle(modal_ctx *ctx, void **out)
+{
+    if (!ctx->solver) {
+        cusolverDnHandle_t h = nullptr;
+        if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return MODAL_ERR_CUDA; }
+        if (cusolverDnSetStream(h, ctx->stream) != CUSOLVER_STATUS_SUCCESS) {
+            cusolverDnDestroy(h);
+            set_error("cusolverDnSetStream failed");
+            return MODAL_ERR_CUDA;
+        }
+        ctx->solver = h;
+    }
+    *out = ctx->solver;
+    return MODAL_OK;
+}
+
+void solver_release(modal_ctx *ctx)
+{
+    if (ctx->solver) cusolverDnDestroy(static_cast<cusolverDnHandle_t>(ctx->solver));
+    ctx->solver = nullptr;
+}
+
 modal_status eig_pca_dev(modal_ctx *ctx)
 {
     const int N = ctx->N;
-    cusolverDnHandle_t h = nullptr;
-    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return MODAL_ERR_CUDA; }
-    cusolverDnSetStream(h, ctx->stream);
+    void *hv = nullptr;
+    MODAL_TRY(solver_handle(ctx, &hv));
+    cusolverDnHandle_t h = static_cast<cusolverDnHandle_t>(hv);
     modal_status st = MODAL_OK;
     int lwork = 0;
     double *A = ctx->chol.as<double>();  // symmetric: row-major == column-major
-    if (ensure(ctx->scratch2, sizeof(double) * (size_t)N) != MODAL_OK) { cusolverDnDestroy(h); return MODAL_ERR_NOMEM; }
+    if (ensure(ctx->scratch2, sizeof(double) * (size_t)N) != MODAL_OK) return MODAL_ERR_NOMEM;
     double *W = ctx->scratch2.as<double>();
     if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N, W, &lwork) !=
         CUSOLVER_STATUS_SUCCESS) {
         set_error("syevd_bufferSize failed");
-        cusolverDnDestroy(h);
         return MODAL_ERR_CUDA;
     }
     st = ensure(ctx->scratch, sizeof(double) * (size_t)lwork + 64);
-    if (st != MODAL_OK) { cusolverDnDestroy(h); return st; }
+    if (st != MODAL_OK) return st;
     int *devinfo = ctx->info.as<int>() + 1;
     int *rank = ctx->info.as<int>() + 2;
     cusolverStatus_t cs = cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N, W,
                                            ctx->scratch.as<double>(), lwork, devinfo);
-    cusolverDnDestroy(h);
     if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return MODAL_ERR_CUDA; }
     int hinfo = 0;
     MODAL_CUDA(cudaMemcpyAsync(&hinfo, devinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

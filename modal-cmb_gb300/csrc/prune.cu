@@ -112,11 +112,16 @@ __global__ void k_lmin_upstream(int N, const double *__restrict__ gamma, const d
 
 struct Solver {
     cusolverDnHandle_t h = nullptr;
-    ~Solver()
-    {
-        if (h) cusolverDnDestroy(h);
-    }
 };
+
+// the context's cached handle (made on first use, bound to its stream)
+modal_status get_solver(modal_ctx *c, Solver &sv)
+{
+    void *hv = nullptr;
+    MODAL_TRY(solver_handle(c, &hv));
+    sv.h = static_cast<cusolverDnHandle_t>(hv);
+    return MODAL_OK;
+}
 
 }  // namespace
 
@@ -154,8 +159,7 @@ modal_status modal_basis_prune(modal_ctx *c, int N, const double *gamma, int nfa
     StageTimer t(c, MODAL_T_PRUNE);
     const size_t NN = (size_t)N * N, nn0 = (size_t)n0 * n0;
     Solver sv;
-    if (cusolverDnCreate(&sv.h) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return MODAL_ERR_CUDA; }
-    cusolverDnSetStream(sv.h, c->stream);
+    MODAL_TRY(get_solver(c, sv));
     int lwork = 0;
     if (n0 > 2 && cusolverDnDsyevd_bufferSize(sv.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n0, nullptr, n0,
                                               nullptr, &lwork) != CUSOLVER_STATUS_SUCCESS) {
@@ -221,8 +225,7 @@ modal_status modal_lambda_min(modal_ctx *c, double *lambda_min, double *eigvec, 
     const size_t NN = (size_t)N * N;
     StageTimer t(c, MODAL_T_ADJOINT);
     Solver sv;
-    if (cusolverDnCreate(&sv.h) != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnCreate failed"); return MODAL_ERR_CUDA; }
-    cusolverDnSetStream(sv.h, c->stream);
+    MODAL_TRY(get_solver(c, sv));
     int lwork = 0;
     if (cusolverDnDsyevd_bufferSize(sv.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, nullptr, N, nullptr,
                                     &lwork) != CUSOLVER_STATUS_SUCCESS) {

@@ -174,8 +174,9 @@ modal_status gamma_vjp_accum_dev(modal_ctx *ctx, const double *G, double *dq);
 // Device descriptor of one shape (projection kernels).
 struct DShape {
     int kind, nterms;
-    long tab_off;
+    long tab_off;  // FP64 tables: [term][f, g, h][l] from this double offset
     double c1, c2, c3, sigma;
+    long tab_off_f = 0;  // FP32 form: [parity of l][l / 2][term][f, g, h, 0] from this float offset
 };
 
 // A planned projection: validated descriptors, buffer offsets, launch shape.
@@ -185,7 +186,10 @@ struct ProjPlan {
     long tab_total = 0;
     std::vector<DShape> desc;
     int SG = 8, CPL = 1, cpb = 0, nsm = 0, fpt = 0;
-    size_t smem = 0, o_q = 0, o_v = 0, o_t = 0, o_s = 0, o_F = 0, o_B = 0, o_c = 0;
+    size_t smem = 0, o_q = 0, o_v = 0, o_t = 0, o_s = 0, o_F = 0, o_B = 0, o_c = 0, o_w = 0, o_sb = 0;
+    long long npts = 0;  // tetrapyd points (FP32 weight table entries)
+    long tabf_total = 0;  // floats of the FP32 separable tables
+    int max_nterms = 0;
 };
 // plan: validate, size every buffer, upload the slab schedule (may allocate);
 // stage: copy shape tables/descriptors to the device; record: enqueue the

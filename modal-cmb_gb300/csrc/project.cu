@@ -218,14 +218,96 @@ __device__ __forceinline__ float permsix_f(int i, int j, int k)
     return (i == k && i == j) ? 1.f : ((i == j || j == k || i == k) ? 3.f : 6.f);
 }
 
-__device__ __forceinline__ float shape_f(const FShape &s, const float *__restrict__ tab, int stride, int i, int j, int k)
+// ---------------------------------------------------------------------------
+// The FP32 weight table.  The per-point weight of the projection,
+//   W(i,j,k) = permsix(i,j,k) h~^2 geometric factor v_i v_j v_k,
+// depends on neither the shape nor the basis.  The FP32 form computes it once
+// per projection into an HBM table in walk order (slab i, row j >= i, then
+// k = j + (i & 1) + 2m, m = 0..), so that every shape group streams it instead
+// of recomputing the geometric factor (three divisions and a square root) per
+// point.  Row offsets within a slab have a closed form; slab bases are a
+// prefix sum over slabs.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline long long tet_tri_sum(long long u)
+{
+    // sum_{v=0}^{u} (floor(v/2) + 1): (a+1)^2 for u = 2a, (a+1)(a+2) for u = 2a+1
+    if (u < 0) return 0;
+    const long long a = u / 2;
+    return (u & 1) ? (a + 1) * (a + 2) : (a + 1) * (a + 1);
+}
+
+// Points of rows i..j-1 of slab i (rows hold k = j + (i & 1) + 2m <= min(i + j, lmax)).
+__host__ __device__ inline long long tet_row_offset(int i, int j, int lmax)
+{
+    const int ip = i & 1;
+    const long long n1 = (i - ip) / 2 + 1;  // points of a row with i + j <= lmax
+    const int J1 = lmax - i;                // last such row
+    long long off = 0;
+    const int e1 = (j - 1 < J1) ? j - 1 : J1;
+    if (e1 >= i) off += (long long)(e1 - i + 1) * n1;
+    const int s2 = (i > J1 + 1) ? i : J1 + 1;  // rows ending at k = lmax
+    if (j - 1 >= s2) off += tet_tri_sum((long long)lmax - ip - s2) - tet_tri_sum((long long)lmax - ip - (j - 1) - 1);
+    return off;
+}
+
+// base[s] = points of slabs lmin..lmin+s-1 (s = 0..L); one block.
+__global__ void k_slab_base(int lmin, int lmax, long long *__restrict__ base)
+{
+    __shared__ long long part[256];
+    const int L = lmax - lmin + 1, per = (L + 255) / 256, t = threadIdx.x;
+    const int a = min(L, t * per), b = min(L, a + per);
+    long long sum = 0;
+    for (int s = a; s < b; s++) sum += tet_row_offset(lmin + s, lmax + 1, lmax);
+    part[t] = sum;
+    __syncthreads();
+    for (int d = 1; d < 256; d <<= 1) {  // inclusive scan
+        const long long v = (t >= d) ? part[t - d] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    long long run = part[t] - sum;  // exclusive
+    for (int s = a; s < b; s++) {
+        base[s] = run;
+        run += tet_row_offset(lmin + s, lmax + 1, lmax);
+    }
+    if (t == 255) base[L] = part[255];
+}
+
+// grid (L slabs, ceil(L / 8)); warp w of block y fills row j = i + 8 y + w.
+__global__ void __launch_bounds__(256) k_weight_table(int lmin, int lmax, const float *__restrict__ vlf,
+                                                      const long long *__restrict__ base, float *__restrict__ Wt)
+{
+    const int i = lmin + blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = i + blockIdx.y * 8 + warp;
+    if (j > lmax) return;
+    const int ip = i & 1, kend = min(i + j, lmax), k0 = j + ip;
+    if (kend < k0) return;
+    const int n = (kend - k0) / 2 + 1;
+    float *row = Wt + base[blockIdx.x] + tet_row_offset(i, j, lmax);
+    const float vij = vlf[i] * vlf[j];
+    for (int m = lane; m < n; m += 32) {
+        const int k = k0 + 2 * m;
+        row[m] = permsix_f(i, j, k) * geo_f(i, j, k) * vij * vlf[k];
+    }
+}
+
+// FP32 separable tables, per shape: [parity of l][l / 2][term][f_t, g_t, h_t, 0]
+// with H = (lmax + 2) / 2 entries per parity.  The k walk of a row keeps one
+// parity, so a warp's lanes read consecutive 16-byte entries: one load per term
+// gives f, g and h at k.
+__device__ __forceinline__ float4 tab4(const FShape &s, const float *__restrict__ tab, int H, int t, int l)
+{
+    return __ldg(reinterpret_cast<const float4 *>(tab + s.tab_off) + ((long)((l & 1) * H + (l >> 1)) * s.nterms + t));
+}
+
+__device__ __forceinline__ float shape_f(const FShape &s, const float *__restrict__ tab, int H, int i, int j, int k)
 {
     if (s.kind == MODAL_SHAPE_SEPARABLE) {
         float acc = 0.f;
         for (int t = 0; t < s.nterms; t++) {
-            const float *f = tab + s.tab_off + (long)t * 3 * stride;
-            const float *g = f + stride, *h = g + stride;
-            float fi = f[i], fj = f[j], fk = f[k], gi = g[i], gj = g[j], gk = g[k], hi = h[i], hj = h[j], hk = h[k];
+            const float4 Ti = tab4(s, tab, H, t, i), Tj = tab4(s, tab, H, t, j), Tk = tab4(s, tab, H, t, k);
+            float fi = Ti.x, fj = Tj.x, fk = Tk.x, gi = Ti.y, gj = Tj.y, gk = Tk.y, hi = Ti.z, hj = Tj.z, hk = Tk.z;
             acc += (fi * (gj * hk + gk * hj) + fj * (gi * hk + gk * hi) + fk * (gi * hj + gj * hi)) * (1.f / 6.f);
         }
         return acc;
@@ -254,27 +336,27 @@ __device__ __forceinline__ float shape_f(const FShape &s, const float *__restric
 // so the per-point work is three table reads and three FMAs per term.
 constexpr int PJ_TCOEF = 8;  // terms per shape with precomputed row coefficients
 
-__device__ __forceinline__ float3 sep_row_coef(const FShape &s, const float *__restrict__ tab, int stride, int t, int i,
-                                               int j)
+__device__ __forceinline__ float3 sep_row_coef(const FShape &s, const float *__restrict__ tab, int H, int t, int i, int j)
 {
-    const float *f = tab + s.tab_off + (long)t * 3 * stride, *g = f + stride, *h = g + stride;
-    const float fi = f[i], fj = f[j], gi = g[i], gj = g[j], hi = h[i], hj = h[j];
+    const float4 Ti = tab4(s, tab, H, t, i), Tj = tab4(s, tab, H, t, j);
+    const float fi = Ti.x, fj = Tj.x, gi = Ti.y, gj = Tj.y, hi = Ti.z, hj = Tj.z;
     return make_float3(fi * gj + fj * gi, fi * hj + fj * hi, gi * hj + gj * hi);
 }
 
-__device__ __forceinline__ float shape_row_f(const FShape &s, const float3 *__restrict__ coef,
-                                             const float *__restrict__ tab, int stride, int i, int j, int k)
+// FP32 tables of the separable shapes, re-laid from the FP64 [term][f, g, h][l]
+// tables; grid (ceil((lmax + 1) max_nterms / 256), S).
+__global__ void k_tab_f32(int lmax, const DShape *__restrict__ shapes, const double *__restrict__ tab64,
+                          float *__restrict__ tabf)
 {
-    if (s.kind == MODAL_SHAPE_SEPARABLE && s.nterms <= PJ_TCOEF) {
-        float acc = 0.f;
-        for (int t = 0; t < s.nterms; t++) {
-            const float *f = tab + s.tab_off + (long)t * 3 * stride, *g = f + stride, *h = g + stride;
-            const float3 c = coef[t];
-            acc += fmaf(c.x, h[k], fmaf(c.y, g[k], c.z * f[k])) * (1.f / 6.f);
-        }
-        return acc;
-    }
-    return shape_f(s, tab, stride, i, j, k);
+    const DShape d = shapes[blockIdx.y];
+    if (d.kind != MODAL_SHAPE_SEPARABLE) return;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int l = e / d.nterms, t = e - l * d.nterms;
+    if (l > lmax) return;
+    const int stride = lmax + 1, H = (lmax + 2) / 2;
+    const double *f = tab64 + d.tab_off + (long)t * 3 * stride;
+    float4 v = make_float4((float)f[l], (float)f[stride + l], (float)f[2 * stride + l], 0.f);
+    reinterpret_cast<float4 *>(tabf + d.tab_off_f)[(long)((l & 1) * H + (l >> 1)) * d.nterms + t] = v;
 }
 
 // Work item w = (slab rank w / G, shape group w % G), slabs heaviest first.
@@ -286,7 +368,10 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                                                            const int *__restrict__ slab_order,
                                                            const float *__restrict__ qf, const float *__restrict__ vlf,
                                                            const FShape *__restrict__ shapes,
-                                                           const float *__restrict__ tabf, float *__restrict__ Fbuf)
+                                                           const float *__restrict__ tabf,
+                                                           const float *__restrict__ Wt,
+                                                           const long long *__restrict__ sbase,
+                                                           float *__restrict__ Fbuf)
 {
     constexpr int JC = 16, CW = 32 * CPL;
     static_assert(SG % 4 == 0, "shape groups are read as float4");
@@ -314,7 +399,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
     const int s0 = (w % G) * SG;
     const int sgv = min(SG, S - s0);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int par = i & 1, PP = P * P, L = lmax - lmin + 1, stride = lmax + 1;
+    const int par = i & 1, PP = P * P, L = lmax - lmin + 1, H = (lmax + 2) / 2;
     if (threadIdx.x < SG) {
         FShape z = {1, 0, 0, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 0.f};
         sh[threadIdx.x] = (threadIdx.x < sgv) ? shapes[s0 + threadIdx.x] : z;
@@ -322,7 +407,6 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
     float *Fhi = Fsm, *Flo = Fsm + SG * PP;
     for (int e = threadIdx.x; e < 2 * SG * PP; e += 256) Fsm[e] = 0.f;
     __syncthreads();
-    const float vi = vlf[i];
     const int jo = (warp >> 1) * 4 + (warp & 1);  // rows jo and jo+2 of each chunk
 
     for (int j0 = i; j0 <= lmax; j0 += JC) {
@@ -338,14 +422,16 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
             const int kendA = min(i + jA, lmax), kendB = hasB ? min(i + jB, lmax) : -1;
             const int kend = max(kendA, kendB);
             const int nk = (kend >= kstart) ? (kend - kstart) / 2 + 1 : 0;
-            const float vA = vi * vlf[jA], vB = hasB ? vi * vlf[jB] : 0.f;
+            // this warp's two rows in the weight table (row B starts one lattice point later)
+            const float *wA = Wt + sbase[slab] + tet_row_offset(i, jA, lmax);
+            const float *wB = hasB ? Wt + sbase[slab] + tet_row_offset(i, jB, lmax) - 1 : wA;
             for (int e = lane; e < 2 * SG * PJ_TCOEF; e += 32) {
                 const int row = e / (SG * PJ_TCOEF), rem = e - row * (SG * PJ_TCOEF);
                 const int sx = rem / PJ_TCOEF, t = rem - sx * PJ_TCOEF;
                 const int j = row ? jB : jA;
                 float3 cv = make_float3(0.f, 0.f, 0.f);
                 if (sx < sgv && sh[sx].kind == MODAL_SHAPE_SEPARABLE && t < sh[sx].nterms && j <= lmax)
-                    cv = sep_row_coef(sh[sx], tabf, stride, t, i, j);
+                    cv = sep_row_coef(sh[sx], tabf, H, t, i, j);
                 coef[warp][row][sx][t] = cv;
             }
             __syncwarp();
@@ -355,18 +441,27 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
 #pragma unroll
                 for (int s = 0; s < SG; s++) fa[s] = fb2[s] = 0.f;
                 if (kk < nk) {
-                    const float vk = vlf[k];
-                    if (k <= kendA) {
-                        float g = permsix_f(i, jA, k) * geo_f(i, jA, k) * vA * vk;
+                    // both rows share k: one table load per term serves the two
+                    const bool inA = k <= kendA, inB = hasB && k >= jB + par && k <= kendB;
+                    const float gA = inA ? wA[kk] : 0.f, gB = inB ? wB[kk] : 0.f;
 #pragma unroll
-                        for (int s = 0; s < SG; s++)
-                            if (s < sgv) fa[s] = g * shape_row_f(sh[s], coef[warp][0][s], tabf, stride, i, jA, k);
-                    }
-                    if (hasB && k >= jB + par && k <= kendB) {
-                        float g = permsix_f(i, jB, k) * geo_f(i, jB, k) * vB * vk;
-#pragma unroll
-                        for (int s = 0; s < SG; s++)
-                            if (s < sgv) fb2[s] = g * shape_row_f(sh[s], coef[warp][1][s], tabf, stride, i, jB, k);
+                    for (int s = 0; s < SG; s++) {
+                        if (s >= sgv) continue;
+                        const FShape &sp = sh[s];
+                        if (sp.kind == MODAL_SHAPE_SEPARABLE && sp.nterms <= PJ_TCOEF) {
+                            float accA = 0.f, accB = 0.f;
+                            for (int t = 0; t < sp.nterms; t++) {
+                                const float4 T = tab4(sp, tabf, H, t, k);
+                                const float3 cA = coef[warp][0][s][t], cB = coef[warp][1][s][t];
+                                accA += fmaf(cA.x, T.z, fmaf(cA.y, T.y, cA.z * T.x)) * (1.f / 6.f);
+                                accB += fmaf(cB.x, T.z, fmaf(cB.y, T.y, cB.z * T.x)) * (1.f / 6.f);
+                            }
+                            if (inA) fa[s] = gA * accA;
+                            if (inB) fb2[s] = gB * accB;
+                        } else {
+                            if (inA) fa[s] = gA * shape_f(sp, tabf, H, i, jA, k);
+                            if (inB) fb2[s] = gB * shape_f(sp, tabf, H, i, jB, k);
+                        }
                     }
                 }
 #pragma unroll
@@ -495,7 +590,7 @@ __global__ void k_fshapes(int S, const DShape *__restrict__ in, FShape *__restri
     FShape f;
     f.kind = d.kind;
     f.nterms = d.nterms;
-    f.tab_off = d.tab_off;
+    f.tab_off = d.tab_off_f;
     const double c[3] = {d.c1, d.c2, d.c3};
     for (int m = 0; m < 3; m++) {
         f.ch[m] = (float)c[m];
@@ -562,6 +657,17 @@ modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_p
         }
     }
     pl.tab_total = tab_total;
+    {   // FP32 layout: 2 parities x H entries x nterms x 4 floats per separable shape
+        const long H = (lmax + 2) / 2;
+        long off = 0;
+        for (int s = 0; s < S; s++)
+            if (pl.desc[s].kind == MODAL_SHAPE_SEPARABLE) {
+                pl.desc[s].tab_off_f = off;
+                off += 2 * H * pl.desc[s].nterms * 4;
+                pl.max_nterms = std::max(pl.max_nterms, pl.desc[s].nterms);
+            }
+        pl.tabf_total = off;
+    }
     MODAL_TRY(ensure(ctx->shape_tab, sizeof(double) * (size_t)(tab_total > 0 ? tab_total : 1)));
     MODAL_TRY(ensure(ctx->shape_desc, sizeof(DShape) * (size_t)S));
     // slab schedule: heaviest slabs first
@@ -579,11 +685,16 @@ modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_p
         size_t o = 0;
         pl.o_q = o; o += al(sizeof(float) * (size_t)L * P);
         pl.o_v = o; o += al(sizeof(float) * (lmax + 1));
-        pl.o_t = o; o += al(sizeof(float) * (size_t)(tab_total > 0 ? tab_total : 1));
+        pl.o_t = o; o += al(sizeof(float) * (size_t)(pl.tabf_total > 0 ? pl.tabf_total : 4));
         pl.o_s = o; o += al(sizeof(FShape) * (size_t)S);
         pl.o_F = o; o += al(sizeof(float) * (size_t)S * L * PP);
         pl.o_B = o; o += al(sizeof(double) * (size_t)S * P * PP);
         pl.o_c = o; o += al(sizeof(int));
+        long long npts = 0;
+        for (int i = lmin; i <= lmax; i++) npts += tet_row_offset(i, lmax + 1, lmax);
+        pl.npts = npts;
+        pl.o_sb = o; o += al(sizeof(long long) * (size_t)(L + 1));
+        pl.o_w = o; o += al(sizeof(float) * (size_t)npts);
         MODAL_TRY(ensure(ctx->scratch, o));
         pl.smem = sizeof(float) * 2 * (size_t)pl.SG * PP;
         int dev = ctx->device, nsm = 0;
@@ -642,12 +753,19 @@ modal_status proj_record(modal_ctx *ctx, const ProjPlan &pl)
         MODAL_TRY(launched(ctx, "d2f_q"));
         k_d2f<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax + 1, ctx->vl.as<double>(), vlf);
         MODAL_TRY(launched(ctx, "d2f_vl"));
-        if (pl.tab_total > 0) {
-            k_d2f<<<ceil_div(pl.tab_total, 256), 256, 0, ctx->stream>>>(pl.tab_total, ctx->shape_tab.as<double>(), tabf);
-            MODAL_TRY(launched(ctx, "d2f_tab"));
+        if (pl.tabf_total > 0) {
+            k_tab_f32<<<dim3(ceil_div((lmax + 1) * pl.max_nterms, 256), S), 256, 0, ctx->stream>>>(
+                lmax, ctx->shape_desc.as<DShape>(), ctx->shape_tab.as<double>(), tabf);
+            MODAL_TRY(launched(ctx, "tab_f32"));
         }
         k_fshapes<<<ceil_div(S, 64), 64, 0, ctx->stream>>>(S, ctx->shape_desc.as<DShape>(), fs);
         MODAL_TRY(launched(ctx, "fshapes"));
+        long long *sbase = reinterpret_cast<long long *>(b + pl.o_sb);
+        float *Wt = reinterpret_cast<float *>(b + pl.o_w);
+        k_slab_base<<<1, 256, 0, ctx->stream>>>(lmin, lmax, sbase);
+        MODAL_TRY(launched(ctx, "slab_base"));
+        k_weight_table<<<dim3(L, ceil_div(L, 8)), 256, 0, ctx->stream>>>(lmin, lmax, vlf, sbase, Wt);
+        MODAL_TRY(launched(ctx, "weight_table"));
         const int G = ceil_div(S, pl.SG), nitems = L * G;
         dim3 grid(L, G);
         int *cnt = nullptr;
@@ -658,7 +776,7 @@ modal_status proj_record(modal_ctx *ctx, const ProjPlan &pl)
         }
         auto run = [&](auto kern) -> modal_status {
             kern<<<grid, 256, pl.smem, ctx->stream>>>(lmin, lmax, P, S, G, nitems, cnt, ctx->slab_order.as<int>(), qf,
-                                                     vlf, fs, tabf, Fbuf);
+                                                     vlf, fs, tabf, Wt, sbase, Fbuf);
             return launched(ctx, "project_slab_f32");
         };
         if (pl.SG == 8) MODAL_TRY(run(k_project_slab_f32<8, 1>));

@@ -3,7 +3,8 @@
 //
 // The symmetric eigen-decomposition of the normalised Gamma (the reference's
 // gsl_eigen_symmv + gsl_eigen_symmv_sort descending, :775-776) is the
-// cuSOLVER library routine cusolverDnDsyevd in FP64 on the GPU.  The outputs
+// cuSOLVER library routine cusolverDnDsyevdx in FP64 on the GPU, asked only for
+// the eigenpairs the outputs use (eigenvalues above the cut).  The outputs
 // follow the reference exactly, with eigenvalues e_i in descending order and
 // r = the number of leading positive eigenvalues:
 //   lambda[i][j]    = V[j][i] / (norm_j sqrt(e_i))   for i < r, else 0
@@ -14,19 +15,20 @@
 
 namespace modal {
 
-// Count leading eigenvalues above floor * e_max in descending order (W is
-// ascending); floor = 0 is the reference's rule (leading positive ones).
-__global__ void k_pca_rank(int N, const double *__restrict__ W, double floor, int *rank)
+// Count leading eigenvalues above floor * e_max in descending order (W holds the
+// meig returned eigenvalues ascending); floor = 0 is the reference's rule
+// (leading positive ones).
+__global__ void k_pca_rank(int meig, const double *__restrict__ W, double floor, int *rank)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const double cut = floor > 0.0 ? floor * W[N - 1] : 0.0;
+    const double cut = (floor > 0.0 && meig > 0) ? floor * W[meig - 1] : 0.0;
     int r = 0;
-    for (int i = 0; i < N && W[N - 1 - i] > cut; i++) r = i + 1;
+    for (int i = 0; i < meig && W[meig - 1 - i] > cut; i++) r = i + 1;
     *rank = r;
 }
 
-// V_rm: row-major buffer whose row a holds the eigenvector of ascending index a.
-__global__ void k_pca_outputs(int N, const double *__restrict__ V_rm, const double *__restrict__ W,
+// V_rm: row-major buffer whose row a < meig holds the eigenvector of ascending index a.
+__global__ void k_pca_outputs(int N, int meig, const double *__restrict__ V_rm, const double *__restrict__ W,
                               const double *__restrict__ norm, const int *__restrict__ rank,
                               double *__restrict__ orthol, double *__restrict__ lambdal)
 {
@@ -37,12 +39,12 @@ __global__ void k_pca_outputs(int N, const double *__restrict__ V_rm, const doub
     // lambda[i][j] = V[j][desc i] / (norm_j sqrt(e_desc i))
     double lam = 0.0;
     if (i < r) {
-        int a = N - 1 - i;
+        int a = meig - 1 - i;
         lam = V_rm[(size_t)a * N + j] / (norm[j] * sqrt(W[a]));
     }
     double inv = 0.0;
     if (j < r) {
-        int a = N - 1 - j;
+        int a = meig - 1 - j;
         inv = norm[i] * V_rm[(size_t)a * N + i] * sqrt(W[a]);
     }
     lambdal[e] = lam;
@@ -85,26 +87,34 @@ modal_status eig_pca_dev(modal_ctx *ctx)
     double *A = ctx->chol.as<double>();  // symmetric: row-major == column-major
     if (ensure(ctx->scratch2, sizeof(double) * (size_t)N) != MODAL_OK) return MODAL_ERR_NOMEM;
     double *W = ctx->scratch2.as<double>();
-    if (cusolverDnDsyevd_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N, W, &lwork) !=
-        CUSOLVER_STATUS_SUCCESS) {
-        set_error("syevd_bufferSize failed");
+    // Only eigenpairs above the cut are used, so the subset solver computes those
+    // alone: eigenvalues in (vl, inf).  The normalised Gamma has a unit diagonal,
+    // so e_max >= 1 and vl = floor (just below) never exceeds floor * e_max; the
+    // exact cut is applied to the returned eigenvalues.  vl = 0 gives every
+    // positive eigenvalue, the reference's rule.
+    const double vl = ctx->pca_floor > 0.0 ? ctx->pca_floor * (1.0 - 1e-12) : 0.0, vu = 1e300;
+    int meig = 0;
+    if (cusolverDnDsyevdx_bufferSize(h, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_V, CUBLAS_FILL_MODE_LOWER, N, A, N,
+                                     vl, vu, 0, 0, &meig, W, &lwork) != CUSOLVER_STATUS_SUCCESS) {
+        set_error("syevdx_bufferSize failed");
         return MODAL_ERR_CUDA;
     }
     st = ensure(ctx->scratch, sizeof(double) * (size_t)lwork + 64);
     if (st != MODAL_OK) return st;
     int *devinfo = ctx->info.as<int>() + 1;
     int *rank = ctx->info.as<int>() + 2;
-    cusolverStatus_t cs = cusolverDnDsyevd(h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N, W,
-                                           ctx->scratch.as<double>(), lwork, devinfo);
-    if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return MODAL_ERR_CUDA; }
+    cusolverStatus_t cs = cusolverDnDsyevdx(h, CUSOLVER_EIG_MODE_VECTOR, CUSOLVER_EIG_RANGE_V, CUBLAS_FILL_MODE_LOWER, N,
+                                            A, N, vl, vu, 0, 0, &meig, W, ctx->scratch.as<double>(), lwork, devinfo);
+    if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevdx failed (%d)", (int)cs); return MODAL_ERR_CUDA; }
     int hinfo = 0;
     MODAL_CUDA(cudaMemcpyAsync(&hinfo, devinfo, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (hinfo != 0) { set_error("syevd info=%d", hinfo); return MODAL_ERR_NOCONV; }
-    k_pca_rank<<<1, 1, 0, ctx->stream>>>(N, W, ctx->pca_floor, rank);
+    if (hinfo != 0) { set_error("syevdx info=%d", hinfo); return MODAL_ERR_NOCONV; }
+    if (meig < 0 || meig > N) { set_error("syevdx returned %d eigenpairs for N=%d", meig, N); return MODAL_ERR_CUDA; }
+    k_pca_rank<<<1, 1, 0, ctx->stream>>>(meig, W, ctx->pca_floor, rank);
     MODAL_TRY(launched(ctx, "pca_rank"));
     size_t NN = (size_t)N * N;
-    k_pca_outputs<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, A, W, ctx->norm.as<double>(), rank,
+    k_pca_outputs<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, meig, A, W, ctx->norm.as<double>(), rank,
                                                                        ctx->orthol.as<double>(), ctx->lambdal.as<double>());
     MODAL_TRY(launched(ctx, "pca_outputs"));
     int hr = 0;

@@ -85,6 +85,7 @@ struct modal_ctx {
     // adjoint: shape legs and forward products, per-mu adjoints, upstreams
     modal::DevBuf adj, adj2, adj3;
     modal::DevBuf prune;  // basis pruning: normalised Gamma, minors, eigenvalues, work
+    modal::DevBuf gemm_part;  // split-K partial sums of the skinny FP64 products (alpha solve)
 
     // polarisation: E basis, E-mode M table, TTE/TEE/EEE triples, their Gammas
     bool have_basis_e = false, have_pol = false, have_gamma_pol = false;

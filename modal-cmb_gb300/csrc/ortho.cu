@@ -17,6 +17,7 @@
 // Alpha solve (eigenmodetoday_mpi.c:148-162, 286-316):
 //   alpha = lambdal^T (lambdal beta),  modesR = lambdainv^T alpha with
 //   lambdainv the lower triangle of orthol (or the PCA lambdainv).
+#include <algorithm>
 #include <climits>
 #include "common.cuh"
 
@@ -105,6 +106,130 @@ modal_status dgemm(modal_ctx *ctx, int M, int N, int K, double alpha, const doub
     else if (transA && !transB) k_dgemm<true, false><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
     else k_dgemm<true, true><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
     return launched(ctx, "dgemm");
+}
+
+// --------------------------------------------------------------------------
+// Skinny FP64 products C[S][N] = A[S][K] op(B) for S <= 16 rows (the alpha
+// solve's S shapes against N x N matrices).  The large operand is read once,
+// coalesced; K is split over KS CTAs per column block for enough parallelism
+// and the partial sums are added in a fixed order (deterministic).
+// --------------------------------------------------------------------------
+constexpr int SK_S = 16, SK_KCH = 128, SK_KS = 8;
+
+// B row-major [K][ldb]: grid (ceil(N / 64), KS); 256 threads = 64 columns x 4 k-lanes.
+__global__ void __launch_bounds__(256) k_skinny_nn(int S, int N, int K, const double *__restrict__ A, int lda,
+                                                   const double *__restrict__ B, int ldb, double *__restrict__ part)
+{
+    __shared__ double As[SK_KCH][SK_S];
+    __shared__ double red[3][SK_S][64];
+    const int col = threadIdx.x & 63, kl = threadIdx.x >> 6, n = blockIdx.x * 64 + col;
+    const int k0 = (int)((long)K * blockIdx.y / gridDim.y), k1 = (int)((long)K * (blockIdx.y + 1) / gridDim.y);
+    double acc[SK_S];
+#pragma unroll
+    for (int s = 0; s < SK_S; s++) acc[s] = 0.0;
+    for (int kc = k0; kc < k1; kc += SK_KCH) {
+        const int len = min(SK_KCH, k1 - kc);
+        for (int e = threadIdx.x; e < SK_KCH * SK_S; e += 256) {
+            const int kk = e / SK_S, s = e - kk * SK_S;
+            As[kk][s] = (kk < len && s < S) ? A[(size_t)s * lda + kc + kk] : 0.0;
+        }
+        __syncthreads();
+        if (n < N)
+            for (int kk = kl; kk < len; kk += 4) {
+                const double b = B[(size_t)(kc + kk) * ldb + n];
+#pragma unroll
+                for (int s = 0; s < SK_S; s++) acc[s] = fma(As[kk][s], b, acc[s]);
+            }
+        __syncthreads();
+    }
+    if (kl > 0)
+#pragma unroll
+        for (int s = 0; s < SK_S; s++) red[kl - 1][s][col] = acc[s];
+    __syncthreads();
+    if (kl == 0 && n < N)
+#pragma unroll
+        for (int s = 0; s < SK_S; s++)
+            if (s < S) part[((size_t)blockIdx.y * S + s) * N + n] = ((acc[s] + red[0][s][col]) + red[1][s][col]) + red[2][s][col];
+}
+
+// B row-major [N][ldb] used transposed: grid (ceil(N / 16), KS); warp w takes rows
+// n = 16 x + 2 w and 2 w + 1, lanes run over k.
+__global__ void __launch_bounds__(256) k_skinny_nt(int S, int N, int K, const double *__restrict__ A, int lda,
+                                                   const double *__restrict__ B, int ldb, double *__restrict__ part)
+{
+    __shared__ double As[SK_S][SK_KCH];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n0 = blockIdx.x * 16 + 2 * warp;
+    const int k0 = (int)((long)K * blockIdx.y / gridDim.y), k1 = (int)((long)K * (blockIdx.y + 1) / gridDim.y);
+    double acc[2][SK_S];
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int s = 0; s < SK_S; s++) acc[r][s] = 0.0;
+    for (int kc = k0; kc < k1; kc += SK_KCH) {
+        const int len = min(SK_KCH, k1 - kc);
+        for (int e = threadIdx.x; e < SK_KCH * SK_S; e += 256) {
+            const int s = e / SK_KCH, kk = e - s * SK_KCH;
+            As[s][kk] = (kk < len && s < S) ? A[(size_t)s * lda + kc + kk] : 0.0;
+        }
+        __syncthreads();
+        for (int kk = lane; kk < len; kk += 32) {
+            double b[2];
+#pragma unroll
+            for (int r = 0; r < 2; r++) b[r] = (n0 + r < N) ? B[(size_t)(n0 + r) * ldb + kc + kk] : 0.0;
+#pragma unroll
+            for (int s = 0; s < SK_S; s++) {
+                const double a = As[s][kk];
+                acc[0][s] = fma(a, b[0], acc[0][s]);
+                acc[1][s] = fma(a, b[1], acc[1][s]);
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int s = 0; s < SK_S; s++) {
+            double v = acc[r][s];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            acc[r][s] = v;
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int r = 0; r < 2; r++)
+#pragma unroll
+            for (int s = 0; s < SK_S; s++)
+                if (n0 + r < N && s < S) part[((size_t)blockIdx.y * S + s) * N + n0 + r] = acc[r][s];
+}
+
+__global__ void k_skinny_sum(int S, int N, int KS, const double *__restrict__ part, double *__restrict__ C, int ldc)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)S * N) return;
+    const int s = (int)(e / N), n = (int)(e - (size_t)s * N);
+    double v = 0.0;
+    for (int p = 0; p < KS; p++) v += part[(size_t)p * S * N + e];
+    C[(size_t)s * ldc + n] = v;
+}
+
+// C = A op(B) (alpha 1, beta 0) with A [S][K]; S > 32 goes to the tiled kernel.
+modal_status dgemm_rows(modal_ctx *ctx, int S, int N, int K, const double *A, int lda, const double *B, int ldb,
+                        bool transB, double *C, int ldc)
+{
+    if (S > 2 * SK_S) return dgemm(ctx, S, N, K, 1.0, A, lda, false, B, ldb, transB, 0.0, C, ldc, 0);
+    if (S <= 0 || N <= 0) return MODAL_OK;
+    MODAL_TRY(ensure(ctx->gemm_part, sizeof(double) * (size_t)SK_KS * SK_S * N));
+    double *part = ctx->gemm_part.as<double>();
+    for (int s0 = 0; s0 < S; s0 += SK_S) {
+        const int Sc = std::min(SK_S, S - s0);
+        if (transB) k_skinny_nt<<<dim3(ceil_div(N, 16), SK_KS), 256, 0, ctx->stream>>>(Sc, N, K, A + (size_t)s0 * lda, lda, B, ldb, part);
+        else k_skinny_nn<<<dim3(ceil_div(N, 64), SK_KS), 256, 0, ctx->stream>>>(Sc, N, K, A + (size_t)s0 * lda, lda, B, ldb, part);
+        MODAL_TRY(launched(ctx, "skinny_gemm"));
+        k_skinny_sum<<<ceil_div((long)Sc * N, 256), 256, 0, ctx->stream>>>(Sc, N, SK_KS, part, C + (size_t)s0 * ldc, ldc);
+        MODAL_TRY(launched(ctx, "skinny_sum"));
+    }
+    return MODAL_OK;
 }
 
 // --------------------------------------------------------------------------
@@ -369,10 +494,10 @@ modal_status alpha_dev(modal_ctx *ctx, int S)
     MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)S * N));
     double *y = ctx->scratch2.as<double>();
     const double *lam = ctx->lambdal.as<double>();
-    MODAL_TRY(dgemm(ctx, S, N, N, 1.0, ctx->beta.as<double>(), N, false, lam, N, true, 0.0, y, N, 0));
-    MODAL_TRY(dgemm(ctx, S, N, N, 1.0, y, N, false, lam, N, false, 0.0, ctx->alpha.as<double>(), N, 0));
-    MODAL_TRY(dgemm(ctx, S, N, N, 1.0, ctx->alpha.as<double>(), N, false, ctx->orthol.as<double>(), N, false, 0.0,
-                    ctx->modesr.as<double>(), N, 0));
+    MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->beta.as<double>(), N, lam, N, true, y, N));
+    MODAL_TRY(dgemm_rows(ctx, S, N, N, y, N, lam, N, false, ctx->alpha.as<double>(), N));
+    MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->alpha.as<double>(), N, ctx->orthol.as<double>(), N, false,
+                         ctx->modesr.as<double>(), N));
     return MODAL_OK;
 }
 

@@ -381,7 +381,10 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
     __shared__ FShape sh[SG];
     __shared__ float3 coef[8][2][SG][PJ_TCOEF];  // row coefficients of separable shapes per (warp, row)
     __shared__ int item;
-    extern __shared__ float Fsm[];  // [SG*P*P] hi, then [SG*P*P] lo
+    // F_i as Kahan pairs, element-major over the fold's 4 x 4 tiles: entry (4x + y) of
+    // tile t at [(4x + y) NT + t], so the threads of a warp (consecutive tiles) touch
+    // consecutive words.  NT = SG nb4^2 tiles, nb4 = ceil(P / 4); hi, then lo.
+    extern __shared__ float Fsm[];
     for (int pass = 0;; pass++) {
     int w;
     if (counter) {
@@ -404,8 +407,9 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
         FShape z = {1, 0, 0, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 0.f};
         sh[threadIdx.x] = (threadIdx.x < sgv) ? shapes[s0 + threadIdx.x] : z;
     }
-    float *Fhi = Fsm, *Flo = Fsm + SG * PP;
-    for (int e = threadIdx.x; e < 2 * SG * PP; e += 256) Fsm[e] = 0.f;
+    const int nb4 = (P + 3) >> 2, NT = SG * nb4 * nb4;
+    float *Fhi = Fsm, *Flo = Fsm + 16 * NT;
+    for (int e = threadIdx.x; e < 32 * NT; e += 256) Fsm[e] = 0.f;
     __syncthreads();
     const int jo = (warp >> 1) * 4 + (warp & 1);  // rows jo and jo+2 of each chunk
 
@@ -521,7 +525,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
         // F_s[b][c] += sum_r q_b(j0+r) H_s[r][c] as 4 x 4 register tiles (two
         // vector loads per 16 FMAs), then one compensated add per element
         {
-            const int nb4 = (P + 3) >> 2, ntile = sgv * nb4 * nb4;
+            const int ntile = sgv * nb4 * nb4;
             for (int ti = threadIdx.x; ti < ntile; ti += 256) {
                 const int sx = ti / (nb4 * nb4), rem = ti - sx * nb4 * nb4, bt = rem / nb4, ct = rem - bt * nb4;
                 float acc[4][4];
@@ -545,7 +549,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                     for (int y = 0; y < 4; y++) {
                         const int b = bt * 4 + x, c = ct * 4 + y;
                         if (b < P && c < P) {
-                            const int e = sx * PP + b * P + c;
+                            const int e = (4 * x + y) * NT + ti;
                             kahan_add(Fhi[e], Flo[e], acc[x][y]);
                         }
                     }
@@ -554,8 +558,9 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
         __syncthreads();
     }
     for (int e = threadIdx.x; e < sgv * PP; e += 256) {
-        const int s = e / PP, rem = e - s * PP;
-        Fbuf[((size_t)(s0 + s) * L + slab) * PP + rem] = Fhi[e] + Flo[e];
+        const int s = e / PP, rem = e - s * PP, b = rem / P, c = rem - b * P;
+        const int f = (4 * (b & 3) + (c & 3)) * NT + (s * nb4 + (b >> 2)) * nb4 + (c >> 2);
+        Fbuf[((size_t)(s0 + s) * L + slab) * PP + rem] = Fhi[f] + Flo[f];
     }
     }
 }
@@ -696,7 +701,8 @@ modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_p
         pl.o_sb = o; o += al(sizeof(long long) * (size_t)(L + 1));
         pl.o_w = o; o += al(sizeof(float) * (size_t)npts);
         MODAL_TRY(ensure(ctx->scratch, o));
-        pl.smem = sizeof(float) * 2 * (size_t)pl.SG * PP;
+        const size_t nb4 = (size_t)(P + 3) / 4;
+        pl.smem = sizeof(float) * 32 * (size_t)pl.SG * nb4 * nb4;  // F Kahan pairs, element-major over 4 x 4 tiles
         int dev = ctx->device, nsm = 0;
         MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         pl.nsm = nsm;

@@ -276,6 +276,30 @@ def test_alpha_vs_oracle(mg, orc, golden):
         assert np.sqrt(abs(d @ G @ d)) <= 1e-8 * np.sqrt(a_ref @ G @ a_ref)
 
 
+@pytest.mark.parametrize("S", [1, 16, 17, 32, 40])
+def test_alpha_products_any_shape_count(mg, S):
+    """alpha = (beta lambda^T) lambda and modesR = alpha orthol for S shapes: one
+    or two 16-row passes of the skinny products (S <= 32) or the tiled product
+    (S > 32), against numpy on the downloaded orthogonalisation outputs."""
+    rng = np.random.default_rng(40 + S)
+    N = 200
+    A = rng.standard_normal((N, N))
+    G = A @ A.T + N * np.eye(N)
+    beta = rng.standard_normal((S, N))
+    with mg.Context(0) as c:
+        q, _, _ = mg.workload(60, 12)
+        c.set_basis(2, 60, q)
+        c.set_modes(mg.mode_triples(12)[:N])
+        o, lam, branch, rank = c.orthogonalise(G, pca_flag=1)
+        a, mR = c.alpha(S, beta)
+        a2, mR2 = c.alpha(S, beta)
+    assert branch == 0 and rank == N
+    a_ref = (beta @ lam.T) @ lam
+    assert rel_fro(a, a_ref) <= 1e-12
+    assert rel_fro(mR, a_ref @ o) <= 1e-12
+    assert np.array_equal(a, a2) and np.array_equal(mR, mR2)  # fixed reduction order
+
+
 def test_full_pipeline_on_device(mg, golden):
     """Gamma -> orthogonalise -> project -> alpha with everything left on the device."""
     g = golden("gamma_small")

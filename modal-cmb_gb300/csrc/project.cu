@@ -73,12 +73,80 @@ __global__ void k_vl(int lmax, const double *__restrict__ cl, double *__restrict
 
 constexpr int JC = 8;
 
+__host__ __device__ inline long long tet_tri_sum(long long u)
+{
+    // sum_{v=0}^{u} (floor(v/2) + 1): (a+1)^2 for u = 2a, (a+1)(a+2) for u = 2a+1
+    if (u < 0) return 0;
+    const long long a = u / 2;
+    return (u & 1) ? (a + 1) * (a + 2) : (a + 1) * (a + 1);
+}
+
+// Points of rows i..j-1 of slab i (rows hold k = j + (i & 1) + 2m <= min(i + j, lmax)).
+__host__ __device__ inline long long tet_row_offset(int i, int j, int lmax)
+{
+    const int ip = i & 1;
+    const long long n1 = (i - ip) / 2 + 1;  // points of a row with i + j <= lmax
+    const int J1 = lmax - i;                // last such row
+    long long off = 0;
+    const int e1 = (j - 1 < J1) ? j - 1 : J1;
+    if (e1 >= i) off += (long long)(e1 - i + 1) * n1;
+    const int s2 = (i > J1 + 1) ? i : J1 + 1;  // rows ending at k = lmax
+    if (j - 1 >= s2) off += tet_tri_sum((long long)lmax - ip - s2) - tet_tri_sum((long long)lmax - ip - (j - 1) - 1);
+    return off;
+}
+
+// base[s] = points of slabs lmin..lmin+s-1 (s = 0..L); one block.
+__global__ void k_slab_base(int lmin, int lmax, long long *__restrict__ base)
+{
+    __shared__ long long part[256];
+    const int L = lmax - lmin + 1, per = (L + 255) / 256, t = threadIdx.x;
+    const int a = min(L, t * per), b = min(L, a + per);
+    long long sum = 0;
+    for (int s = a; s < b; s++) sum += tet_row_offset(lmin + s, lmax + 1, lmax);
+    part[t] = sum;
+    __syncthreads();
+    for (int d = 1; d < 256; d <<= 1) {  // inclusive scan
+        const long long v = (t >= d) ? part[t - d] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    long long run = part[t] - sum;  // exclusive
+    for (int s = a; s < b; s++) {
+        base[s] = run;
+        run += tet_row_offset(lmin + s, lmax + 1, lmax);
+    }
+    if (t == 255) base[L] = part[255];
+}
+
+// FP64 form of the weight table: the same products in the same order as the
+// FP64 point weight, so the projection is unchanged to the last bit.
+__global__ void __launch_bounds__(256) k_weight_table_fp64(int lmin, int lmax, const double *__restrict__ vl,
+                                                           const long long *__restrict__ base, double *__restrict__ Wd)
+{
+    const int i = lmin + blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = i + blockIdx.y * 8 + warp;
+    if (j > lmax) return;
+    const int ip = i & 1, kend = min(i + j, lmax), k0 = j + ip;
+    if (kend < k0) return;
+    const int n = (kend - k0) / 2 + 1;
+    double *row = Wd + base[blockIdx.x] + tet_row_offset(i, j, lmax);
+    const double vi = vl[i], vj = vl[j];
+    for (int m = lane; m < n; m += 32) {
+        const int k = k0 + 2 * m;
+        row[m] = d_permsix(i, j, k) * d_geo(i, j, k) * vi * vj * vl[k];
+    }
+}
+
 template <int FPT>
 __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, int P, int S, int KMAX,
                                                             const int *__restrict__ slab_order,
                                                             const double *__restrict__ q, const double *__restrict__ vl,
                                                             const DShape *__restrict__ shapes,
-                                                            const double *__restrict__ tab, double *__restrict__ Fbuf)
+                                                            const double *__restrict__ tab,
+                                                            const double *__restrict__ Wd,
+                                                            const long long *__restrict__ sbase,
+                                                            double *__restrict__ Fbuf)
 {
     extern __shared__ double sm[];
     double *f = sm;               // [JC][KMAX]
@@ -87,7 +155,6 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
     const int i = lmin + slab;
     const int tid = threadIdx.x;
     const int PP = P * P, L = lmax - lmin + 1, stride = lmax + 1;
-    const double vi = vl[i];
     const int par = i & 1;
     for (int s = 0; s < S; s++) {
         const DShape sh = shapes[s];
@@ -101,7 +168,7 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
                 if (j <= lmax) {
                     int k = j + par + 2 * kk, k1 = min(i + j, lmax);
                     if (k <= k1)
-                        val = d_permsix(i, j, k) * d_geo(i, j, k) * vi * vl[j] * vl[k] * d_shape(sh, tab, stride, i, j, k);
+                        val = Wd[sbase[slab] + tet_row_offset(i, j, lmax) + kk] * d_shape(sh, tab, stride, i, j, k);
                 }
                 f[e] = val;
             }
@@ -228,52 +295,6 @@ __device__ __forceinline__ float permsix_f(int i, int j, int k)
 // point.  Row offsets within a slab have a closed form; slab bases are a
 // prefix sum over slabs.
 // ---------------------------------------------------------------------------
-__host__ __device__ inline long long tet_tri_sum(long long u)
-{
-    // sum_{v=0}^{u} (floor(v/2) + 1): (a+1)^2 for u = 2a, (a+1)(a+2) for u = 2a+1
-    if (u < 0) return 0;
-    const long long a = u / 2;
-    return (u & 1) ? (a + 1) * (a + 2) : (a + 1) * (a + 1);
-}
-
-// Points of rows i..j-1 of slab i (rows hold k = j + (i & 1) + 2m <= min(i + j, lmax)).
-__host__ __device__ inline long long tet_row_offset(int i, int j, int lmax)
-{
-    const int ip = i & 1;
-    const long long n1 = (i - ip) / 2 + 1;  // points of a row with i + j <= lmax
-    const int J1 = lmax - i;                // last such row
-    long long off = 0;
-    const int e1 = (j - 1 < J1) ? j - 1 : J1;
-    if (e1 >= i) off += (long long)(e1 - i + 1) * n1;
-    const int s2 = (i > J1 + 1) ? i : J1 + 1;  // rows ending at k = lmax
-    if (j - 1 >= s2) off += tet_tri_sum((long long)lmax - ip - s2) - tet_tri_sum((long long)lmax - ip - (j - 1) - 1);
-    return off;
-}
-
-// base[s] = points of slabs lmin..lmin+s-1 (s = 0..L); one block.
-__global__ void k_slab_base(int lmin, int lmax, long long *__restrict__ base)
-{
-    __shared__ long long part[256];
-    const int L = lmax - lmin + 1, per = (L + 255) / 256, t = threadIdx.x;
-    const int a = min(L, t * per), b = min(L, a + per);
-    long long sum = 0;
-    for (int s = a; s < b; s++) sum += tet_row_offset(lmin + s, lmax + 1, lmax);
-    part[t] = sum;
-    __syncthreads();
-    for (int d = 1; d < 256; d <<= 1) {  // inclusive scan
-        const long long v = (t >= d) ? part[t - d] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    long long run = part[t] - sum;  // exclusive
-    for (int s = a; s < b; s++) {
-        base[s] = run;
-        run += tet_row_offset(lmin + s, lmax + 1, lmax);
-    }
-    if (t == 255) base[L] = part[255];
-}
-
 // grid (L slabs, ceil(L / 8)); warp w of block y fills row j = i + 8 y + w.
 __global__ void __launch_bounds__(256) k_weight_table(int lmin, int lmax, const float *__restrict__ vlf,
                                                       const long long *__restrict__ base, float *__restrict__ Wt)
@@ -715,7 +736,14 @@ modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_p
         if (pl.smem > 220 * 1024) { set_error("project: lmax=%d too large for the slab tile", lmax); return MODAL_ERR_ARG; }
         pl.fpt = ceil_div(PP, 256);
         if (pl.fpt > 16) { set_error("project: P=%d too large", P); return MODAL_ERR_ARG; }
-        MODAL_TRY(ensure(ctx->scratch, sizeof(double) * ((size_t)S * L * PP + (size_t)S * P * PP)));
+        // F partials [S][L][P*P] | B [S][P][P*P] | slab bases [L+1] | weight table [points]
+        long long npts = 0;
+        for (int i = lmin; i <= lmax; i++) npts += tet_row_offset(i, lmax + 1, lmax);
+        pl.npts = npts;
+        pl.o_B = sizeof(double) * (size_t)S * L * PP;
+        pl.o_sb = pl.o_B + sizeof(double) * (size_t)S * P * PP;
+        pl.o_w = pl.o_sb + sizeof(long long) * (size_t)(L + 1);
+        MODAL_TRY(ensure(ctx->scratch, pl.o_w + sizeof(double) * (size_t)npts));
         auto attr = [&](auto kern) -> modal_status {
             MODAL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
             return MODAL_OK;
@@ -794,13 +822,20 @@ modal_status proj_record(modal_ctx *ctx, const ProjPlan &pl)
                                                                               ctx->beta.as<double>());
         return launched(ctx, "project_beta");
     }
-    double *Fbuf = ctx->scratch.as<double>();
-    double *B = Fbuf + (size_t)S * L * PP;
+    uint8_t *b8 = ctx->scratch.as<uint8_t>();
+    double *Fbuf = reinterpret_cast<double *>(b8);
+    double *B = reinterpret_cast<double *>(b8 + pl.o_B);
+    long long *sbase = reinterpret_cast<long long *>(b8 + pl.o_sb);
+    double *Wd = reinterpret_cast<double *>(b8 + pl.o_w);
+    k_slab_base<<<1, 256, 0, ctx->stream>>>(lmin, lmax, sbase);
+    MODAL_TRY(launched(ctx, "slab_base"));
+    k_weight_table_fp64<<<dim3(L, ceil_div(L, 8)), 256, 0, ctx->stream>>>(lmin, lmax, ctx->vl.as<double>(), sbase, Wd);
+    MODAL_TRY(launched(ctx, "weight_table_fp64"));
     const int KMAX = (lmax - lmin) / 2 + 2;
     auto run = [&](auto kern) -> modal_status {
         kern<<<L, 256, pl.smem, ctx->stream>>>(lmin, lmax, P, S, KMAX, ctx->slab_order.as<int>(), ctx->q.as<double>(),
                                                ctx->vl.as<double>(), ctx->shape_desc.as<DShape>(),
-                                               ctx->shape_tab.as<double>(), Fbuf);
+                                               ctx->shape_tab.as<double>(), Wd, sbase, Fbuf);
         return launched(ctx, "project_slab_fp64");
     };
     if (pl.fpt <= 1) MODAL_TRY(run(k_project_slab_fp64<1>));

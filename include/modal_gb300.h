@@ -149,6 +149,16 @@ modal_status modal_get_gl(modal_ctx *ctx, int *nmu, double *nodes, double *weigh
  * gamma may be NULL: the result stays on the device for the next steps. */
 modal_status modal_gamma(modal_ctx *ctx, modal_prec prec, double *gamma);
 
+/* Gamma restricted to the quadrature nodes mu_begin .. mu_end - 1 (0 <= mu_begin <
+ * mu_end <= n_mu): the sum over the nodes in calculate_orthol
+ * (orthogonalisation_late.c:272-296) taken over that node range only.  Partials over disjoint ranges that
+ * cover all nodes add up to Gamma, so Gamma shards over the mu axis with one sum
+ * reduction of N x N doubles; the reference splits the (m, n) pairs over ranks
+ * instead (ortho_late_mpi.c:242-255).  gamma [N][N] on the host is required; the
+ * context's device Gamma is left invalid (a partial), so modal_orthogonalise
+ * needs the summed Gamma passed in. */
+modal_status modal_gamma_partial(modal_ctx *ctx, modal_prec prec, int mu_begin, int mu_end, double *gamma);
+
 /* result[0] = Gamma_mn (and result[1..3] = TTE, TEE, EEE after
  * modal_set_modes_pol), the per-pair interface of calculate_orthol
  * (orthogonalisation_late.c:239; global.h:211).  Computes the whole matrix

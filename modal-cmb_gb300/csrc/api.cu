@@ -433,12 +433,35 @@ modal_status modal_gamma(modal_ctx *c, modal_prec prec, double *gamma)
     if (!c->have_glint) MODAL_TRY(modal_init_glint(c));
     {
         StageTimer t(c, MODAL_T_GAMMA);
-        if (prec == MODAL_PREC_FP64) MODAL_TRY(gamma_fp64_dev(c));
-        else MODAL_TRY(gamma_split_dev(c));
+        if (prec == MODAL_PREC_FP64) MODAL_TRY(gamma_fp64_dev(c, 0, c->nmu));
+        else MODAL_TRY(gamma_split_dev(c, 0, c->nmu));
     }
     c->have_gamma = true;
     c->have_ortho = false;
     if (gamma) MODAL_TRY(d2h(c, gamma, c->gamma.ptr, sizeof(double) * (size_t)c->N * c->N));
+    return sync(c);
+}
+
+modal_status modal_gamma_partial(modal_ctx *c, modal_prec prec, int mu_begin, int mu_end, double *gamma)
+{
+    MODAL_TRY(need(c, c && c->have_modes, "modal_gamma_partial: set basis and modes first"));
+    if (prec != MODAL_PREC_FP64 && prec != MODAL_PREC_SPLIT) { set_error("modal_gamma_partial: prec=%d", (int)prec); return MODAL_ERR_ARG; }
+    if (!gamma) { set_error("modal_gamma_partial: gamma is NULL"); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    if (!c->have_glint) MODAL_TRY(modal_init_glint(c));
+    if (mu_begin < 0 || mu_end > c->nmu || mu_begin >= mu_end) {
+        set_error("modal_gamma_partial: node range [%d, %d) outside [0, %d) or empty", mu_begin, mu_end, c->nmu);
+        return MODAL_ERR_ARG;
+    }
+    {
+        StageTimer t(c, MODAL_T_GAMMA);
+        if (prec == MODAL_PREC_FP64) MODAL_TRY(gamma_fp64_dev(c, mu_begin, mu_end - mu_begin));
+        else MODAL_TRY(gamma_split_dev(c, mu_begin, mu_end - mu_begin));
+    }
+    // the device buffer now holds a partial sum, not Gamma
+    c->have_gamma = false;
+    c->have_ortho = false;
+    MODAL_TRY(d2h(c, gamma, c->gamma.ptr, sizeof(double) * (size_t)c->N * c->N));
     return sync(c);
 }
 

@@ -159,8 +159,9 @@ modal_status gl_nodes_dev(modal_ctx *ctx, int n, double *d_mu, double *d_w);
 modal_status legendre_table_dev(modal_ctx *ctx, int nmu, int lmax, const double *d_mu, double *d_pl);
 modal_status mij_dev(modal_ctx *ctx);
 modal_status mij_table_dev(modal_ctx *ctx, const double *q, int lmin, int lmax, int P, DevBuf &out);
-modal_status gamma_fp64_dev(modal_ctx *ctx);
-modal_status gamma_split_dev(modal_ctx *ctx);
+// Gamma over the quadrature nodes mu0 .. mu0 + nmu - 1 (all of them: mu0 = 0, nmu = ctx->nmu).
+modal_status gamma_fp64_dev(modal_ctx *ctx, int mu0, int nmu);
+modal_status gamma_split_dev(modal_ctx *ctx, int mu0, int nmu);
 modal_status ortho_dev(modal_ctx *ctx, int pca_flag);
 modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec);
 modal_status alpha_dev(modal_ctx *ctx, int S);

@@ -168,12 +168,12 @@ __global__ void __launch_bounds__(256) k_gamma_fp64(int N, int P, int nmu, int K
     }
 }
 
-modal_status gamma_fp64_dev(modal_ctx *ctx)
+modal_status gamma_fp64_dev(modal_ctx *ctx, int mu0, int nmu)
 {
-    const int N = ctx->N, P = ctx->P, nmu = ctx->nmu;
+    const int N = ctx->N, P = ctx->P;
     MODAL_TRY(ensure(ctx->gamma, sizeof(double) * (size_t)N * N));
     MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * nmu));
-    k_wgt48<<<ceil_div(nmu, 256), 256, 0, ctx->stream>>>(nmu, ctx->w.as<double>(), ctx->scratch2.as<double>());
+    k_wgt48<<<ceil_div(nmu, 256), 256, 0, ctx->stream>>>(nmu, ctx->w.as<double>() + mu0, ctx->scratch2.as<double>());
     MODAL_TRY(launched(ctx, "wgt48"));
     int KC = (96 * 1024) / (P * P * 8);
     if (KC < 1) KC = 1;
@@ -185,7 +185,8 @@ modal_status gamma_fp64_dev(modal_ctx *ctx)
     MODAL_CUDA(cudaFuncSetAttribute(k_gamma_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int nt = ceil_div(N, 32);
     dim3 grid(nt, nt);
-    k_gamma_fp64<<<grid, 256, smem, ctx->stream>>>(N, P, nmu, KC, ctx->triples.as<int>(), ctx->mt.as<double>(),
+    k_gamma_fp64<<<grid, 256, smem, ctx->stream>>>(N, P, nmu, KC, ctx->triples.as<int>(),
+                                                   ctx->mt.as<double>() + (size_t)mu0 * P * P,
                                                    ctx->scratch2.as<double>(), ctx->gamma.as<double>());
     return launched(ctx, "gamma_fp64");
 }

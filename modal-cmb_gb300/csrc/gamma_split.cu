@@ -477,10 +477,11 @@ struct SplitPlan {
     long long ntsym = 0;
 };
 
-modal_status gamma_split_dev(modal_ctx *ctx)
+modal_status gamma_split_dev(modal_ctx *ctx, int mu0, int nmu)
 {
     MODAL_TRY(get_encode());
-    const int P = ctx->P, N = ctx->N, nmu = ctx->nmu;
+    const int P = ctx->P, N = ctx->N;
+    const double *mt = ctx->mt.as<double>() + (size_t)mu0 * P * P, *w = ctx->w.as<double>() + mu0;
     const int U = P * (P + 1) / 2;
     const int Upad = ceil_div(U, SP_BM) * SP_BM;
     const long UV = (long)U * (U + 1) / 2;
@@ -555,10 +556,10 @@ modal_status gamma_split_dev(modal_ctx *ctx)
     }
     MODAL_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
 
-    k_wgt48_f<<<ceil_div(Kpad, 256), 256, 0, ctx->stream>>>(nmu, Kpad, ctx->w.as<double>(), wf);
+    k_wgt48_f<<<ceil_div(Kpad, 256), 256, 0, ctx->stream>>>(nmu, Kpad, w, wf);
     MODAL_TRY(launched(ctx, "wgt48_f"));
     k_split_x<<<ceil_div((long)Upad * 32, 256), 256, 0, ctx->stream>>>(
-        U, Upad, P, nmu, Kpad, reinterpret_cast<const int2 *>(b + o_pairs), ctx->mt.as<double>(), X1, X2, xf, sx);
+        U, Upad, P, nmu, Kpad, reinterpret_cast<const int2 *>(b + o_pairs), mt, X1, X2, xf, sx);
     MODAL_TRY(launched(ctx, "split_x"));
     k_split_y<<<ceil_div(UVpad * 32, 256), 256, 0, ctx->stream>>>(
         (int)UV, (int)UVpad, Kpad, reinterpret_cast<const int2 *>(b + o_vtp), xf, wf, Y1, Y2, sy);

@@ -28,7 +28,7 @@ EXPORTS = [
     "modal_ctx_create", "modal_ctx_destroy", "modal_last_error", "modal_ctx_stream", "modal_ctx_launches",
     "modal_ctx_sync", "modal_gl_nodes", "modal_legendre_table", "modal_basis_legendre", "modal_geometric",
     "modal_tetrapyd_count", "modal_set_basis", "modal_set_modes", "modal_set_gl", "modal_init_glint",
-    "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_orthol_pair", "modal_orthogonalise",
+    "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_gamma_partial", "modal_orthol_pair", "modal_orthogonalise",
     "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
     "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
@@ -88,6 +88,7 @@ def lib():
             "modal_get_mij": (i, [vp, vp]),
             "modal_get_gl": (i, [vp, ctypes.POINTER(i), vp, vp]),
             "modal_gamma": (i, [vp, i, vp]),
+            "modal_gamma_partial": (i, [vp, i, i, i, vp]),
             "modal_orthol_pair": (i, [vp, i, i, vp]),
             "modal_orthogonalise": (i, [vp, vp, i, vp, vp, ctypes.POINTER(i), ctypes.POINTER(i)]),
             "modal_set_spectrum": (i, [vp, vp]),
@@ -298,6 +299,13 @@ class Context:
         else:
             assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == self.N * self.N
         _check(lib().modal_gamma(self.h, prec, _ptr(out)))
+        return out
+
+    def gamma_partial(self, prec, mu_begin, mu_end):
+        """Gamma over the quadrature nodes mu_begin..mu_end-1 only (a shard of the
+        sum over mu; partials over a partition of the nodes add up to Gamma)."""
+        out = np.empty((self.N, self.N))
+        _check(lib().modal_gamma_partial(self.h, prec, mu_begin, mu_end, _ptr(out)))
         return out
 
     def orthol_pair(self, m, n, all_four=False):
@@ -627,6 +635,17 @@ CONFIGS = {
     # mid-size case for kernel captures: operands larger than L2, a few GB at most
     "prof": dict(lmax=1000, P=20, shapes=("sep", 4, 1, 2)),
 }
+
+
+def mu_shard(nmu, rank, world):
+    """[begin, end) of the quadrature nodes that rank `rank` of `world` sums over:
+    the balanced split the reference uses for its pair loop (ortho_late_mpi.c:
+    240-255), the first nmu % world ranks taking one node more."""
+    if not (0 <= rank < world) or nmu < world:
+        raise ValueError(f"mu_shard: rank {rank} of {world} for {nmu} nodes")
+    base, extra = divmod(nmu, world)
+    begin = rank * base + min(rank, extra)
+    return begin, begin + base + (1 if rank < extra else 0)
 
 
 def workload(lmax, P, lmin=2):

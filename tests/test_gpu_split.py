@@ -21,6 +21,28 @@ def _both(mg, lmin, lmax, P, triples=None):
     return G64, Gs, Gs2
 
 
+def test_gamma_partials_over_mu_shards(mg):
+    """Gamma over disjoint node ranges (mu_shard of 3 ranks) adds up to Gamma:
+    to rounding in FP64, and within the split tolerance in the split form."""
+    lmin, lmax, P = 2, 400, 10
+    q, tr, cl = mg.workload(lmax, P, lmin)
+    with mg.Context(0) as c:
+        c.set_basis(lmin, lmax, q)
+        c.set_modes(tr)
+        c.init_glint()
+        G64 = c.gamma(mg.PREC_FP64)
+        nmu = 3 * lmax // 2 + 1
+        shards = [mg.mu_shard(nmu, r, 3) for r in range(3)]
+        S64 = sum(c.gamma_partial(mg.PREC_FP64, b, e) for b, e in shards)
+        Ssp = sum(c.gamma_partial(mg.PREC_SPLIT, b, e) for b, e in shards)
+        with pytest.raises(mg.ModalError):
+            c.gamma_partial(mg.PREC_FP64, 5, 5)
+        with pytest.raises(mg.ModalError):  # the device Gamma is a partial now
+            c.orthogonalise(None)
+    assert rel_max(S64, G64) <= 1e-13
+    assert rel_fro(Ssp, G64) <= 1e-6 and rel_max(Ssp, G64) <= 1e-6
+
+
 @pytest.mark.parametrize("lmin,lmax,P", [(2, 40, 1), (2, 60, 4), (2, 500, 10), (3, 600, 17), (2, 700, 20)])
 def test_split_gamma_vs_fp64(mg, lmin, lmax, P):
     G64, Gs, Gs2 = _both(mg, lmin, lmax, P)

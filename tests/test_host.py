@@ -62,6 +62,54 @@ def test_replica_timing_is_max_over_ranks_gloo(tmp_path):
         assert vals == [2.0, 5.0, 0.5]
 
 
+def _gamma_shard_rank(rank, ws, port, out):
+    import torch
+    import torch.distributed as td
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws))
+    for d in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "modal-cmb_gb300")):
+        sys.path.insert(0, d)
+    import modal_gb300 as mg
+    import oracle
+    td.init_process_group("gloo", rank=rank, world_size=ws)
+    try:
+        lmax, P = 60, 6
+        q, tr, cl = mg.workload(lmax, P)
+        orc = oracle.Oracle()
+        nmu = 3 * lmax // 2 + 1
+        x, w = orc.gl_nodes(nmu)
+        M = orc.mij(orc.legendre_table(x, lmax), 2, lmax, q)
+        b, e = mg.mu_shard(nmu, rank, ws)
+        part = torch.from_numpy(orc.gamma(np.ascontiguousarray(M[:, :, b:e]), w[b:e], tr))
+        td.all_reduce(part, op=td.ReduceOp.SUM)
+        np.save(f"{out}.{rank}.npy", part.numpy())
+    finally:
+        td.destroy_process_group()
+
+
+def test_gamma_mu_shards_sum_over_ranks_gloo(tmp_path):
+    """Gamma shards over the quadrature nodes: two gloo ranks each sum their
+    mu_shard of the nodes and one sum all-reduce gives the whole Gamma (the
+    oracle computes the partials, so this runs on the CPU)."""
+    import socket
+    import torch.multiprocessing as mp
+    sys.path.insert(0, ROOT)
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = os.fspath(tmp_path / "g")
+    mp.start_processes(_gamma_shard_rank, args=(2, port, out), nprocs=2, start_method="spawn", join=True)
+    import modal_gb300 as mg
+    import oracle
+    lmax, P = 60, 6
+    q, tr, cl = mg.workload(lmax, P)
+    orc = oracle.Oracle()
+    x, w = orc.gl_nodes(3 * lmax // 2 + 1)
+    full = orc.gamma(orc.mij(orc.legendre_table(x, lmax), 2, lmax, q), w, tr)
+    for r in range(2):
+        got = np.load(f"{out}.{r}.npy")
+        assert np.max(np.abs(got - full)) <= 1e-13 * np.max(np.abs(full))
+
+
 def test_max_over_ranks_single_rank_is_identity():
     sys.path.insert(0, ROOT)
     import bench

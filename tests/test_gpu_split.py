@@ -1,6 +1,7 @@
-"""Split-precision (FP16x2, tensor-core) Gamma against the FP64 form on the
-GPU.  Tolerance: relative Frobenius and relative max error <= 1e-6 (the
-target for the split form); emulation predicts ~5e-8."""
+"""Split-precision forms against FP64 on the GPU: the tensor-core Gamma (FP16
+hi/lo pieces), its node-range partials, and the compensated FP32 projection.
+Tolerance: relative Frobenius and relative max error <= 1e-6 (the target for
+the split form); emulation predicts ~5e-8."""
 import numpy as np
 import pytest
 from conftest import rel_fro, rel_max
@@ -19,6 +20,29 @@ def _both(mg, lmin, lmax, P, triples=None):
         Gs = c.gamma(mg.PREC_SPLIT)
         Gs2 = c.gamma(mg.PREC_SPLIT)
     return G64, Gs, Gs2
+
+
+def test_split_projection_many_term_shapes(mg):
+    """Separable shapes of more than 8 terms take the FP32 kernel's general
+    evaluation (all nine table values per term), next to few-term and bump
+    shapes in the same group: <= 1e-6 against FP64, and the captured batch
+    gives the same bits as the direct call."""
+    lmin, lmax, P = 2, 300, 10
+    cl = mg.synthetic_cl(lmax)
+    q = mg.weighted_q(mg.legendre_q(lmin, lmax, P), cl, lmin)
+    shapes = (mg.separable_shapes(lmax, 3, seed=21, tmin=9, tmax=12) + mg.separable_shapes(lmax, 3, seed=22, tmin=1, tmax=3)
+              + mg.bump_shapes(2, seed=23))
+    assert any(s["tab"].shape[0] > 8 for s in shapes)
+    with mg.Context(0) as c:
+        c.set_basis(lmin, lmax, q)
+        c.set_modes(mg.mode_triples(P))
+        c.set_spectrum(cl)
+        b64 = c.project(shapes, mg.PREC_FP64)
+        bs = c.project(shapes, mg.PREC_SPLIT)
+        bb = c.project_batch(shapes, mg.PREC_SPLIT)
+    assert np.array_equal(bs, bb)
+    for s in range(len(shapes)):
+        assert rel_fro(bs[s], b64[s]) <= 1e-6, (s, rel_fro(bs[s], b64[s]))
 
 
 def test_gamma_partials_over_mu_shards(mg):

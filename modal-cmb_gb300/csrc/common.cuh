@@ -66,7 +66,10 @@ struct modal_ctx {
     modal::DevBuf shape_desc;  // device shape descriptors
     modal::DevBuf slab_order;  // projection slab schedule
     modal::DevBuf split;       // split-precision Gamma: operand pieces, T table, per-P tables
-    int split_P = -1;          // P the per-P tables in `split` were built for
+    int split_P = -1;          // layout the tables in `split` were uploaded for: P, K padding, buffer
+    long split_key = -1;
+    void *split_ptr = nullptr;
+    size_t split_bytes = 0;
     int gl_n = -1;             // n of the GPU quadrature held in mu/w (-1: none or caller-supplied)
 
     // late x primordial transfer Gamma

@@ -543,7 +543,10 @@ modal_status gamma_split_dev(modal_ctx *ctx, int mu0, int nmu)
     double *sx = reinterpret_cast<double *>(b + o_sx), *sy = reinterpret_cast<double *>(b + o_sy);
     int *err = reinterpret_cast<int *>(b + o_err);
     float *Tsym = reinterpret_cast<float *>(b + o_T);
-    if (ctx->split_P != P) {
+    // the host tables depend on P and, through the offsets, on the K padding; a
+    // reallocated buffer has lost them
+    if (ctx->split_P != P || ctx->split_key != (long)Kpad || ctx->split_ptr != ctx->split.ptr ||
+        ctx->split_bytes != ctx->split.bytes) {
         MODAL_CUDA(cudaMemcpyAsync(b + o_pairs, pairs.data(), U * sizeof(int2), cudaMemcpyHostToDevice, ctx->stream));
         MODAL_CUDA(cudaMemcpyAsync(b + o_pidx, pidx.data(), pidx.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
         MODAL_CUDA(cudaMemcpyAsync(b + o_vbase, vbase.data(), U * 8, cudaMemcpyHostToDevice, ctx->stream));
@@ -553,6 +556,9 @@ modal_status gamma_split_dev(modal_ctx *ctx, int mu0, int nmu)
                                    ctx->stream));
         MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
         ctx->split_P = P;
+        ctx->split_key = Kpad;
+        ctx->split_ptr = ctx->split.ptr;
+        ctx->split_bytes = ctx->split.bytes;
     }
     MODAL_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
 

@@ -45,6 +45,25 @@ def test_split_projection_many_term_shapes(mg):
         assert rel_fro(bs[s], b64[s]) <= 1e-6, (s, rel_fro(bs[s], b64[s]))
 
 
+def test_split_gamma_after_basis_and_range_changes(mg):
+    """One context: the split form's cached tables follow changes of l_max (the
+    node count and the K padding) at the same P, and node-range partials after a
+    full Gamma."""
+    P = 6
+    with mg.Context(0) as c:
+        for lmax in (300, 700, 200):
+            q, tr, cl = mg.workload(lmax, P)
+            c.set_basis(2, lmax, q)
+            c.set_modes(tr)
+            c.init_glint()
+            G64 = c.gamma(mg.PREC_FP64)
+            Gs = c.gamma(mg.PREC_SPLIT)
+            assert rel_max(Gs, G64) <= 1e-6, lmax
+        nmu = 3 * 200 // 2 + 1
+        Sp = c.gamma_partial(mg.PREC_SPLIT, 0, 64) + c.gamma_partial(mg.PREC_SPLIT, 64, nmu)
+        assert rel_max(Sp, G64) <= 1e-6
+
+
 def test_gamma_partials_over_mu_shards(mg):
     """Gamma over disjoint node ranges (mu_shard of 3 ranks) adds up to Gamma:
     to rounding in FP64, and within the split tolerance in the split form."""

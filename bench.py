@@ -337,6 +337,7 @@ def run_ours(a, ws, rank, local):
         cpu = cpu_baseline(a.config, lmax, P, q, tr, cl, shapes, samples=1)
     ctx.close()
     extras = run_extras(mg, local) if rank == 0 and a.config == "cfg2" else None
+    next_rows = run_next_rows(mg, local, not a.no_cpu_baseline) if rank == 0 and a.config == "cfg2" else None
     line = {
         "metric": METRIC, "value": go_ms * 1e-3, "unit": "s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -348,6 +349,7 @@ def run_ours(a, ws, rank, local):
         "projections_per_s": S * ws / (proj_ms * 1e-3),
         "tuning": tuning,
         "extras": extras,
+        "next_rows": next_rows,
         "stage_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in tm.items()},
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -390,6 +392,108 @@ def run_extras(mg, local):
         t0 = time.perf_counter()
         order, lam = c.basis_prune()
         out["basis_prune_364_s"] = time.perf_counter() - t0
+    return out
+
+
+def _dev_ms(c, fn, reps=3):
+    """Median device time of fn() on the context stream (CUDA events), after one warm-up."""
+    import torch
+    stream = torch.cuda.ExternalStream(c.stream)
+    fn()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def _fit_cpu(fn, n1, n2, N, power):
+    """CPU time at size N from timings at n1 < n2, modelled as a + b n^power (a:
+    the work that does not grow with the sample, such as tables or the grid walk)."""
+    t = []
+    for n in (n1, n2):
+        t0 = time.perf_counter()
+        fn(n)
+        t.append(time.perf_counter() - t0)
+    b = max(0.0, (t[1] - t[0]) / (n2 ** power - n1 ** power))
+    a = max(0.0, t[0] - b * n1 ** power)
+    return a + b * N ** power
+
+
+def run_next_rows(mg, local, with_cpu):
+    """The rows next to the hot path, each on one synthetic workload: device time
+    through the C ABI and, with the CPU baseline, the CPU restatement of the
+    reference's routine timed on a bounded sample of the same workload and scaled
+    by that routine's cost law (stated per row).  The CPU restatement's OpenMP
+    routines use every host core."""
+    out = {}
+    orc = None
+    if with_cpu:
+        import oracle
+        orc = oracle.Oracle()
+    cores = os.cpu_count() or 1
+
+    # polarised Gamma: calculate_orthol results[1..3] (orthogonalisation_late.c:239-336)
+    lmax, P = 1000, 16
+    cl, qT, qE, ttt, tte, tee, eee = mg.pol_workload(lmax, lmax, 2, P, P)
+    N = len(ttt)
+    with mg.Context(local) as c:
+        c.set_basis(2, lmax, qT)
+        c.set_modes(ttt)
+        c.set_basis_e(2, lmax, qE)
+        c.set_modes_pol(tte, tee, eee)
+        c.init_glint()
+        row = {"workload": f"TTE+TEE+EEE Gamma, T and E on l=2..{lmax}, P_T=P_E={P}, N={N}",
+               "gpu_ms": _dev_ms(c, c.gamma_pol)}
+        x, w = c.get_gl()
+    if orc is not None:
+        pl = orc.legendre_table(x, lmax)
+        MT, ME = orc.mij(pl, 2, lmax, qT), orc.mij(pl, 2, lmax, qE)
+        row["cpu_s"] = _fit_cpu(lambda n: orc.gamma_pol(MT, ME, w, tte[:n], tee[:n], eee[:n]), 192, 384, N, 2)
+        row["cpu_sample"] = f"192 and 384 of {N} modes of each family, fitted as a + b n^2; cores {cores}"
+    out["polarised_gamma"] = row
+
+    # late x primordial transfer Gamma: calculate_gamma_2d over all (m, n) (calculate_gamma.c:773-934)
+    lmax, P, Pp, xsize = 600, 16, 8, 32
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = mg.transfer_workload(lmax, Pp, xsize)
+    prim = mg.mode_triples(Pp)
+    N, Np = len(tr), len(prim)
+    with mg.Context(local) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        c.init_glint()
+        c.set_transfer(xvec, qt, prim)
+        row = {"workload": f"transfer Gamma, l=2..{lmax}, P={P} (N={N}), P_prim={Pp} (N_prim={Np}), {xsize} x points",
+               "gpu_ms": _dev_ms(c, lambda: c.gamma_transfer(0.7))}
+        x, w = c.get_gl()
+    if orc is not None:
+        row["cpu_s"] = _fit_cpu(lambda n: orc.gamma_transfer(2, lmax, q, tr[:n], cl, x, w, xvec, qt, prim, 0.7),
+                                16, 64, N, 1)
+        row["cpu_sample"] = f"16 and 64 of {N} late modes (rows), fitted as a + b n (a: the per-x M tables); cores {cores}"
+    out["transfer_gamma"] = row
+
+    # primordial k-space side: calculate_ortho (orthogonalisation.c:14-86) and calculate_eigen
+    kmin, kmax_i, kmax, Pp = 1, 120, 0.5, 12
+    basis, prim, shapes = mg.prim_workload(kmax_i, Pp)
+    N = len(prim)
+    npts = len(mg.prim_points(kmin, kmax_i))
+    with mg.Context(local) as c:
+        row = {"workload": f"k-grid Gram matrix and 2 shape projections, grid 1..{kmax_i} ({npts} points), P={Pp}, N={N}",
+               "gpu_ms_ortho": _dev_ms(c, lambda: c.prim_ortho(kmin, kmax_i, kmax, basis, prim)),
+               "gpu_ms_eigen": _dev_ms(c, lambda: c.prim_eigen(kmin, kmax_i, kmax, basis, prim, shapes))}
+    if orc is not None:
+        row["cpu_s_ortho"] = _fit_cpu(lambda n: orc.prim_ortho(kmin, kmax_i, kmax, basis, prim[:n]), 48, 96, N, 2)
+        row["cpu_s_eigen"] = _fit_cpu(lambda n: [orc.prim_eigen(kmin, kmax_i, kmax, basis, prim[:n], sh) for sh in shapes],
+                                      12, 48, N, 1)
+        row["cpu_sample"] = (f"48 and 96 of {N} modes for the Gram matrix (a + b n^2), 12 and 48 for the "
+                             "projections (a + b n); 1 core")
+    out["primordial"] = row
     return out
 
 

@@ -212,5 +212,11 @@ void batch_release(modal_ctx *ctx);
 //   lower != 0: only entries with n <= m (tiles above the diagonal skipped).
 modal_status dgemm(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, int lda, bool transA,
                    const double *B, int ldb, bool transB, double beta, double *C, int ldc, int lower);
+// C (+)= A op(B) for A [S][K] with few rows S: skinny kernels for S <= 32 (alpha 1; accumulate: C +=)
+modal_status dgemm_rows(modal_ctx *ctx, int S, int N, int K, const double *A, int lda, const double *B, int ldb,
+                        bool transB, double *C, int ldc, bool accumulate);
+// dgemm with K split over CTAs for small output grids and long K (alpha 1; accumulate: C +=)
+modal_status dgemm_splitk(modal_ctx *ctx, int M, int N, int K, const double *A, int lda, bool transA, const double *B,
+                          int ldb, bool transB, double *C, int ldc, int lower, bool accumulate);
 
 }  // namespace modal

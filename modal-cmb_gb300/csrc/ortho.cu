@@ -31,10 +31,13 @@ constexpr int GT = 64, GK = 16;
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, const double *__restrict__ A, int lda,
                                                const double *__restrict__ B, int ldb, double beta, double *C, int ldc,
-                                               int lower)
+                                               int lower, long cstride)
 {
     const int bm = blockIdx.y * GT, bn = blockIdx.x * GT;
     if (lower && bn > bm + GT - 1) return;
+    // slice z of gridDim.z sums k in [kbeg, kend) into C + z * cstride
+    const int kbeg = (int)((long)K * blockIdx.z / gridDim.z), kend = (int)((long)K * (blockIdx.z + 1) / gridDim.z);
+    C += (size_t)blockIdx.z * cstride;
     __shared__ double As[GK][GT + 1];
     __shared__ double Bs[GK][GT + 1];
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
@@ -44,7 +47,7 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
 #pragma unroll
         for (int j = 0; j < 4; j++) acc[i][j] = 0.0;
 
-    for (int k0 = 0; k0 < K; k0 += GK) {
+    for (int k0 = kbeg; k0 < kend; k0 += GK) {
 #pragma unroll
         for (int t = 0; t < (GK * GT) / 256; t++) {
             int e = tid + 256 * t;
@@ -53,7 +56,7 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
             else { kk = e % GK; mm = e / GK; }
             int m = bm + mm, k = k0 + kk;
             double v = 0.0;
-            if (m < M && k < K) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+            if (m < M && k < kend) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
             As[kk][mm] = v;
         }
 #pragma unroll
@@ -64,7 +67,7 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
             else { nn = e % GT; kk = e / GT; }
             int n = bn + nn, k = k0 + kk;
             double v = 0.0;
-            if (n < N && k < K) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
+            if (n < N && k < kend) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
             Bs[kk][nn] = v;
         }
         __syncthreads();
@@ -96,16 +99,58 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
     }
 }
 
+static modal_status dgemm_launch(modal_ctx *ctx, dim3 grid, int M, int N, int K, double alpha, const double *A, int lda,
+                                 bool transA, const double *B, int ldb, bool transB, double beta, double *C, int ldc,
+                                 int lower, long cstride)
+{
+    if (!transA && !transB) k_dgemm<false, false><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower, cstride);
+    else if (!transA && transB) k_dgemm<false, true><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower, cstride);
+    else if (transA && !transB) k_dgemm<true, false><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower, cstride);
+    else k_dgemm<true, true><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower, cstride);
+    return launched(ctx, "dgemm");
+}
+
 modal_status dgemm(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, int lda, bool transA,
                    const double *B, int ldb, bool transB, double beta, double *C, int ldc, int lower)
 {
     if (M <= 0 || N <= 0) return MODAL_OK;
     dim3 grid(ceil_div(N, GT), ceil_div(M, GT));
-    if (!transA && !transB) k_dgemm<false, false><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-    else if (!transA && transB) k_dgemm<false, true><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-    else if (transA && !transB) k_dgemm<true, false><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-    else k_dgemm<true, true><<<grid, 256, 0, ctx->stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower);
-    return launched(ctx, "dgemm");
+    return dgemm_launch(ctx, grid, M, N, K, alpha, A, lda, transA, B, ldb, transB, beta, C, ldc, lower, 0);
+}
+
+// C (+)= op(A) op(B) with K split over KS slices of the tiled kernel, for products
+// whose M x N tile grid is too small to fill the GPU but whose K is long (the
+// primordial grid's point sums).  The KS partial products land in a buffer and
+// are added in a fixed order.
+__global__ void k_splitk_sum(int M, int N, int KS, const double *__restrict__ part, double *__restrict__ C, int ldc,
+                             int lower, int accumulate)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)M * N) return;
+    const int m = (int)(e / N), n = (int)(e - (size_t)m * N);
+    if (lower && n > m) return;
+    double v = accumulate ? C[(size_t)m * ldc + n] : 0.0;
+    for (int p = 0; p < KS; p++) v += part[(size_t)p * M * N + e];
+    C[(size_t)m * ldc + n] = v;
+}
+
+modal_status dgemm_splitk(modal_ctx *ctx, int M, int N, int K, const double *A, int lda, bool transA, const double *B,
+                          int ldb, bool transB, double *C, int ldc, int lower, bool accumulate)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return MODAL_OK;
+    int nsm = 0;
+    MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    long tiles = (long)ceil_div(M, GT) * ceil_div(N, GT);
+    if (lower) tiles = (tiles + ceil_div(M, GT)) / 2;
+    int KS = (int)std::min<long>(std::max<long>(1, ceil_div(2L * nsm, tiles)), std::max(1, K / 256));
+    KS = std::min(KS, 64);
+    if (KS == 1) return dgemm(ctx, M, N, K, 1.0, A, lda, transA, B, ldb, transB, accumulate ? 1.0 : 0.0, C, ldc, lower);
+    MODAL_TRY(ensure(ctx->gemm_part, sizeof(double) * (size_t)KS * M * N));
+    double *part = ctx->gemm_part.as<double>();
+    MODAL_TRY(dgemm_launch(ctx, dim3(ceil_div(N, GT), ceil_div(M, GT), KS), M, N, K, 1.0, A, lda, transA, B, ldb, transB,
+                           0.0, part, N, lower, (long)M * N));
+    k_splitk_sum<<<ceil_div((long)M * N, 256), 256, 0, ctx->stream>>>(M, N, KS, part, C, ldc, lower, accumulate ? 1 : 0);
+    return launched(ctx, "splitk_sum");
 }
 
 // --------------------------------------------------------------------------
@@ -117,20 +162,22 @@ modal_status dgemm(modal_ctx *ctx, int M, int N, int K, double alpha, const doub
 constexpr int SK_S = 16, SK_KCH = 128, SK_KS = 8;
 
 // B row-major [K][ldb]: grid (ceil(N / 64), KS); 256 threads = 64 columns x 4 k-lanes.
+// R: rows held per thread (S <= R <= SK_S).
+template <int R>
 __global__ void __launch_bounds__(256) k_skinny_nn(int S, int N, int K, const double *__restrict__ A, int lda,
                                                    const double *__restrict__ B, int ldb, double *__restrict__ part)
 {
-    __shared__ double As[SK_KCH][SK_S];
-    __shared__ double red[3][SK_S][64];
+    __shared__ double As[SK_KCH][R];
+    __shared__ double red[3][R][64];
     const int col = threadIdx.x & 63, kl = threadIdx.x >> 6, n = blockIdx.x * 64 + col;
     const int k0 = (int)((long)K * blockIdx.y / gridDim.y), k1 = (int)((long)K * (blockIdx.y + 1) / gridDim.y);
-    double acc[SK_S];
+    double acc[R];
 #pragma unroll
-    for (int s = 0; s < SK_S; s++) acc[s] = 0.0;
+    for (int s = 0; s < R; s++) acc[s] = 0.0;
     for (int kc = k0; kc < k1; kc += SK_KCH) {
         const int len = min(SK_KCH, k1 - kc);
-        for (int e = threadIdx.x; e < SK_KCH * SK_S; e += 256) {
-            const int kk = e / SK_S, s = e - kk * SK_S;
+        for (int e = threadIdx.x; e < SK_KCH * R; e += 256) {
+            const int kk = e / R, s = e - kk * R;
             As[kk][s] = (kk < len && s < S) ? A[(size_t)s * lda + kc + kk] : 0.0;
         }
         __syncthreads();
@@ -138,37 +185,38 @@ __global__ void __launch_bounds__(256) k_skinny_nn(int S, int N, int K, const do
             for (int kk = kl; kk < len; kk += 4) {
                 const double b = B[(size_t)(kc + kk) * ldb + n];
 #pragma unroll
-                for (int s = 0; s < SK_S; s++) acc[s] = fma(As[kk][s], b, acc[s]);
+                for (int s = 0; s < R; s++) acc[s] = fma(As[kk][s], b, acc[s]);
             }
         __syncthreads();
     }
     if (kl > 0)
 #pragma unroll
-        for (int s = 0; s < SK_S; s++) red[kl - 1][s][col] = acc[s];
+        for (int s = 0; s < R; s++) red[kl - 1][s][col] = acc[s];
     __syncthreads();
     if (kl == 0 && n < N)
 #pragma unroll
-        for (int s = 0; s < SK_S; s++)
+        for (int s = 0; s < R; s++)
             if (s < S) part[((size_t)blockIdx.y * S + s) * N + n] = ((acc[s] + red[0][s][col]) + red[1][s][col]) + red[2][s][col];
 }
 
 // B row-major [N][ldb] used transposed: grid (ceil(N / 16), KS); warp w takes rows
 // n = 16 x + 2 w and 2 w + 1, lanes run over k.
+template <int R>
 __global__ void __launch_bounds__(256) k_skinny_nt(int S, int N, int K, const double *__restrict__ A, int lda,
                                                    const double *__restrict__ B, int ldb, double *__restrict__ part)
 {
-    __shared__ double As[SK_S][SK_KCH];
+    __shared__ double As[R][SK_KCH];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n0 = blockIdx.x * 16 + 2 * warp;
     const int k0 = (int)((long)K * blockIdx.y / gridDim.y), k1 = (int)((long)K * (blockIdx.y + 1) / gridDim.y);
-    double acc[2][SK_S];
+    double acc[2][R];
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
-        for (int s = 0; s < SK_S; s++) acc[r][s] = 0.0;
+        for (int s = 0; s < R; s++) acc[r][s] = 0.0;
     for (int kc = k0; kc < k1; kc += SK_KCH) {
         const int len = min(SK_KCH, k1 - kc);
-        for (int e = threadIdx.x; e < SK_KCH * SK_S; e += 256) {
+        for (int e = threadIdx.x; e < SK_KCH * R; e += 256) {
             const int s = e / SK_KCH, kk = e - s * SK_KCH;
             As[s][kk] = (kk < len && s < S) ? A[(size_t)s * lda + kc + kk] : 0.0;
         }
@@ -178,7 +226,7 @@ __global__ void __launch_bounds__(256) k_skinny_nt(int S, int N, int K, const do
 #pragma unroll
             for (int r = 0; r < 2; r++) b[r] = (n0 + r < N) ? B[(size_t)(n0 + r) * ldb + kc + kk] : 0.0;
 #pragma unroll
-            for (int s = 0; s < SK_S; s++) {
+            for (int s = 0; s < R; s++) {
                 const double a = As[s][kk];
                 acc[0][s] = fma(a, b[0], acc[0][s]);
                 acc[1][s] = fma(a, b[1], acc[1][s]);
@@ -189,7 +237,7 @@ __global__ void __launch_bounds__(256) k_skinny_nt(int S, int N, int K, const do
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
-        for (int s = 0; s < SK_S; s++) {
+        for (int s = 0; s < R; s++) {
             double v = acc[r][s];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -199,34 +247,43 @@ __global__ void __launch_bounds__(256) k_skinny_nt(int S, int N, int K, const do
 #pragma unroll
         for (int r = 0; r < 2; r++)
 #pragma unroll
-            for (int s = 0; s < SK_S; s++)
+            for (int s = 0; s < R; s++)
                 if (n0 + r < N && s < S) part[((size_t)blockIdx.y * S + s) * N + n0 + r] = acc[r][s];
 }
 
-__global__ void k_skinny_sum(int S, int N, int KS, const double *__restrict__ part, double *__restrict__ C, int ldc)
+__global__ void k_skinny_sum(int S, int N, int KS, const double *__restrict__ part, double *__restrict__ C, int ldc,
+                             int accumulate)
 {
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (size_t)S * N) return;
     const int s = (int)(e / N), n = (int)(e - (size_t)s * N);
-    double v = 0.0;
+    double v = accumulate ? C[(size_t)s * ldc + n] : 0.0;
     for (int p = 0; p < KS; p++) v += part[(size_t)p * S * N + e];
     C[(size_t)s * ldc + n] = v;
 }
 
-// C = A op(B) (alpha 1, beta 0) with A [S][K]; S > 32 goes to the tiled kernel.
+// C (+)= A op(B) (alpha 1) with A [S][K]; S > 32 goes to the tiled kernel.
 modal_status dgemm_rows(modal_ctx *ctx, int S, int N, int K, const double *A, int lda, const double *B, int ldb,
-                        bool transB, double *C, int ldc)
+                        bool transB, double *C, int ldc, bool accumulate)
 {
-    if (S > 2 * SK_S) return dgemm(ctx, S, N, K, 1.0, A, lda, false, B, ldb, transB, 0.0, C, ldc, 0);
+    if (S > 2 * SK_S) return dgemm(ctx, S, N, K, 1.0, A, lda, false, B, ldb, transB, accumulate ? 1.0 : 0.0, C, ldc, 0);
     if (S <= 0 || N <= 0) return MODAL_OK;
     MODAL_TRY(ensure(ctx->gemm_part, sizeof(double) * (size_t)SK_KS * SK_S * N));
     double *part = ctx->gemm_part.as<double>();
     for (int s0 = 0; s0 < S; s0 += SK_S) {
         const int Sc = std::min(SK_S, S - s0);
-        if (transB) k_skinny_nt<<<dim3(ceil_div(N, 16), SK_KS), 256, 0, ctx->stream>>>(Sc, N, K, A + (size_t)s0 * lda, lda, B, ldb, part);
-        else k_skinny_nn<<<dim3(ceil_div(N, 64), SK_KS), 256, 0, ctx->stream>>>(Sc, N, K, A + (size_t)s0 * lda, lda, B, ldb, part);
+        const double *As = A + (size_t)s0 * lda;
+        auto run = [&](auto nt, auto nn) {
+            if (transB) nt<<<dim3(ceil_div(N, 16), SK_KS), 256, 0, ctx->stream>>>(Sc, N, K, As, lda, B, ldb, part);
+            else nn<<<dim3(ceil_div(N, 64), SK_KS), 256, 0, ctx->stream>>>(Sc, N, K, As, lda, B, ldb, part);
+        };
+        if (Sc <= 2) run(k_skinny_nt<2>, k_skinny_nn<2>);
+        else if (Sc <= 4) run(k_skinny_nt<4>, k_skinny_nn<4>);
+        else if (Sc <= 8) run(k_skinny_nt<8>, k_skinny_nn<8>);
+        else run(k_skinny_nt<SK_S>, k_skinny_nn<SK_S>);
         MODAL_TRY(launched(ctx, "skinny_gemm"));
-        k_skinny_sum<<<ceil_div((long)Sc * N, 256), 256, 0, ctx->stream>>>(Sc, N, SK_KS, part, C + (size_t)s0 * ldc, ldc);
+        k_skinny_sum<<<ceil_div((long)Sc * N, 256), 256, 0, ctx->stream>>>(Sc, N, SK_KS, part, C + (size_t)s0 * ldc, ldc,
+                                                                            accumulate ? 1 : 0);
         MODAL_TRY(launched(ctx, "skinny_sum"));
     }
     return MODAL_OK;
@@ -494,10 +551,10 @@ modal_status alpha_dev(modal_ctx *ctx, int S)
     MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)S * N));
     double *y = ctx->scratch2.as<double>();
     const double *lam = ctx->lambdal.as<double>();
-    MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->beta.as<double>(), N, lam, N, true, y, N));
-    MODAL_TRY(dgemm_rows(ctx, S, N, N, y, N, lam, N, false, ctx->alpha.as<double>(), N));
+    MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->beta.as<double>(), N, lam, N, true, y, N, false));
+    MODAL_TRY(dgemm_rows(ctx, S, N, N, y, N, lam, N, false, ctx->alpha.as<double>(), N, false));
     MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->alpha.as<double>(), N, ctx->orthol.as<double>(), N, false,
-                         ctx->modesr.as<double>(), N));
+                         ctx->modesr.as<double>(), N, false));
     return MODAL_OK;
 }
 

@@ -169,7 +169,7 @@ __global__ void k_prim_modes(long n, int N, int P, const int *__restrict__ ijk, 
     if (Bw) Bw[e] = x[t] * v;
 }
 
-// Shape values of a chunk: Sw[t][s] = x_t S_s(pt), n2[s] += x S^2 (per-chunk partial, atomics)
+// Shape values of a chunk: Sw[s][t] = x_t S_s(pt), n2[s] += x S^2 (per-chunk partial, atomics)
 __global__ void k_prim_shapes(long n, int S, int stride, const int *__restrict__ ijk, const double *__restrict__ x,
                               const DShape *__restrict__ sh, const double *__restrict__ tab, double *__restrict__ Sw,
                               double *__restrict__ n2)
@@ -194,7 +194,7 @@ __global__ void k_prim_shapes(long n, int S, int stride, const int *__restrict__
         const double x1 = i / L - d.c1, x2 = j / L - d.c2, x3 = k / L - d.c3;
         val = exp(-(x1 * x1 + x2 * x2 + x3 * x3) / (2.0 * d.sigma * d.sigma));
     }
-    Sw[e] = x[t] * val;
+    Sw[(size_t)s * n + t] = x[t] * val;
     atomicAdd(&n2[s], x[t] * (val * val));
 }
 
@@ -341,7 +341,7 @@ modal_status modal_prim_ortho(modal_ctx *c, int min, int max, double kmax, int P
                                                                    run.Bw);
         MODAL_TRY(launched(c, "prim_modes"));
         // G[s][r] += sum_t Bw[t][s] B[t][r]  (lower triangle s >= r)
-        MODAL_TRY(dgemm(c, N, N, (int)n, 1.0, run.Bw, N, true, run.B, N, false, 1.0, G, N, 1));
+        MODAL_TRY(dgemm_splitk(c, N, N, (int)n, run.Bw, N, true, run.B, N, false, G, N, 1, true));
     }
     k_pack_upper<<<ceil_div((long)N * (N + 1) / 2, 256), 256, 0, c->stream>>>(N, G, packed);
     MODAL_TRY(launched(c, "pack_upper"));
@@ -395,7 +395,7 @@ modal_status modal_prim_eigen(modal_ctx *c, int min, int max, double kmax, int P
     MODAL_CUDA(cudaMemsetAsync(A, 0, sizeof(double) * (size_t)S * N, c->stream));
     MODAL_CUDA(cudaMemsetAsync(n2, 0, sizeof(double) * S, c->stream));
     StageTimer t(c, MODAL_T_PROJECT);
-    double *Sw = run.Bw;  // [C][S] shape values times x
+    double *Sw = run.Bw;  // [S][C] shape values times x
     for (long p0 = 0; p0 < run.g.npts; p0 += run.C) {
         const long n = std::min(run.C, run.g.npts - p0);
         k_prim_weights<<<ceil_div(n, 256), 256, 0, c->stream>>>(p0, n, min, max, run.g.nslab, run.d_off, kmax, run.x,
@@ -406,8 +406,8 @@ modal_status modal_prim_eigen(modal_ctx *c, int min, int max, double kmax, int P
         MODAL_TRY(launched(c, "prim_modes"));
         k_prim_shapes<<<ceil_div(n * S, 256), 256, 0, c->stream>>>(n, S, max + 1, run.ijk, run.x, dsh, tab, Sw, n2);
         MODAL_TRY(launched(c, "prim_shapes"));
-        // A[s][r] += sum_t Sw[t][s] B[t][r]
-        MODAL_TRY(dgemm(c, S, N, (int)n, 1.0, Sw, S, true, run.B, N, false, 1.0, A, N, 0));
+        // A[s][r] += sum_t Sw[s][t] B[t][r]
+        MODAL_TRY(dgemm_rows(c, S, N, (int)n, Sw, (int)n, run.B, N, false, A, N, true));
     }
     t.stop();
     MODAL_CUDA(cudaMemcpyAsync(alpha, A, sizeof(double) * (size_t)S * N, cudaMemcpyDeviceToHost, c->stream));

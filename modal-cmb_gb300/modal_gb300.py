@@ -581,6 +581,43 @@ def separable_shapes(lmax, S, seed, tmin=1, tmax=2):
     return out
 
 
+def pol_workload(lmaxT, lmaxE, lminE, PT, PE):
+    """Polarised case: T basis on 2..lmaxT, E basis on lminE..lmaxE with its own
+    weight, and the first N = C(PT+2, 3) triples of each family in the
+    find_perm_late_XXX conventions (TTE: T,T,E; TEE: T,E,E; EEE)."""
+    cl = synthetic_cl(max(lmaxT, lmaxE))
+    qT = weighted_q(legendre_q(2, lmaxT, PT), cl, 2)
+    qE = weighted_q(legendre_q(lminE, lmaxE, PE), cl * 2.0, lminE)
+    ttt = mode_triples(PT)
+    N = len(ttt)
+    tte = np.array([(p, r, s) for p in range(PT) for r in range(p, PT) for s in range(PE)][:N], dtype=np.int32)
+    tee = np.array([(t, a, b) for t in range(PT) for a in range(PE) for b in range(a, PE)][:N], dtype=np.int32)
+    eee = mode_triples(PE)[:N]
+    return cl, qT, qE, ttt, tte, tee, eee
+
+
+def transfer_workload(lmax, Pp, xsize):
+    """Radial grid x in [1000, 12000] and smooth synthetic transfer functions
+    q~_p(l, x) [xsize][Pp][lmax+1] for the late x primordial Gamma."""
+    xvec = np.linspace(1000.0, 12000.0, xsize)
+    l = np.arange(lmax + 1.0)
+    p = np.arange(Pp)[:, None]
+    qt = np.stack([np.cos((p + 1) * x / 4000.0) * np.sin(0.1 * l * (1 + p) + x / 3000.0) / (1.0 + l) for x in xvec])
+    return xvec, qt
+
+
+def prim_workload(kmax_i, Pp):
+    """Primordial k-grid case: cosine basis on grid indices 0..kmax_i, all
+    p <= r <= s < Pp triples, one separable and one bump shape."""
+    x = np.arange(kmax_i + 1) / kmax_i
+    basis = np.stack([np.cos(np.pi * p * x) + 0.1 * p * x for p in range(Pp)], axis=1)
+    shapes = separable_shapes(kmax_i, 1, 3, 1, 2) + bump_shapes(1, 4)
+    for sh in shapes:  # index 0 unused with kmin = 1
+        if sh["kind"] == SHAPE_SEPARABLE:
+            sh["tab"][:, :, 0] = 0.0
+    return basis, mode_triples(Pp), shapes
+
+
 def bspline_matrix(lmin, lmax, nb=64, degree=3):
     """[L][nb] clamped uniform B-splines of the given degree on [lmin, lmax]
     (Cox-de Boor recursion; input builder for the basis-optimisation workload)."""

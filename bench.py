@@ -478,6 +478,24 @@ def run_next_rows(mg, local, with_cpu):
         row["cpu_sample"] = f"16 and 64 of {N} late modes (rows), fitted as a + b n (a: the per-x M tables); cores {cores}"
     out["transfer_gamma"] = row
 
+    # 3D transfer Gamma: calculate_gamma_TTT_3D_nested (calculate_gamma_3d.c:274-440)
+    lmax, P, Pp, xsize = 300, 12, 8, 32
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = mg.transfer_workload(lmax, Pp, xsize)
+    prim = mg.mode_triples(Pp)
+    N, Np = len(tr), len(prim)
+    with mg.Context(local) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        c.set_transfer(xvec, qt, prim)
+        row = {"workload": f"3D transfer Gamma, l=2..{lmax}, P={P} (N={N}), P_prim={Pp} (N_prim={Np}), {xsize} x points",
+               "gpu_ms": _dev_ms(c, lambda: c.gamma_transfer_3d(0.7))}
+    if orc is not None:
+        row["cpu_s"] = _fit_cpu(lambda n: orc.gamma_3d(2, lmax, q, tr, cl, xvec, qt, prim[:n], 0.7), 8, 32, Np, 1)
+        row["cpu_sample"] = f"8 and 32 of {Np} primordial modes, fitted as a + b n; cores {cores}"
+    out["transfer_gamma_3d"] = row
+
     # primordial k-space side: calculate_ortho (orthogonalisation.c:14-86) and calculate_eigen
     kmin, kmax_i, kmax, Pp = 1, 120, 0.5, 12
     basis, prim, shapes = mg.prim_workload(kmax_i, Pp)

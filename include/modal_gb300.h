@@ -217,6 +217,17 @@ modal_status modal_set_transfer(modal_ctx *ctx, int Pp, int xsize, const double 
  * from modal_set_spectrum and scale deltaphi^2/(8 pi).  FP64 on the GPU. */
 modal_status modal_gamma_transfer(modal_ctx *ctx, double deltaphi, double *gamma_t);
 
+/* The 3D transfer Gamma, gamma_mpi.c's rflag_do3D == 0 path: gamma_t[m][n] =
+ * 6 deltaphi^2 sum over the tetrapyd (l = 2..lmax) of permsix h~^2 prod
+ * (2l+1)^{-1/3} plijk_TTT(m, l1, l2, l3) s_n(l1, l2, l3), where s_n is the
+ * trapezium x-integral of calculate_sijk_TTT (calculate_gamma_TTT_3D_nested,
+ * calculate_gamma_3d.c:274-440, 783-860; init_gamma_3Dint :23-60), for every
+ * late mode m < N and primordial mode n < Nprim (the reference sizes the
+ * matrix by the primordial count and fills m < Nprim).  Inputs as for
+ * modal_gamma_transfer (modal_set_transfer, modal_set_spectrum).  FP64 on the
+ * GPU: each primordial mode is projected as one radial shape. */
+modal_status modal_gamma_transfer_3d(modal_ctx *ctx, double deltaphi, double *gamma_t);
+
 /* Eigenvalue floor of the PCA branch: keep the leading eigenvalues of the
  * normalised Gamma above floor * (largest eigenvalue).  0 (the default) is the
  * reference's rule, every positive eigenvalue (ortho_late_mpi.c:786-792).  At

@@ -184,6 +184,17 @@ struct DShape {
     long tab_off_f = 0;  // FP32 form: [parity of l][l / 2][term][f, g, h, 0] from this float offset
 };
 
+// Internal shape kind of the 3D transfer Gamma: the radial integral s_n(l1,l2,l3)
+// of primordial mode n = DShape::nterms (calculate_sijk_TTT), arguments below.
+constexpr int SHAPE_RADIAL = 2;
+struct RadialArgs {
+    const double *qt = nullptr;  // [xsize][Pp][L1] transfer functions q~_p(l, x)
+    const double *x = nullptr;   // [xsize] radial grid
+    const double *wq = nullptr;  // [L1] (2l+1)^{1/6}/sqrt(C_l + N_l/b_l^2), 0 for l < 2
+    const int *prim = nullptr;   // [Nprim][3] primordial triples
+    int xsize = 0, Pp = 0, L1 = 0;
+};
+
 // A planned projection: validated descriptors, buffer offsets, launch shape.
 struct ProjPlan {
     int S = 0;
@@ -194,6 +205,7 @@ struct ProjPlan {
     size_t smem = 0, o_q = 0, o_v = 0, o_t = 0, o_s = 0, o_F = 0, o_B = 0, o_c = 0, o_w = 0, o_sb = 0;
     long long npts = 0;  // tetrapyd points (FP32 weight table entries)
     long tabf_total = 0;  // floats of the FP32 separable tables
+    RadialArgs ra;        // radial shapes (3D transfer Gamma only)
     int max_nterms = 0;
 };
 // plan: validate, size every buffer, upload the slab schedule (may allocate);

@@ -44,8 +44,34 @@ __device__ __forceinline__ double d_geo(int l1, int l2, int l3)
     return p1 * p2 * p3;
 }
 
-__device__ __forceinline__ double d_shape(const DShape &s, const double *__restrict__ tab, int stride, int i, int j, int k)
+// s_n(i,j,k) / (wq_i wq_j wq_k) of calculate_sijk_TTT (calculate_gamma_3d.c:813-860):
+// the trapezium integral (integrate, :783-811) over x of x^2 (1/6) sum over the six
+// orderings of q~(i,a) q~(j,b) q~(k,c), with the reference's rule that drops any of
+// the first 10 samples above 1e-18 applied to the weighted sample.  The weights
+// wq come back through the projection's point weight.
+__device__ double d_radial(const RadialArgs &ra, int n, int i, int j, int k)
 {
+    const int a1 = ra.prim[3 * n], a2 = ra.prim[3 * n + 1], a3 = ra.prim[3 * n + 2], L1 = ra.L1;
+    const double wp = ra.wq[i] * ra.wq[j] * ra.wq[k];
+    double r = 0.0, yprev = 0.0;
+    for (int x = 0; x < ra.xsize; x++) {
+        const double *qx = ra.qt + (size_t)x * ra.Pp * L1;
+        const double *q1 = qx + (size_t)a1 * L1, *q2 = qx + (size_t)a2 * L1, *q3 = qx + (size_t)a3 * L1;
+        const double p1 = q1[i], p2 = q2[i], p3 = q3[i], p4 = q1[j], p5 = q2[j], p6 = q3[j], p7 = q1[k], p8 = q2[k],
+                     p9 = q3[k];
+        const double sum = p1 * p5 * p9 + p2 * p6 * p7 + p3 * p4 * p8 + p3 * p5 * p7 + p2 * p4 * p9 + p1 * p6 * p8;
+        double y = ra.x[x] * ra.x[x] * sum * (1.0 / 6.0);
+        if (x < 10 && fabs(wp * y) > 1e-18) y = 0.0;
+        if (x > 0) r += (ra.x[x] - ra.x[x - 1]) * (yprev + y) * 0.5;
+        yprev = y;
+    }
+    return r;
+}
+
+__device__ __forceinline__ double d_shape(const DShape &s, const double *__restrict__ tab, int stride, int i, int j, int k,
+                                          const RadialArgs &ra)
+{
+    if (s.kind == SHAPE_RADIAL) return d_radial(ra, s.nterms, i, j, k);
     if (s.kind == MODAL_SHAPE_SEPARABLE) {
         double acc = 0.0;
         for (int t = 0; t < s.nterms; t++) {
@@ -146,7 +172,7 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
                                                             const double *__restrict__ tab,
                                                             const double *__restrict__ Wd,
                                                             const long long *__restrict__ sbase,
-                                                            double *__restrict__ Fbuf)
+                                                            double *__restrict__ Fbuf, const RadialArgs ra)
 {
     extern __shared__ double sm[];
     double *f = sm;               // [JC][KMAX]
@@ -168,7 +194,7 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
                 if (j <= lmax) {
                     int k = j + par + 2 * kk, k1 = min(i + j, lmax);
                     if (k <= k1)
-                        val = Wd[sbase[slab] + tet_row_offset(i, j, lmax) + kk] * d_shape(sh, tab, stride, i, j, k);
+                        val = Wd[sbase[slab] + tet_row_offset(i, j, lmax) + kk] * d_shape(sh, tab, stride, i, j, k, ra);
                 }
                 f[e] = val;
             }
@@ -835,7 +861,7 @@ modal_status proj_record(modal_ctx *ctx, const ProjPlan &pl)
     auto run = [&](auto kern) -> modal_status {
         kern<<<L, 256, pl.smem, ctx->stream>>>(lmin, lmax, P, S, KMAX, ctx->slab_order.as<int>(), ctx->q.as<double>(),
                                                ctx->vl.as<double>(), ctx->shape_desc.as<DShape>(),
-                                               ctx->shape_tab.as<double>(), Wd, sbase, Fbuf);
+                                               ctx->shape_tab.as<double>(), Wd, sbase, Fbuf, pl.ra);
         return launched(ctx, "project_slab_fp64");
     };
     if (pl.fpt <= 1) MODAL_TRY(run(k_project_slab_fp64<1>));
@@ -857,4 +883,61 @@ modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal
     return proj_record(ctx, pl);
 }
 
+__global__ void k_wq(int lmax, const double *__restrict__ cl, double *__restrict__ wq)
+{
+    const int l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l > lmax) return;
+    wq[l] = (l < 2) ? 0.0 : pow(2.0 * l + 1.0, 1.0 / 6.0) * (1.0 / sqrt(cl[l]));
+}
+
 }  // namespace modal
+
+using namespace modal;
+
+extern "C" modal_status modal_gamma_transfer_3d(modal_ctx *c, double deltaphi, double *gamma_t)
+{
+    if (!c || !gamma_t) { set_error("modal_gamma_transfer_3d: NULL argument"); return MODAL_ERR_ARG; }
+    if (!c->have_modes || !c->have_spec || c->tr_xsize < 2) {
+        set_error("modal_gamma_transfer_3d: set basis, modes, spectrum and transfer functions first");
+        return MODAL_ERR_STATE;
+    }
+    if (c->lmin < 2) { set_error("modal_gamma_transfer_3d: lmin must be >= 2"); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    const int S = c->tr_Nprim, N = c->N, lmax = c->lmax;
+    // each primordial mode is one radial shape of the FP64 projection
+    std::vector<modal_shape> placeholder(S);
+    for (int s = 0; s < S; s++) {
+        placeholder[s] = modal_shape{};
+        placeholder[s].kind = MODAL_SHAPE_BUMP;
+        placeholder[s].sigma = 1.0;
+    }
+    ProjPlan pl;
+    MODAL_TRY(proj_plan(c, S, placeholder.data(), MODAL_PREC_FP64, pl));
+    for (int s = 0; s < S; s++) {
+        pl.desc[s].kind = SHAPE_RADIAL;
+        pl.desc[s].nterms = s;
+    }
+    MODAL_TRY(ensure(c->scratch2, sizeof(double) * (size_t)(lmax + 1)));
+    k_wq<<<ceil_div(lmax + 1, 256), 256, 0, c->stream>>>(lmax, c->cl.as<double>(), c->scratch2.as<double>());
+    MODAL_TRY(launched(c, "wq"));
+    pl.ra.qt = c->tr_qt.as<double>();
+    pl.ra.x = c->tr_x.as<double>();
+    pl.ra.wq = c->scratch2.as<double>();
+    pl.ra.prim = c->tr_prim.as<int>();
+    pl.ra.xsize = c->tr_xsize;
+    pl.ra.Pp = c->tr_Pp;
+    pl.ra.L1 = lmax + 1;
+    {
+        StageTimer t(c, MODAL_T_GAMMA);
+        MODAL_TRY(proj_stage(c, pl, placeholder.data()));
+        MODAL_TRY(proj_record(c, pl));
+    }
+    std::vector<double> b((size_t)S * N);
+    MODAL_CUDA(cudaMemcpyAsync(b.data(), c->beta.ptr, sizeof(double) * b.size(), cudaMemcpyDeviceToHost, c->stream));
+    MODAL_CUDA(cudaStreamSynchronize(c->stream));
+    c->have_beta = false;  // the device beta holds these radial projections, not shapes'
+    const double f = 6.0 * deltaphi * deltaphi;  // calculate_gamma_3d.c:434-439
+    for (int m = 0; m < N; m++)
+        for (int n = 0; n < S; n++) gamma_t[(size_t)m * S + n] = f * b[(size_t)n * N + m];
+    return MODAL_OK;
+}

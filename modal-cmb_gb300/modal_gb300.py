@@ -31,7 +31,7 @@ EXPORTS = [
     "modal_get_mij", "modal_get_gl", "modal_gamma", "modal_gamma_partial", "modal_orthol_pair", "modal_orthogonalise",
     "modal_set_spectrum", "modal_project", "modal_alpha", "modal_ctx_profile", "modal_ctx_timer",
     "modal_ctx_timer_reset", "modal_gamma_fp64_noalloc", "modal_modify_bispectrum", "modal_calculate_modes",
-    "modal_set_transfer", "modal_gamma_transfer", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
+    "modal_set_transfer", "modal_gamma_transfer", "modal_gamma_transfer_3d", "modal_project_gl", "modal_gamma_vjp", "modal_project_gl_vjp",
     "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
     "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol", "modal_set_transfer_pol",
@@ -102,6 +102,7 @@ def lib():
             "modal_calculate_modes": (i, [vp, i, vp, vp]),
             "modal_set_transfer": (i, [vp, i, i, vp, vp, i, vp]),
             "modal_gamma_transfer": (i, [vp, d, vp]),
+            "modal_gamma_transfer_3d": (i, [vp, d, vp]),
             "modal_project_gl": (i, [vp, i, vp, vp, vp]),
             "modal_gamma_vjp": (i, [vp, vp, vp]),
             "modal_project_gl_vjp": (i, [vp, i, vp, vp, vp]),
@@ -386,6 +387,12 @@ class Context:
     def gamma_transfer(self, deltaphi):
         out = np.empty((self.N, self.Nprim))
         _check(lib().modal_gamma_transfer(self.h, float(deltaphi), _ptr(out)))
+        return out
+
+    def gamma_transfer_3d(self, deltaphi):
+        """[N][Nprim] 3D transfer Gamma (tetrapyd sum of the radial integrals)."""
+        out = np.empty((self.N, self.Nprim))
+        _check(lib().modal_gamma_transfer_3d(self.h, float(deltaphi), _ptr(out)))
         return out
 
     def set_transfer_pol(self, qtilde_e, spec9, fsky_t, fsky_e):

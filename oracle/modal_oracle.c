@@ -945,3 +945,72 @@ int orc_prim_eigen(int min, int max, double kmax, int P, const double *basis, in
     free(pts);
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* 3D transfer Gamma (calculate_gamma_3d.c): calculate_gamma_TTT_3D_nested    */
+/* (:274-440) over the tetrapyd of gamma_3d_host (gamma_mpi.c:30-152) with    */
+/* the point set of decompose_gamma_TTT_3D_mpi (:92-211):                     */
+/*   Gamma[m][n] = 6 dphi^2 sum_pts z plijk_m(i,j,k) s_n(i,j,k),              */
+/*   z = permsix h~^2 prod (2l+1)^{-1/3} (lweight3D, init_gamma_3Dint :23-44),*/
+/*   s_n = trapezium over x of x^2 (1/6) sum_perms q3(i,a1) q3(j,a2) q3(k,a3) */
+/*   (calculate_sijk_TTT :813-860, integrate :783-811), the first 10 samples  */
+/*   dropped where |y| > 1e-18; q3(l,a,x) = (2l+1)^{1/6}/sqrt(cl[l]) q~_a(l,x)*/
+/*   for l > 1 (init_gamma_3Dint :46-60).  Points i = 2..lmax, j = i..lmax,   */
+/*   k = j + (i % 2) .. min(i + j, lmax) step 2.  out[N][Nprim].             */
+/* ------------------------------------------------------------------------ */
+int orc_gamma_3d(int lmin, int lmax, int P, const double *basis, int N, const int *triples, const double *cl, int xsize,
+                 const double *xvec, int Pp, const double *qt, int Nprim, const int *prim, double dphi, double *out)
+{
+    const int L1 = lmax + 1;
+    double *lw = malloc(sizeof(double) * L1), *wq = malloc(sizeof(double) * L1);
+    for (int l = 0; l <= lmax; l++) {
+        lw[l] = l > 1 ? 1e0 / pow(2e0 * l + 1e0, 1e0 / 3e0) : 0e0;
+        wq[l] = l > 1 ? pow(2e0 * l + 1e0, 1e0 / 6e0) * (1e0 / sqrt(cl[l])) : 0e0;
+    }
+    const int nth = omp_get_max_threads();
+    double *acc = calloc((size_t)nth * N * Nprim, sizeof(double));
+    #pragma omp parallel
+    {
+        const int t = omp_get_thread_num();
+        double *g = acc + (size_t)t * N * Nprim;
+        double *y = malloc(sizeof(double) * xsize), *s = malloc(sizeof(double) * Nprim), *Q = malloc(sizeof(double) * N);
+        #pragma omp for schedule(dynamic, 1)
+        for (int i = 2; i <= lmax; i++)
+            for (int j = i; j <= lmax; j++)
+                for (int k = j + (i % 2); k <= (i + j < lmax ? i + j : lmax); k += 2) {
+                    const double z = orc_permsix(i, j, k) * orc_geometric(i, j, k) * lw[i] * lw[j] * lw[k];
+                    for (int n = 0; n < Nprim; n++) {
+                        const int a1 = prim[3 * n], a2 = prim[3 * n + 1], a3 = prim[3 * n + 2];
+                        for (int x = 0; x < xsize; x++) {
+                            const double *qx = qt + (size_t)x * Pp * L1;
+                            const double p1 = wq[i] * qx[(size_t)a1 * L1 + i], p2 = wq[i] * qx[(size_t)a2 * L1 + i],
+                                         p3 = wq[i] * qx[(size_t)a3 * L1 + i];
+                            const double p4 = wq[j] * qx[(size_t)a1 * L1 + j], p5 = wq[j] * qx[(size_t)a2 * L1 + j],
+                                         p6 = wq[j] * qx[(size_t)a3 * L1 + j];
+                            const double p7 = wq[k] * qx[(size_t)a1 * L1 + k], p8 = wq[k] * qx[(size_t)a2 * L1 + k],
+                                         p9 = wq[k] * qx[(size_t)a3 * L1 + k];
+                            const double sum = p1 * p5 * p9 + p2 * p6 * p7 + p3 * p4 * p8 + p3 * p5 * p7 + p2 * p4 * p9 +
+                                               p1 * p6 * p8;
+                            double v = xvec[x] * xvec[x] * sum * (1e0 / 6e0);
+                            if (x < 10 && fabs(v) > 1e-18) v = 0e0;
+                            y[x] = v;
+                        }
+                        double r = 0e0;
+                        for (int x = 0; x < xsize - 1; x++) r += (xvec[x + 1] - xvec[x]) * (y[x] + y[x + 1]) * 0.5;
+                        s[n] = r;
+                    }
+                    for (int m = 0; m < N; m++) Q[m] = plijk(basis, P, triples + 3 * m, lmin, lmax, i, j, k) * z;
+                    for (int m = 0; m < N; m++)
+                        for (int n = 0; n < Nprim; n++) g[(size_t)m * Nprim + n] += Q[m] * s[n];
+                }
+        free(y); free(s); free(Q);
+    }
+    const double f = 6e0 * dphi * dphi;
+    for (size_t e = 0; e < (size_t)N * Nprim; e++) {
+        double v = 0e0;
+        for (int t = 0; t < nth; t++) v += acc[(size_t)t * N * Nprim + e];
+        out[e] = v * f;
+    }
+    free(acc); free(lw); free(wq);
+    return 0;
+}

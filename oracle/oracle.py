@@ -96,6 +96,7 @@ class Oracle:
             ("orc_calculate_modes", i, [i, i, i, vp, i, vp, i, vp, vp]),
             ("orc_integrate_cubic_spline", d, [vp, vp, i]),
             ("orc_gamma_transfer", i, [i, i, i, vp, i, vp, vp, i, vp, vp, i, vp, i, vp, i, vp, d, vp]),
+            ("orc_gamma_3d", i, [i, i, i, vp, i, vp, vp, i, vp, i, vp, i, vp, d, vp]),
             ("orc_gamma_pol", i, [i, vp, vp, vp, i, i, i, vp, vp, vp, vp, vp, vp]),
             ("orc_gamma_transfer_pol", i, [i, i, i, vp, i, i, i, vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                            vp, vp, d, d, i, vp, vp, i, vp, i, vp, vp, i, vp, d, vp]),
@@ -216,6 +217,16 @@ class Oracle:
                                   qt.shape[1], _p(qt), Nprim, _p(prim), float(dphi), _p(out))
         return out
 
+    def gamma_3d(self, lmin, lmax, q, triples, cl, xvec, qt, prim, dphi):
+        """[N][Nprim]: calculate_gamma_TTT_3D_nested's 3D transfer Gamma (any N, Nprim)."""
+        q, cl, xvec, qt = (np.ascontiguousarray(a, dtype=np.float64) for a in (q, cl, xvec, qt))
+        triples, prim = (np.ascontiguousarray(a, dtype=np.int32) for a in (triples, prim))
+        N, Nprim = triples.shape[0], prim.shape[0]
+        out = np.empty((N, Nprim))
+        self.L.orc_gamma_3d(lmin, lmax, q.shape[1], _p(q), N, _p(triples), _p(cl), xvec.size, _p(xvec), qt.shape[1],
+                            _p(qt), Nprim, _p(prim), float(dphi), _p(out))
+        return out
+
     def gamma_pol(self, MT, ME, w, tte, tee, eee):
         """(Gamma_TTE, Gamma_TEE, Gamma_EEE) from Mij_T / Mij_E [P][P][nmu]."""
         MT, ME = np.ascontiguousarray(MT), np.ascontiguousarray(ME)
@@ -334,6 +345,7 @@ class Ref:
             ("ref_modify_bispectrum", i, [i, vp, vp]),
             ("ref_calculate_modes", i, [i, vp, vp]),
             ("ref_gamma_transfer", i, [i, vp, i, vp, i, vp, d, vp]),
+            ("ref_gamma_3d", i, [i, vp, i, vp, i, vp, d, vp]),
             ("ref_setup_pol", i, [i, i, i, vp, vp, vp, vp]),
             ("ref_gamma_pol", i, [vp]),
             ("ref_setup_pol_spectra", i, [i, vp, d, d]),
@@ -374,6 +386,17 @@ class Ref:
         t = [np.ascontiguousarray(x, dtype=np.int32) for x in (tte, tee, eee)]
         self._keep_pol = (qE, t)
         self.L.ref_setup_pol(lminE, lmaxE, qE.shape[1], _p(qE), _p(t[0]), _p(t[1]), _p(t[2]))
+
+    def gamma_3d(self, xvec, qt, prim, dphi):
+        """[N][N]: calculate_gamma_TTT_3D_nested through gamma_3d_host's set-up on one
+        thread (primordial and late term counts equal, as the reference sizes it)."""
+        xvec, qt = (np.ascontiguousarray(a, dtype=np.float64) for a in (xvec, qt))
+        prim = np.ascontiguousarray(prim, dtype=np.int32)
+        out = np.zeros((self.N, self.N))
+        r = self.L.ref_gamma_3d(xvec.size, _p(xvec), qt.shape[1], _p(qt), prim.shape[0], _p(prim), float(dphi), _p(out))
+        if r != 0:
+            raise ValueError("ref_gamma_3d: the primordial term count must equal the late one")
+        return out
 
     def gamma_transfer_pol(self, spec9, fsky_t, fsky_e, xvec, qtT, qtE, prim, dphi):
         """[4][N][Nprim]: calculate_gamma_2d's TTT, TTE, TEE, EEE with polarisation."""

@@ -9,4 +9,6 @@
 #include <alloca.h>
 void *_mm_malloc(size_t size, size_t align);
 void _mm_free(void *p);
+/* Intel offload placement attribute (local_barrier.c/.h): no meaning here */
+#define __declspec(x)
 #endif

@@ -561,3 +561,85 @@ int ref_prim_eigen(int min, int max, double kmax, int P, const double *basis, in
     omp_set_num_threads(nt);
     return 0;
 }
+
+/* ---- the 3D transfer Gamma (calculate_gamma_3d.c) ---------------------- */
+#include "mkl.h"
+#include "calculate_gamma_3d.h"
+
+/* the qtilde l grid is l = 0..lmax (dense) */
+int get_qtilde_T_lsize(void) { return eflag_T_lmax + 1; }
+int get_qtilde_E_lsize(void) { return eflag_T_lmax + 1; }
+int get_qtilde_T_lvec(int *v) { for (int l = 0; l <= eflag_T_lmax; l++) v[l] = l; return 0; }
+int get_qtilde_E_lvec(int *v) { for (int l = 0; l <= eflag_T_lmax; l++) v[l] = l; return 0; }
+double *get_basis_late_T_flat(void) { return g_basis; }
+
+/* CBLAS dgemm semantics (row major), plain loops: C = alpha op(A) op(B) + beta C */
+void cblas_dgemm(CBLAS_LAYOUT layout, CBLAS_TRANSPOSE ta, CBLAS_TRANSPOSE tb, int M, int N, int K, double alpha,
+                 const double *A, int lda, const double *B, int ldb, double beta, double *C, int ldc)
+{
+    if (layout != CblasRowMajor) abort();
+    for (int m = 0; m < M; m++)
+        for (int n = 0; n < N; n++) {
+            double s = 0.0;
+            for (int k = 0; k < K; k++) {
+                const double a = ta == CblasNoTrans ? A[(long)m * lda + k] : A[(long)k * lda + m];
+                const double b = tb == CblasNoTrans ? B[(long)k * ldb + n] : B[(long)n * ldb + k];
+                s += a * b;
+            }
+            C[(long)m * ldc + n] = alpha * s + beta * C[(long)m * ldc + n];
+        }
+}
+
+extern void init_gamma_3Dint(void);
+
+/* The reference's per-core barrier (local_barrier.c) synchronises the hardware
+ * threads of one core; the glue runs one thread per core, for which the barrier
+ * only flips its sense. */
+void userCoreBarrier(barrier_t *bar) { bar->usersense = 1 - bar->usersense; }
+
+/* gamma_3d_host (gamma_mpi.c:30-152) on one thread: init_gamma_3Dint, the
+ * domain decomposition for one rank, calculate_gamma_TTT_3D_nested, and the
+ * result [N][N] (the reference sizes it by the primordial term count, which
+ * this glue ties to the late one: Nprim must equal N). */
+int ref_gamma_3d(int xsize, const double *xvec, int Pp, const double *qt, int Nprim, const int *prim, double dphi,
+                 double *out)
+{
+    if (Nprim != g_N) return -1;
+    g_xsize = xsize; g_Pp = Pp; g_Nprim = Nprim; deltaphi = dphi;
+    g_xvec = malloc(sizeof(double) * (size_t)xsize);
+    memcpy(g_xvec, xvec, sizeof(double) * (size_t)xsize);
+    size_t nq = (size_t)xsize * Pp * (eflag_T_lmax + 1);
+    g_qt = malloc(sizeof(double) * nq);
+    memcpy(g_qt, qt, sizeof(double) * nq);
+    g_prim = malloc(sizeof(int) * 3 * (size_t)Nprim);
+    memcpy(g_prim, prim, sizeof(int) * 3 * (size_t)Nprim);
+    init_gamma_3Dint();
+    const int N = g_N, Npad = (N + 7) & ~7, xpad = (xsize + 7) & ~7;
+    double *xdiff = calloc((size_t)xsize, sizeof(double)), *ixdiff = calloc((size_t)xsize, sizeof(double));
+    for (int i = 0; i < xsize - 1; i++) { xdiff[i] = g_xvec[i + 1] - g_xvec[i]; ixdiff[i] = 1.0 / xdiff[i]; }
+    corebarrier_t cb = {0};
+    barrier_t bar = {1, 0, 1, &cb};
+    thread_g3d_data_t td;
+    memset(&td, 0, sizeof td);
+    td.mvec = calloc((size_t)Npad * Npad, sizeof(double));
+    td.intgrlvec = calloc((size_t)MAXBLOCKSIZE * Npad, sizeof(double));
+    td.plijkz = calloc((size_t)MAXBLOCKSIZE * Npad, sizeof(double));
+    td.yvec = calloc((size_t)xpad, sizeof(double));
+    td.xsize = xsize;
+    td.xvec = g_xvec;
+    td.xdiff = xdiff;
+    td.ixdiff = ixdiff;
+    td.bar = &bar;
+    omp_set_num_threads(1);
+    #pragma omp parallel num_threads(1)
+    {
+        decompose_gamma_TTT_3D_mpi(&td, 0, 1, 0.0);
+        calculate_gamma_TTT_3D_nested(&td, MAXBLOCKSIZE);
+    }
+    for (int m = 0; m < N; m++)
+        for (int n = 0; n < N; n++) out[(long)m * N + n] = td.mvec[(long)m * Npad + n];
+    free(td.mvec); free(td.intgrlvec); free(td.plijkz); free(td.yvec); free(xdiff); free(ixdiff);
+    free(g_xvec); g_xvec = &g_x0; g_xsize = 1; g_Pp = 1;
+    free(g_qt); g_qt = NULL; free(g_prim); g_prim = NULL;
+    return 0;
+}

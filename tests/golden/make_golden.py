@@ -230,6 +230,22 @@ def pol_golden():
     print("gamma_pol done", G.shape)
 
 
+def gamma_3d_golden():
+    """12. 3D transfer Gamma: calculate_gamma_TTT_3D_nested through gamma_3d_host's
+    set-up (reference in place), late and primordial term counts equal."""
+    ref = O.Ref()
+    out = {}
+    for name, (lmax, P, Pp, xsize, dphi) in {"a": (40, 3, 3, 30, 0.7), "b": (63, 4, 4, 37, 1.3)}.items():
+        q, tr, cl = M.workload(lmax, P)
+        xvec, qt = transfer_inputs(lmax, Pp, xsize)
+        ref.setup(2, lmax, q, tr, cl)
+        out["gamma_" + name] = ref.gamma_3d(xvec, qt, M.mode_triples(Pp), dphi)
+        out["dims_" + name] = np.array([lmax, P, Pp, xsize])
+        out["dphi_" + name] = np.array([dphi])
+    np.savez_compressed(os.path.join(OUT, "gamma_3d.npz"), **out)
+    print("gamma_3d done")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["prune"]:
         prune_golden()
@@ -238,9 +254,12 @@ if __name__ == "__main__":
         pol_transfer_golden()
     elif sys.argv[1:] == ["prim"]:
         prim_golden()
+    elif sys.argv[1:] == ["g3d"]:
+        gamma_3d_golden()
     else:
         main()
         prune_golden()
         pol_golden()
         pol_transfer_golden()
         prim_golden()
+        gamma_3d_golden()

@@ -65,6 +65,7 @@ def test_argument_errors_without_gpu(built_lib, mg):
     assert L.modal_prim_points(5, 2, None, None) == 1
     assert L.modal_prim_ortho(None, 1, 10, 1.0, 3, None, 1, None, None) == 1
     assert L.modal_gamma_partial(None, 0, 0, 1, None) == 1
+    assert L.modal_gamma_transfer_3d(None, 1.0, None) == 1
 
 
 def test_tetrapyd_count_host_logic(built_lib, mg, orc):

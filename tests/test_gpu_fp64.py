@@ -398,6 +398,42 @@ def test_transfer_gamma_vs_reference(mg, golden, name):
     assert rel_max(G, g["gamma_" + name]) <= tol
 
 
+@pytest.mark.parametrize("name", ["a", "b"])
+def test_transfer_gamma_3d_vs_reference(mg, golden, name):
+    """calculate_gamma_TTT_3D_nested (gamma_mpi.c's rflag_do3D == 0 path) on the GPU
+    vs the in-place reference: 1e-12."""
+    g = golden("gamma_3d")
+    lmax, P, Pp, xsize = (int(v) for v in g["dims_" + name])
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = mg.transfer_workload(lmax, Pp, xsize)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        c.set_transfer(xvec, qt, mg.mode_triples(Pp))
+        G = c.gamma_transfer_3d(float(g["dphi_" + name][0]))
+    assert rel_max(G, g["gamma_" + name]) <= 1e-12
+
+
+def test_transfer_gamma_3d_vs_oracle_rectangular(mg, orc):
+    """N late modes != N_prim primordial modes, odd sizes, repeat call identical."""
+    lmax, P, Pp, xsize = 90, 5, 3, 41
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = mg.transfer_workload(lmax, Pp, xsize)
+    prim = mg.mode_triples(Pp)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        c.set_transfer(xvec, qt, prim)
+        G = c.gamma_transfer_3d(0.9)
+        G2 = c.gamma_transfer_3d(0.9)
+    Go = orc.gamma_3d(2, lmax, q, tr, cl, xvec, qt, prim, 0.9)
+    assert G.shape == (len(tr), len(prim))
+    assert rel_max(G, Go) <= 1e-12
+    assert np.array_equal(G, G2)
+
+
 def test_transfer_gamma_vs_oracle_wider(mg, orc):
     """Tile edges: N and Nprim not multiples of 32, Pp != P."""
     lmax, P, Pp, xsize = 120, 5, 6, 37

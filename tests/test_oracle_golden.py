@@ -198,6 +198,18 @@ def _transfer_inputs(lmax, Pp, xsize):
 
 
 @pytest.mark.parametrize("name", ["a", "b"])
+def test_gamma_3d_matches_reference(orc, golden, mg, name):
+    """calculate_gamma_TTT_3D_nested (the rflag_do3D == 0 path of gamma_mpi.c) vs the
+    in-place reference: the tetrapyd sum with the radial trapezium integrals."""
+    g = golden("gamma_3d")
+    lmax, P, Pp, xsize = (int(v) for v in g["dims_" + name])
+    q, tr, cl = mg.workload(lmax, P)
+    xvec, qt = mg.transfer_workload(lmax, Pp, xsize)
+    G = orc.gamma_3d(2, lmax, q, tr, cl, xvec, qt, mg.mode_triples(Pp), float(g["dphi_" + name][0]))
+    assert rel_max(G, g["gamma_" + name]) <= 1e-13
+
+
+@pytest.mark.parametrize("name", ["a", "b"])
 def test_transfer_gamma_matches_reference(orc, golden, mg, name):
     """calculate_gamma_2d path of calculate_gamma.c vs the in-place reference."""
     g = golden("gamma_transfer")

@@ -228,6 +228,14 @@ modal_status modal_gamma_transfer(modal_ctx *ctx, double deltaphi, double *gamma
  * GPU: each primordial mode is projected as one radial shape. */
 modal_status modal_gamma_transfer_3d(modal_ctx *ctx, double deltaphi, double *gamma_t);
 
+/* Load an orthogonalisation computed elsewhere, as eigenmodetoday_mpi.c reads
+ * it from the orthol_TTT / lambdal_TTT files (read_orthol / read_lambdal,
+ * fixed_data.c:3453-3469, 3749-3788): orthol and lambdal host [N][N]
+ * row-major.  modal_alpha then forms alpha = lambdal^T lambdal beta and
+ * modesR from the lower triangle of orthol (eigenmodetoday_mpi.c:148-162,
+ * 303-316), as after modal_orthogonalise.  Needs the modes (N). */
+modal_status modal_set_ortho(modal_ctx *ctx, const double *orthol, const double *lambdal);
+
 /* Eigenvalue floor of the PCA branch: keep the leading eigenvalues of the
  * normalised Gamma above floor * (largest eigenvalue).  0 (the default) is the
  * reference's rule, every positive eigenvalue (ortho_late_mpi.c:786-792).  At

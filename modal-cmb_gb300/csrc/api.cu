@@ -505,6 +505,22 @@ modal_status modal_orthogonalise(modal_ctx *c, const double *gamma, int pca_flag
     return MODAL_OK;
 }
 
+modal_status modal_set_ortho(modal_ctx *c, const double *orthol, const double *lambdal)
+{
+    MODAL_TRY(need(c, c && c->have_modes, "modal_set_ortho: set the modes (N) first"));
+    if (!orthol || !lambdal) { set_error("modal_set_ortho: orthol and lambdal are required"); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    const size_t NN = (size_t)c->N * c->N;
+    c->have_ortho = false;
+    MODAL_TRY(h2d(c, c->orthol, orthol, sizeof(double) * NN));
+    MODAL_TRY(h2d(c, c->lambdal, lambdal, sizeof(double) * NN));
+    MODAL_TRY(lambdainv_dev(c));
+    c->ortho_branch = 2;  // caller-supplied: modesR takes the lower triangle
+    c->ortho_rank = c->N;
+    c->have_ortho = true;
+    return sync(c);
+}
+
 modal_status modal_set_pca_floor(modal_ctx *c, double floor)
 {
     if (!c || !(floor >= 0.0 && floor < 1.0)) { set_error("modal_set_pca_floor: floor must be in [0, 1)"); return MODAL_ERR_ARG; }

@@ -168,6 +168,7 @@ modal_status gamma_split_dev(modal_ctx *ctx, int mu0, int nmu);
 modal_status ortho_dev(modal_ctx *ctx, int pca_flag);
 modal_status project_dev(modal_ctx *ctx, int S, const modal_shape *shapes, modal_prec prec);
 modal_status alpha_dev(modal_ctx *ctx, int S);
+modal_status lambdainv_dev(modal_ctx *ctx);  // linv = lower triangle of orthol
 modal_status transpose_dev(modal_ctx *ctx, const double *in, double *out, int R, int C);
 modal_status basis_legendre_dev(modal_ctx *ctx, int size, int pmax, double min, double max, const double *d_values,
                                 double *d_out);

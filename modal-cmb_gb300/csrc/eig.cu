@@ -28,9 +28,11 @@ __global__ void k_pca_rank(int meig, const double *__restrict__ W, double floor,
 }
 
 // V_rm: row-major buffer whose row a < meig holds the eigenvector of ascending index a.
+// lambdainv: the lower triangle of orthol (zero above the diagonal), the matrix
+// eigenmodetoday_mpi.c:148-160 builds from the orthol file for modesR.
 __global__ void k_pca_outputs(int N, int meig, const double *__restrict__ V_rm, const double *__restrict__ W,
                               const double *__restrict__ norm, const int *__restrict__ rank,
-                              double *__restrict__ orthol, double *__restrict__ lambdal)
+                              double *__restrict__ orthol, double *__restrict__ lambdal, double *__restrict__ lambdainv)
 {
     size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= (size_t)N * N) return;
@@ -49,6 +51,7 @@ __global__ void k_pca_outputs(int N, int meig, const double *__restrict__ V_rm, 
     }
     lambdal[e] = lam;
     orthol[e] = inv;
+    lambdainv[e] = (i >= j) ? inv : 0.0;
 }
 
 // One cuSOLVER handle per context, bound to the context's stream.  Creating a
@@ -114,8 +117,10 @@ modal_status eig_pca_dev(modal_ctx *ctx)
     k_pca_rank<<<1, 1, 0, ctx->stream>>>(meig, W, ctx->pca_floor, rank);
     MODAL_TRY(launched(ctx, "pca_rank"));
     size_t NN = (size_t)N * N;
+    MODAL_TRY(ensure(ctx->linv, sizeof(double) * NN));
     k_pca_outputs<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(N, meig, A, W, ctx->norm.as<double>(), rank,
-                                                                       ctx->orthol.as<double>(), ctx->lambdal.as<double>());
+                                                                       ctx->orthol.as<double>(), ctx->lambdal.as<double>(),
+                                                                       ctx->linv.as<double>());
     MODAL_TRY(launched(ctx, "pca_outputs"));
     int hr = 0;
     MODAL_CUDA(cudaMemcpyAsync(&hr, rank, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

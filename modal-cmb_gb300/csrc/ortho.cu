@@ -541,8 +541,28 @@ modal_status ortho_dev(modal_ctx *ctx, int pca_flag)
 
 // --------------------------------------------------------------------------
 // Alpha solve for S shapes: y = beta lambdal^T, alpha = y lambdal,
-// modesR = alpha lambdainv with lambdainv = orthol (rows j, cols i).
+// modesR = alpha lambdainv, where lambdainv is the lower triangle of orthol
+// (eigenmodetoday_mpi.c:148-160, 303-316): orthol itself on the Cholesky
+// branch, the copy in linv otherwise (k_pca_outputs, or lambdainv_dev for an
+// orthogonalisation loaded by modal_set_ortho).
 // --------------------------------------------------------------------------
+__global__ void k_lower_triangle(int N, const double *__restrict__ a, double *__restrict__ t)
+{
+    size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)N * N) return;
+    int i = (int)(e / N), j = (int)(e % N);
+    t[e] = (i >= j) ? a[e] : 0.0;
+}
+
+modal_status lambdainv_dev(modal_ctx *ctx)
+{
+    const size_t NN = (size_t)ctx->N * ctx->N;
+    MODAL_TRY(ensure(ctx->linv, sizeof(double) * NN));
+    k_lower_triangle<<<ceil_div((long)NN, 256), 256, 0, ctx->stream>>>(ctx->N, ctx->orthol.as<double>(),
+                                                                        ctx->linv.as<double>());
+    return launched(ctx, "lower_triangle");
+}
+
 modal_status alpha_dev(modal_ctx *ctx, int S)
 {
     const int N = ctx->N;
@@ -553,8 +573,9 @@ modal_status alpha_dev(modal_ctx *ctx, int S)
     const double *lam = ctx->lambdal.as<double>();
     MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->beta.as<double>(), N, lam, N, true, y, N, false));
     MODAL_TRY(dgemm_rows(ctx, S, N, N, y, N, lam, N, false, ctx->alpha.as<double>(), N, false));
-    MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->alpha.as<double>(), N, ctx->orthol.as<double>(), N, false,
-                         ctx->modesr.as<double>(), N, false));
+    const double *lambdainv = ctx->ortho_branch == 0 ? ctx->orthol.as<double>() : ctx->linv.as<double>();
+    MODAL_TRY(dgemm_rows(ctx, S, N, N, ctx->alpha.as<double>(), N, lambdainv, N, false, ctx->modesr.as<double>(), N,
+                         false));
     return MODAL_OK;
 }
 

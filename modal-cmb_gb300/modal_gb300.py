@@ -35,7 +35,7 @@ EXPORTS = [
     "modal_alpha_gl", "modal_adjoint_residual", "modal_basis_prune", "modal_lambda_min",
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
     "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol", "modal_set_transfer_pol",
-    "modal_gamma_transfer_pol", "modal_prim_points", "modal_prim_ortho", "modal_prim_eigen",
+    "modal_gamma_transfer_pol", "modal_prim_points", "modal_prim_ortho", "modal_prim_eigen", "modal_set_ortho",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
@@ -103,6 +103,7 @@ def lib():
             "modal_set_transfer": (i, [vp, i, i, vp, vp, i, vp]),
             "modal_gamma_transfer": (i, [vp, d, vp]),
             "modal_gamma_transfer_3d": (i, [vp, d, vp]),
+            "modal_set_ortho": (i, [vp, vp, vp]),
             "modal_project_gl": (i, [vp, i, vp, vp, vp]),
             "modal_gamma_vjp": (i, [vp, vp, vp]),
             "modal_project_gl_vjp": (i, [vp, i, vp, vp, vp]),
@@ -496,6 +497,12 @@ class Context:
         out = np.empty((self.lmax - self.lmin + 1, self.P)) if grad else None
         _check(lib().modal_lambda_min(self.h, ctypes.byref(lam), _ptr(v), _ptr(out)))
         return lam.value, v, out
+
+    def set_ortho(self, orthol, lambdal):
+        """Load orthol/lambdal [N][N] (e.g. read from the orthol/lambdal files) for alpha."""
+        o, lam = _f64(orthol), _f64(lambdal)
+        assert o.shape == lam.shape == (self.N, self.N)
+        _check(lib().modal_set_ortho(self.h, _ptr(o), _ptr(lam)))
 
     def alpha(self, S, beta=None, download=True):
         b = None if beta is None else _f64(beta)

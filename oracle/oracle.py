@@ -334,6 +334,7 @@ class Ref:
             ("ref_asy", i, [i, vp, vp]),
             ("ref_legendre_Pl", d, [i, d]),
             ("ref_basis_legendre", i, [i, i, d, d, vp, vp]),
+            ("ref_basis_family", i, [i, i, i, d, d, vp, vp]),
             ("ref_init_gamma", i, []),
             ("ref_orthol_pair", i, [i, i, vp]),
             ("ref_gamma", l, [i, l, vp]),
@@ -375,6 +376,14 @@ class Ref:
         values = np.ascontiguousarray(values, dtype=np.float64)
         out = np.empty((values.size, pmax + 1))
         self.L.ref_basis_legendre(values.size, pmax, float(vmin), float(vmax), _p(values), _p(out))
+        return out
+
+    def basis_family(self, kind, values, pmax, vmin, vmax):
+        """basis_functions_{legendre, fourier, sinlog, bi} for kind 0..3."""
+        values = np.ascontiguousarray(values, dtype=np.float64)
+        out = np.empty((values.size, pmax + 1))
+        if self.L.ref_basis_family(kind, values.size, pmax, float(vmin), float(vmax), _p(values), _p(out)) != 0:
+            raise ValueError(f"basis family {kind} with pmax {pmax}")
         return out
 
     def init_gamma(self):

@@ -217,6 +217,25 @@ int ref_basis_legendre(int size, int pmax, double min, double max, const double 
     return 0;
 }
 
+extern int basis_functions_fourier(double **array, int size, int pmax, double min, double max, double *values);
+extern int basis_functions_sinlog(double **array, int size, int pmax, double min, double max, double *values);
+extern int basis_functions_bi(double **array, int size, int pmax, double min, double max, double *values);
+
+/* One of the basis families of basis_functions.c: 0 legendre, 1 fourier,
+ * 2 sinlog, 3 bi (pmax <= 30). */
+int ref_basis_family(int kind, int size, int pmax, double min, double max, const double *values, double *out)
+{
+    if (kind < 0 || kind > 3 || (kind == 3 && pmax > 30)) return 1;
+    double **a = create_array(size, pmax + 1);
+    if (kind == 0) basis_functions_legendre(a, size, pmax, min, max, (double *)values);
+    if (kind == 1) basis_functions_fourier(a, size, pmax, min, max, (double *)values);
+    if (kind == 2) basis_functions_sinlog(a, size, pmax, min, max, (double *)values);
+    if (kind == 3) basis_functions_bi(a, size, pmax, min, max, (double *)values);
+    for (int i = 0; i < size; i++) memcpy(out + (long)i * (pmax + 1), a[i], sizeof(double) * (pmax + 1));
+    free(a[0]); free(a);
+    return 0;
+}
+
 /* init_orthol_glint + calculate_orthoMij_T over all P^2 (i,j) pairs + sync,
  * the sequence of ortho_late_mpi.c:170-229 on one rank. */
 int ref_init_gamma(void)

@@ -246,6 +246,21 @@ def gamma_3d_golden():
     print("gamma_3d done")
 
 
+def basis_families_golden():
+    """13. basis_functions.c's families (legendre, fourier, sinlog, bi) on
+    l = 2..700 and on a grid that starts at 0 (sinlog's small-value branch)."""
+    ref = O.Ref()
+    out = {}
+    for name, (lo, hi, pmax) in {"a": (2, 700, 30), "b": (0, 120, 9)}.items():
+        v = np.arange(lo, hi + 1, dtype=np.float64)
+        vmin = max(lo, 1e-3) if name == "b" else lo  # sinlog takes log(v/min)
+        for kind, fam in enumerate(("legendre", "fourier", "sinlog", "bi")):
+            out[f"{fam}_{name}"] = ref.basis_family(kind, v, pmax, vmin, hi)
+        out["dims_" + name] = np.array([lo, hi, pmax, vmin])
+    np.savez_compressed(os.path.join(OUT, "basis_families.npz"), **out)
+    print("basis_families done")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["prune"]:
         prune_golden()
@@ -256,6 +271,8 @@ if __name__ == "__main__":
         prim_golden()
     elif sys.argv[1:] == ["g3d"]:
         gamma_3d_golden()
+    elif sys.argv[1:] == ["basis"]:
+        basis_families_golden()
     else:
         main()
         prune_golden()
@@ -263,3 +280,4 @@ if __name__ == "__main__":
         pol_transfer_golden()
         prim_golden()
         gamma_3d_golden()
+        basis_families_golden()

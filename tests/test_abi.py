@@ -58,6 +58,7 @@ def test_argument_errors_without_gpu(built_lib, mg):
     assert L.modal_adjoint_residual(None, 1, None, None, None) == 1
     assert L.modal_lambda_min(None, None, None, None) == 1
     assert L.modal_project_batch(None, 1, None, 0, None) == 1
+    assert L.modal_set_ortho(None, None, None) == 1
     assert L.modal_autotune(None, None) == 1
     assert L.modal_ctx_captures(None) == 0
     assert L.modal_set_basis_e(None, 2, 10, 3, None) == 1

@@ -85,3 +85,210 @@ def test_mode_orders(mg):
         assert np.array_equal(got, want)
     c1 = mf._order_case1(12)
     assert len({tuple(r) for r in c1.tolist()}) == 12
+
+
+def test_prim_orders(tmp_path):
+    d = str(tmp_path) + "/"
+    (tmp_path / "prim.txt").write_text("0 0 0\n0 0 1\n0 1 1\n1 1 1\n0 0 2\n")
+    base = f"[model]\ndirectory = {d}\norder_file_prim = prim.txt\n[basis]\n"
+    for case, want in [(2, mf._order_case2(4).tolist()), (1, mf._order_case1(4).tolist()),
+                       (3, [[0, 0, 0], [0, 0, 1], [0, 1, 1], [1, 1, 1]]),
+                       # case 4: N-1 file triples, (pmax+1, pmax+1, pmax+2) put in at index 1
+                       (4, [[0, 0, 0], [2, 2, 3], [0, 0, 1], [0, 1, 1]])]:
+        (tmp_path / "p.ini").write_text(base + f"order_prim = {case}\n")
+        t, pm = mf.prim_order(mf.read_ini(os.fspath(tmp_path / "p.ini")), 4)
+        assert t.tolist() == want and pm == max(r[2] for r in want), case
+    (tmp_path / "p.ini").write_text(base + "order_prim = 3\n")
+    with pytest.raises(ValueError):
+        mf.prim_order(mf.read_ini(os.fspath(tmp_path / "p.ini")), 6)
+
+
+def test_proj_names_follow_parameter_c(tmp_path):
+    d = str(tmp_path) + "/"
+    names = mf.proj_names(mf.read_ini(_ini(tmp_path)))
+    # parameter.c:725-760: directory + proj + _T_ + T_lmax + _ + order_prim; sizes without the order
+    assert names == {"T_data": d + "proj_T_2000_3", "E_data": d + "proj_E_1500_3",
+                     "T_size": d + "proj_T_2000_size", "E_size": d + "proj_E_1500_size"}
+    (tmp_path / "abs.ini").write_text("[basis]\nproj_file = /data/tr\n")
+    names = mf.proj_names(mf.read_ini(os.fspath(tmp_path / "abs.ini")))
+    assert names == {"T_data": "/data/tr_T", "E_data": "/data/tr_E", "T_size": "/data/tr_T_size",
+                     "E_size": "/data/tr_E_size"}
+
+
+@pytest.mark.parametrize("order_prim,pol", [(3, False), (4, True)])
+def test_qtilde_files_round_trip(tmp_path, order_prim, pol):
+    """write_qtilde lays the files out as output_qtilde (size file of two native
+    ints, row 0 = x grid, column 0 = l); read_qtilde gives back the
+    [xsize][P][lsize] table, with order_prim 4 through the _l1/_l2 pair."""
+    d = str(tmp_path) + "/"
+    (tmp_path / "t.ini").write_text(f"[model]\ndirectory = {d}\nT_lmax = 30\nE_lmax = 30\n"
+                                    f"do_polarisation = {int(pol)}\n[basis]\norder_prim = {order_prim}\n")
+    ini = mf.read_ini(os.fspath(tmp_path / "t.ini"))
+    rng = np.random.default_rng(3)
+    xs, P, L = 9, 4, 31
+    x = np.linspace(10.0, 90.0, xs)
+    qT, qE = rng.standard_normal((xs, P, L)), rng.standard_normal((xs, P, L))
+    names = mf.write_qtilde(ini, x, qT, qE if pol else None)
+    assert np.fromfile(names["T_size"], dtype=np.int32).tolist() == [L + 1, xs + 1]
+    sfx = ["0", "1", "l1", "l2"] if order_prim == 4 else ["0", "1", "2", "3"]
+    for n, sx in enumerate(sfx):
+        raw = mf.array_read(f"{names['T_data']}_{sx}").reshape(L + 1, xs + 1)
+        assert raw[0, 0] == n and np.array_equal(raw[0, 1:], x) and np.array_equal(raw[1:, 0], np.arange(L))
+        assert np.array_equal(raw[5, 3], qT[2, n, 4])  # data[l+1][i+1] = q~_n(l, x_i)
+    got = mf.read_qtilde(ini, P - 1)
+    assert np.array_equal(got["x"], x) and np.array_equal(got["lvec_T"], np.arange(L))
+    assert np.array_equal(got["qt_T"], qT)
+    if pol:
+        assert np.array_equal(got["qt_E"], qE)
+    else:
+        assert "qt_E" not in got
+    with pytest.raises(FileNotFoundError):  # a missing index file is an error, not a short table
+        os.remove(f"{names['T_data']}_{sfx[-1]}")
+        mf.read_qtilde(ini, P - 1)
+
+
+def test_modes_suffix_follows_output_modes(tmp_path):
+    """output_modes names the file _<model> then one _<p> per shape parameter up
+    to the last one with a non-zero model:shapeX_end (0 where its own end is 0)."""
+    cases = [("", 7, "_7"), ("shape1_end = 3\n", 7, "_7_1"), ("shape2_end = 3\n", 999, "_999_0_2"),
+             ("shape1_end = 1\nshape3_end = 5\n", 998, "_998_1_0_3")]
+    for body, model, want in cases:
+        (tmp_path / "m.ini").write_text("[model]\n" + body)
+        ini = mf.read_ini(os.fspath(tmp_path / "m.ini"))
+        assert mf.modes_suffix(ini, model, 1, 2, 3) == want, body
+
+
+def _order_ini(tmp_path, case, N_file, pol=False):
+    d = str(tmp_path) + "/"
+    raw = mf._order_case2(N_file)
+    np.savetxt(tmp_path / "ttt.txt", raw, fmt="%d")
+    np.savetxt(tmp_path / "tte.txt", raw[:, [0, 1, 2]] % 3, fmt="%d")
+    np.savetxt(tmp_path / "tee.txt", np.stack([raw[:, 1] % 2, raw[:, 2] % 2, raw[:, 0]], 1), fmt="%d")
+    np.savetxt(tmp_path / "eee.txt", raw % 4, fmt="%d")
+    (tmp_path / "o.ini").write_text(
+        f"[model]\ndirectory = {d}\ndo_polarisation = {int(pol)}\norder_TTT_file_late = ttt.txt\n"
+        f"order_TTE_file_late = tte.txt\norder_TEE_file_late = tee.txt\norder_EEE_file_late = eee.txt\n"
+        f"[basis]\norder_late = {case}\n")
+    return mf.read_ini(os.fspath(tmp_path / "o.ini")), raw
+
+
+def test_late_orders_shift_and_extra_terms(tmp_path):
+    """set_terms_late: orders 4-7, 9 and 10 read the file shifted down and put
+    their extra-function triples (offsets from pmax_T) in the freed rows."""
+    N = 12
+    for case, k, rows, add in [(3, 0, {}, 0), (8, 0, {}, 0), (4, 1, {1: (1, 1, 2)}, 2), (7, 1, {1: (1, 1, 2)}, 2),
+                               (9, 1, {1: (1, 1, 2)}, 2), (5, 3, {1: (1, 1, 1), 2: (2, 2, 3), 3: (4, 4, 5)}, 5),
+                               (6, 4, {1: (1, 1, 2), 2: (3, 5, 8), 3: (3, 6, 7), 4: (4, 5, 6)}, 8),
+                               (10, 3, {0: (2, 2, 4), 1: (1, 3, 4), 2: (1, 1, 5)}, 5)]:
+        ini, raw = _order_ini(tmp_path, case, N)
+        lo = mf.late_orders(ini, N)
+        t = lo["ttt"]
+        # untouched rows: the file's row n - k above the shift (n >= k for order 10), row n below it
+        first = k if case == 10 else k + 1
+        for n in range(N):
+            if n in rows:
+                continue
+            want = raw[n - k] if (k and n >= first) else raw[n]
+            assert t[n].tolist() == want.tolist(), (case, n)
+        shifted = np.array([raw[n - k] if (k and n >= first) else raw[n] for n in range(N)])
+        pm = int(shifted[:, 2].max())
+        for n, offs in rows.items():
+            assert t[n].tolist() == [pm + o for o in offs], (case, n)
+        assert lo["pmax_T"] == pm + add, case
+    ini, raw = _order_ini(tmp_path, 3, N)
+    with pytest.raises(ValueError):
+        mf.late_orders(ini, N + 1)
+    with pytest.raises(ValueError):
+        mf.late_orders(mf.read_ini(os.fspath(tmp_path / "o.ini")) | {"basis:order_late": "11"}, N)
+
+
+def test_late_orders_polarised_files(tmp_path):
+    """TTE and EEE lines are the triples; a TEE line (a, b, c) is (c, a, b), T
+    index first (fixed_data.c:343-349); pmax_T/pmax_E count the T and E
+    entries."""
+    N = 10
+    ini, raw = _order_ini(tmp_path, 2, N, pol=True)
+    lo = mf.late_orders(ini, N)
+    assert lo["ttt"].tolist() == mf._order_case2(N).tolist()
+    tee_file = np.loadtxt(tmp_path / "tee.txt", dtype=int)
+    assert lo["tee"].tolist() == tee_file[:, [2, 0, 1]].tolist()
+    assert lo["tte"].tolist() == (raw % 3).tolist() and lo["eee"].tolist() == (raw % 4).tolist()
+    assert lo["pmax_T"] == max(raw[:, 2].max(), (raw[:, 1] % 3).max(), lo["tee"][:, 0].max())
+    assert lo["pmax_E"] == max((raw[:, 2] % 3).max(), lo["tee"][:, 2].max(), (raw[:, 2] % 4).max())
+    lo2 = mf.late_orders(ini, N, pol_lists=(lo["tte"], lo["tee"], lo["eee"]))
+    assert all(np.array_equal(lo[k], lo2[k]) for k in ("tte", "tee", "eee"))
+
+
+def test_basis_families_match_reference(golden):
+    """basis_functions.c compiled in place: Legendre, Fourier and sin-log
+    bit for bit (the same libm calls in the same order); the 'bi' family,
+    restated from its definition, to 1e-12 up to degree 7, beyond which the
+    reference's monomial evaluation loses digits (next test)."""
+    g = golden("basis_families")
+    for name in "ab":
+        lo, hi, pmax, vmin = g["dims_" + name]
+        v = np.arange(lo, hi + 1, dtype=np.float64)
+        for fam, fn in (("legendre", mf.basis_legendre), ("fourier", mf.basis_fourier),
+                        ("sinlog", mf.basis_sinlog)):
+            assert np.array_equal(fn(v, int(pmax), float(vmin), float(hi)), g[f"{fam}_{name}"]), (name, fam)
+        bi, ref = mf.basis_bi(v, int(pmax), float(vmin), float(hi)), g["bi_" + name]
+        for j in range(8):
+            assert np.max(np.abs(bi[:, j] - ref[:, j])) <= 1e-12 * np.max(np.abs(ref[:, j])), (name, j)
+
+
+def test_bi_family_orthonormal():
+    """Known answer for the 'bi' polynomials: orthonormal on [0, 1] under the
+    weight 2x - 3x^2/2 (a 64-point Gauss rule is exact here) to 1e-13
+    through degree 30, with p_0 = sqrt 2 and positive leading coefficients."""
+    x, w = np.polynomial.legendre.leggauss(64)
+    t = (x + 1.0) / 2.0
+    wt = w / 2.0 * (2.0 * t - 1.5 * t * t)
+    B = mf.basis_bi(t, 30, 0.0, 1.0)
+    G = (B * wt[:, None]).T @ B
+    assert np.max(np.abs(G - np.eye(31))) <= 1e-13
+    assert np.allclose(B[:, 0], np.sqrt(2.0), rtol=0, atol=1e-15)
+    assert np.all(np.diff(B[-3:, 30]) > 0)  # increasing towards x = 1 (positive leading coefficient)
+
+
+@pytest.mark.parametrize("case", [1, 4, 6, 7, 8, 9, 10])
+def test_basis_late_columns(tmp_path, case):
+    """create_basis_late's tables: the family columns, and the appended
+    closed-form columns of orders 4, 6, 7, 9 and 10 (row 0 zero except for
+    order 9), checked entry by entry against the formulas."""
+    import math
+    lmin, lmax, n = 2, 300, 12
+    (tmp_path / "b.ini").write_text(f"[model]\nT_lmin = {lmin}\nT_lmax = {lmax}\ndo_polarisation = 1\n"
+                                    f"E_lmin = 3\nE_lmax = 200\n[basis]\norder_late = {case}\n")
+    ini = mf.read_ini(os.fspath(tmp_path / "b.ini"))
+    l = np.arange(lmax + 1.0)
+    spectra = {"cl_tt": 1.0 / (1.0 + l * l), "noise_tt": 1e-6 + 0 * l, "beam_tt": np.exp(-l * 1e-3),
+               "cl_tp": 0.1 / (2.0 + l)}
+    B, E = mf.basis_late(ini, n, 5, spectra if case == 6 else None)
+    T = np.arange(lmin, lmax + 1.0)
+    assert B.shape == (T.size, n + 1) and E.shape == (198, 6)
+    fam = {1: mf.basis_bi, 4: mf.basis_fourier, 6: mf.basis_fourier, 7: mf.basis_bi, 8: mf.basis_sinlog,
+           9: mf.basis_legendre, 10: mf.basis_legendre}[case]
+    nfam = {1: n + 1, 4: n - 1, 6: n - 7, 7: n - 1, 8: n + 1, 9: n - 1, 10: n - 4}[case]
+    assert np.array_equal(B[:, :nfam], fam(T, nfam - 1, float(lmin), float(lmax)))
+    efam = {1: mf.basis_bi, 4: mf.basis_fourier, 6: mf.basis_fourier, 7: mf.basis_bi, 8: mf.basis_sinlog,
+            9: mf.basis_legendre, 10: mf.basis_legendre}[case]
+    assert np.array_equal(E, efam(np.arange(3, 201.0), 5, 3.0, 200.0))
+    i = 57
+    x = T[i] * (T[i] + 1) / (lmax * (lmax + 1.0))
+    z, wv = math.sqrt(x), math.pow((2 * T[i] + 1) / (2 * lmax + 1.0), 1 / 6)
+    if case in (4, 7, 9):
+        assert B[i, n - 1] == wv / z and B[i, n] == wv * z
+        assert (B[0, n - 1] == 0 and B[0, n] == 0) == (case != 9)
+    if case == 6:
+        li = int(T[i])
+        c = wv / math.sqrt(spectra["cl_tt"][li] + spectra["noise_tt"][li] / spectra["beam_tt"][li] ** 2)
+        want = [wv / z, wv * z, c, c * x, c * spectra["cl_tt"][li], c * spectra["cl_tp"][li],
+                c * x * spectra["cl_tt"][li], c * x * spectra["cl_tp"][li]]
+        assert np.allclose(B[i, n - 7:], want, rtol=1e-15, atol=0) and np.all(B[0, n - 7:] == 0)
+    if case == 10:
+        l1 = T[i] / lmax
+        want = [wv / (l1 * z), wv / z, wv * l1 / z, wv * z, wv * l1 * l1 * z]
+        assert np.allclose(B[i, n - 4:], want, rtol=1e-15, atol=0)
+    with pytest.raises(ValueError):
+        (tmp_path / "c.ini").write_text("[model]\nT_lmax = 50\n[basis]\norder_late = 5\n")
+        mf.basis_late(mf.read_ini(os.fspath(tmp_path / "c.ini")), 8)

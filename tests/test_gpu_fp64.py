@@ -300,6 +300,31 @@ def test_alpha_products_any_shape_count(mg, S):
     assert np.array_equal(a, a2) and np.array_equal(mR, mR2)  # fixed reduction order
 
 
+@pytest.mark.parametrize("S", [3, 40])
+def test_alpha_modesR_pca_branch_lower_triangle(mg, orc, S):
+    """On the PCA branch orthol is dense; eigenmodetoday_mpi.c builds lambdainv
+    from its lower triangle only, so modesR = alpha tril(orthol).  GPU alpha and
+    modesR against the oracle's restatement on the downloaded outputs: 1e-12."""
+    rng = np.random.default_rng(77)
+    N = 180
+    A = rng.standard_normal((N, N))
+    G = A @ A.T + N * np.eye(N)
+    beta = rng.standard_normal((S, N))
+    with mg.Context(0) as c:
+        q, _, _ = mg.workload(60, 12)
+        c.set_basis(2, 60, q)
+        c.set_modes(mg.mode_triples(12)[:N])
+        o, lam, branch, rank = c.orthogonalise(G, pca_flag=0)
+        a, mR = c.alpha(S, beta)
+    assert branch == 1 and rank == N
+    assert np.count_nonzero(np.triu(o, 1)) > 0  # dense: the truncation matters
+    for s in range(S):
+        a_o, m_o = orc.alpha(o, lam, beta[s])
+        assert rel_max(a[s], a_o) <= 1e-12
+        assert rel_max(mR[s], m_o) <= 1e-12
+        assert rel_max(mR[s], a[s] @ np.tril(o)) <= 1e-12
+
+
 def test_full_pipeline_on_device(mg, golden):
     """Gamma -> orthogonalise -> project -> alpha with everything left on the device."""
     g = golden("gamma_small")

@@ -10,6 +10,7 @@ later stages read:
   output_names(ini)                  -> the orthol/lambdal/modes/gamma file names
   array_write(path, a) / array_read  -> raw native FP64, no header
   load_three_int(path)               -> [n][3] mode orderings (io.c:229-257)
+  load_spectra(ini, ...)             -> load_cl / load_BN / load_lens / load_TL on integer l
   late_orders(ini, N)                -> set_terms_late orderings 1 to 10 (TTT and polarised)
   basis_late(ini, pmax_t, ...)       -> create_basis_late's basis tables (orders 1-4, 6-10)
   prim_order(ini, N)                 -> set_terms_prim orderings 1 to 5 and pmax_prim
@@ -22,15 +23,16 @@ later stages read:
 
 Command line:
   python modal_files.py ortho_late <ini> [<basis_T.unf> --pt P] [--basis-e <basis_E.unf> --pe PE] [--split]
-  python modal_files.py gamma_late <ini> [<basis_T.unf> --pt P] --cl <cl_total.unf>
+  python modal_files.py gamma_late <ini> [<basis_T.unf> --pt P] [--cl <cl_total.unf>]
       [--basis-e <basis_E.unf> --pe PE --spec9 <spec9.unf>]
-  python modal_files.py modes_late <ini> [<basis_T.unf> --pt P] --cl <cl_total.unf> --tab <shape.npy> --model M
+  python modal_files.py modes_late <ini> [<basis_T.unf> --pt P] [--cl <cl_total.unf>] --tab <shape.npy> --model M
 Mode lists come from the INI file as set_terms_late builds them.  Basis files
 are raw FP64 [L][P] tables (basis_late_T / basis_late_E layouts,
 fixed_data.c:1764); without one the drivers build create_basis_late's table;
-cl_total is raw FP64 over l = 0..T_lmax, C_l + N_l/b_l^2 of the TT weight, and
-spec9 raw FP64 [9][T_lmax+1] (cl TT, TE, EE, beam TT, TE, EE, noise TT, TE,
-EE), the spectra load_cl / load_BN interpolate onto integer l.
+the spectra come from the INI's cls / BN / pixel-window files (load_spectra),
+or as raw FP64: cl_total over l = 0..T_lmax (C_l + N_l/b_l^2 of the TT
+weight) and spec9 [9][T_lmax+1] (cl TT, TE, EE, beam TT, TE, EE, noise TT,
+TE, EE).
 """
 import argparse
 import os
@@ -275,6 +277,160 @@ def mode_order(ini, N):
     return late_orders(ini, N, pol=False)["ttt"]
 
 
+# ------------------------------------------------------------ spectra
+
+def _ini_path(ini, key, default):
+    """A file key of parameter.c: absolute as given, else directory + value."""
+    v = getstring(ini, key, default)
+    return v if v.startswith("/") else _params(ini)["directory"] + v
+
+
+def load_txt_dbl(path, columns):
+    """load_txt_dbl (io.c:64-93): lines starting with '#' skipped, the first
+    `columns` numbers of every other line (missing ones read as 0).  Returns
+    [rows][columns]."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#"):
+                continue
+            vals = []
+            for tok in line.split()[:columns]:
+                try:
+                    vals.append(float(tok))
+                except ValueError:
+                    break
+            rows.append(vals + [0.0] * (columns - len(vals)))
+    return np.array(rows, dtype=np.float64).reshape(-1, columns)
+
+
+def natural_spline(x, y):
+    """Natural cubic spline through (x, y) (zero second derivative at both
+    ends), the interpolant of GSL's gsl_interp_cspline that load_cl / load_BN
+    use.  Restated from its definition: the second derivatives M solve
+    h_{i-1} M_{i-1} + 2 (h_{i-1} + h_i) M_i + h_i M_{i+1}
+      = 6 ((y_{i+1} - y_i)/h_i - (y_i - y_{i-1})/h_{i-1}).
+    Returns f(t) for t in [x_0, x_last]; outside it raises ValueError (GSL
+    stops there with a domain error)."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    n = x.size
+    if n < 3 or np.any(np.diff(x) <= 0):
+        raise ValueError("a natural spline needs at least 3 increasing abscissae")
+    h = np.diff(x)
+    M = np.zeros(n)
+    if n > 2:
+        diag = 2.0 * (h[:-1] + h[1:])
+        off = h[1:-1].copy()
+        rhs = 6.0 * (np.diff(y[1:]) / h[1:] - np.diff(y[:-1]) / h[:-1])
+        m = n - 2
+        cp, dp = np.zeros(m), np.zeros(m)  # Thomas algorithm on the symmetric tridiagonal system
+        for i in range(m):
+            den = diag[i] - (off[i - 1] * cp[i - 1] if i else 0.0)
+            cp[i] = off[i] / den if i < m - 1 else 0.0
+            dp[i] = (rhs[i] - (off[i - 1] * dp[i - 1] if i else 0.0)) / den
+        for i in range(m - 1, -1, -1):
+            M[i + 1] = dp[i] - (cp[i] * M[i + 2] if i < m - 1 else 0.0)
+
+    def f(t):
+        t = np.asarray(t, dtype=np.float64)
+        if np.any(t < x[0]) or np.any(t > x[-1]):
+            raise ValueError(f"spline evaluated outside [{x[0]}, {x[-1]}]")
+        i = np.clip(np.searchsorted(x, t, side="right") - 1, 0, n - 2)
+        hi, a, b = h[i], x[i + 1] - t, t - x[i]
+        return (M[i] * a ** 3 + M[i + 1] * b ** 3) / (6.0 * hi) + (y[i] / hi - M[i] * hi / 6.0) * a \
+            + (y[i + 1] / hi - M[i + 1] * hi / 6.0) * b
+    return f
+
+
+def _on_l(lmax, l_raw, y_raw, scale=None):
+    """Spline of a table onto l = 0..lmax, zero for l <= l_raw[0] - 1/2 (the
+    reference's guard), with scale(l) applied to the interpolated value."""
+    out = np.zeros(lmax + 1)
+    l = np.arange(lmax + 1, dtype=np.float64)
+    on = l > l_raw[0] - 0.5
+    if np.any(on):
+        v = natural_spline(l_raw, y_raw)(l[on])
+        with np.errstate(divide="ignore", invalid="ignore"):  # l = 0 in a D_l table gives inf, as in C
+            out[on] = v if scale is None else scale(l[on], v)
+    return out
+
+
+def load_spectra(ini, lens=False, tl=False):
+    """load_cl, load_BN, load_lens and load_TL (fixed_data.c:1116-1498, 1542-1597):
+    spectra on integer l from the INI file's tables, by natural cubic splines.
+      cl_tt (and cl_te, cl_ee with do_polarisation) over l = 0..T_lmax
+        (E_lmax), 2 pi D_l / (l (l+1)) from model:cls_lensed_file (l, TT, EE,
+        BB, TE) with basis:uselens 1, else model:cls_scalar_file (l, TT, EE,
+        TE, P, PT);
+      beam_tt = pixel window x spline of model:BN_TT_file (l, beam, noise),
+        noise_tt = spline of its noise; the pixel window (model:pixw_file,
+        l, w) is taken by row index, as the reference does; E likewise from
+        model:BN_EE_file; beam_te = sqrt(beam_tt beam_ee), noise_te = 0;
+      cl_tp (lens): spline of the scalar file's PT column / l^3;
+      t_wgt (tl): spline of model:transfer_wgt_file (l, T_l) at l = 1..T_lmax.
+    Values at l <= (first tabulated l) - 1/2 are 0, as the reference sets them.
+    Also cl_total = cl_tt + noise_tt / beam_tt^2 at l >= 2 (the TT weight's
+    spectrum, 1 below l = 2), and spec9 for the polarised transfer Gamma."""
+    import math
+    p = _params(ini)
+    lT, lE = p["T_lmax"], p["E_lmax"]
+    pol = p["do_polarisation"] == 1
+    out = {}
+    dl2cl = lambda l, v: 2.0 * math.pi * v / (l * (l + 1.0))  # noqa: E731
+    if getint(ini, "basis:uselens", 1) == 1:
+        d = load_txt_dbl(_ini_path(ini, "model:cls_lensed_file", "cls_planck_DDX9_lensed.txt"), 5)
+        cols = {"tt": 1, "ee": 2, "te": 4}
+    else:
+        d = load_txt_dbl(_ini_path(ini, "model:cls_scalar_file", "cls_planck_DDX9_scalar.txt"), 6)
+        cols = {"tt": 1, "ee": 2, "te": 3}
+    if lT > d[-1, 0]:
+        raise ValueError(f"Cls do not contain enough l's, max data {lT} max cl: {int(d[-1, 0])}")
+    out["cl_tt"] = _on_l(lT, d[:, 0], d[:, cols["tt"]], dl2cl)
+    if pol:
+        out["cl_te"] = _on_l(lE, d[:, 0], d[:, cols["te"]], dl2cl)
+        out["cl_ee"] = _on_l(lE, d[:, 0], d[:, cols["ee"]], dl2cl)
+    pix = load_txt_dbl(_ini_path(ini, "model:pixw_file", "pixwgt_2048.txt"), 2)[:, 1]
+    for x, lm in (("tt", lT),) + ((("ee", lE),) if pol else ()):
+        bn = load_txt_dbl(_ini_path(ini, f"model:BN_{x.upper()}_file", f"BN_{x.upper()}.txt"), 3)
+        if lm > bn[-1, 0]:
+            raise ValueError(f"BN {x.upper()} do not contain enough l's, max data {lm} max BN: {int(bn[-1, 0])}")
+        if pix.size < lm + 1:
+            raise ValueError(f"pixel window has {pix.size} rows, l = 0..{lm} needs {lm + 1}")
+        out[f"beam_{x}"] = _on_l(lm, bn[:, 0], bn[:, 1], lambda l, v: pix[l.astype(np.int64)] * v)
+        out[f"noise_{x}"] = _on_l(lm, bn[:, 0], bn[:, 2])
+    if pol:
+        out["beam_te"] = np.sqrt(out["beam_tt"][:lE + 1] * out["beam_ee"])
+        out["noise_te"] = np.zeros(lE + 1)
+    if lens:
+        d6 = load_txt_dbl(_ini_path(ini, "model:cls_scalar_file", "cls_planck_DDX9_scalar.txt"), 6)
+        if lT > d6[-1, 0]:
+            raise ValueError(f"Cls do not contain enough l's, max data {lT} max cl: {int(d6[-1, 0])}")
+        out["cl_tp"] = _on_l(lT, d6[:, 0], d6[:, 5], lambda l, v: v / (l * l * l))
+    if tl:
+        t = load_txt_dbl(_ini_path(ini, "model:transfer_wgt_file", "wmap7_Tl.txt"), 2)
+        if lT > t[-1, 0]:
+            raise ValueError(f"T do not contain enough l's, max data {lT} max T: {int(t[-1, 0])}")
+        w = np.zeros(lT + 1)
+        w[1:] = natural_spline(t[:, 0], t[:, 1])(np.arange(1, lT + 1, dtype=np.float64))
+        out["t_wgt"] = w
+    ct = np.ones(lT + 1)
+    with np.errstate(divide="ignore", invalid="ignore"):  # zero beam below the tables: not finite, rejected later
+        ct[2:] = out["cl_tt"][2:] + out["noise_tt"][2:] / (out["beam_tt"][2:] * out["beam_tt"][2:])
+    out["cl_total"] = ct
+    if pol:
+        n = lT + 1
+
+        def ext(a):
+            e = np.zeros(n)
+            e[:min(n, a.size)] = a[:n]
+            return e
+        out["spec9"] = np.stack([out["cl_tt"], ext(out["cl_te"]), ext(out["cl_ee"]), out["beam_tt"],
+                                 ext(out["beam_te"]), ext(out["beam_ee"]), out["noise_tt"], ext(out["noise_te"]),
+                                 ext(out["noise_ee"])])
+    return out
+
+
 # ------------------------------------------------------------ basis tables
 
 def _libm(f, a):
@@ -388,14 +544,16 @@ def basis_bi(values, pmax, vmin, vmax):
 def basis_late(ini, pmax_t, pmax_e=None, spectra=None, pol=None):
     """create_basis_late (fixed_data.c:1754-1986): (basis_T [T_size][pmax_T+1],
     basis_E [E_size][pmax_E+1] or None) on l = T_lmin..T_lmax (E_lmin..E_lmax)
-    for basis:order_late 1-4 and 6-10.  Orders 1-3 and 7 use the 'bi'
-    polynomials (basis_bi), 4 and 6 Fourier, 8 sin-log, 9 and 10 shifted
-    Legendre; 4, 6, 7, 9 and 10 append their closed-form columns in
+    for basis:order_late 1-10.  Orders 1-3 and 7 use the 'bi' polynomials
+    (basis_bi), 4-6 Fourier, 8 sin-log, 9 and 10 shifted Legendre; 4-7, 9
+    and 10 append their closed-form columns in
     w = ((2l+1)/(2lmax+1))^{1/6} and z = sqrt(l(l+1)/(lmax(lmax+1))), and
     order 6 those scaled by c = w/sqrt(C_l + N_l/b_l^2) with C_l and the
     lensing cross-spectrum C_l^{TP}: spectra = {"cl_tt", "noise_tt",
-    "beam_tt", "cl_tp"} over l = 0..T_lmax.  Order 5 needs load_TL's table
-    and is not restated.  Row 0 of order 10's columns pmax-3 and pmax-2 is
+    "beam_tt", "cl_tp"} over l = 0..T_lmax, order 5 the transfer weight
+    spectra["t_wgt"] (load_TL), taken by row index as the reference takes
+    it.  load_spectra reads both from the INI's files.  Row 0 of order 10's
+    columns pmax-3 and pmax-2 is
     left uninitialised by the reference; it is 0 here.  The E basis
     (model:do_polarisation 1) is bi for orders < 4 and 7, Fourier for 4-6,
     sin-log for 8 and Legendre for 9 and 10; pol overrides do_polarisation."""
@@ -448,8 +606,23 @@ def basis_late(ini, pmax_t, pmax_e=None, spectra=None, pol=None):
         B[1:, n - 2] = ws * l1 / zs
         B[1:, n - 1] = ws * zs
         B[1:, n] = ws * (l1 * l1) * zs
+    elif case == 5:
+        if spectra is None or "t_wgt" not in spectra:
+            raise ValueError("order_late 5 needs load_TL's t_wgt (load_spectra(ini, tl=True))")
+        tw = np.asarray(spectra["t_wgt"], dtype=np.float64)
+        if tw.size < Tvec.size:
+            raise ValueError(f"t_wgt has {tw.size} values, {Tvec.size} rows need as many")
+        tw = tw[:Tvec.size]  # by row index, as the reference reads it
+        B[:, :n - 4] = basis_fourier(Tvec, n - 5, Tmin, Tmax)
+        B[0, n - 4] = tw[0]
+        xs, zs, ws, ts = x[1:], z[1:], w[1:], tw[1:]
+        B[1:, n - 4] = ts
+        B[1:, n - 3] = ws / zs
+        B[1:, n - 2] = ws * zs
+        B[1:, n - 1] = ts * ws / zs
+        B[1:, n] = ts * ws * zs
     else:
-        raise ValueError(f"order_late {case}: not restated (order 5 needs load_TL's t_wgt table)")
+        raise ValueError(f"invalid order_late {case}")
     E = None
     if p["do_polarisation"] == 1 if pol is None else pol:
         if pmax_e is None:
@@ -595,6 +768,8 @@ def _late_setup(ini, basis_t, basis_e, pol_orders, spectra, pol=None):
     lo = late_orders(ini, N, pol, pol_orders)
     tri = lo["ttt"]
     if basis_t is None:
+        if spectra is None and p["order_late"] in (5, 6):
+            spectra = load_spectra(ini, lens=p["order_late"] == 6, tl=p["order_late"] == 5)
         basis_t, be = basis_late(ini, lo["pmax_T"], lo["pmax_E"] if pol else None, spectra, pol)
         basis_e = be if basis_e is None else basis_e
     basis_t = np.asarray(basis_t, dtype=np.float64)
@@ -657,8 +832,9 @@ def gamma_late(ini_path, basis_t, cl_total, basis_e=None, pol_orders=None, spec9
     model:do_polarisation is 1).  The lambdal_XXX files are the ones
     ortho_late wrote for the same INI.  Mode lists and basis tables as for
     ortho_late (basis_t None: basis_late's); cl_total over l = 0..T_lmax
-    (C_l + N_l/b_l^2); with polarisation spec9 [9][T_lmax + 1].  Returns the
-    dict of written paths."""
+    (C_l + N_l/b_l^2); with polarisation spec9 [9][T_lmax + 1]; either None:
+    load_spectra's, from the INI's spectrum files.  Returns the dict of
+    written paths."""
     import warnings
 
     import modal_gb300 as mg
@@ -669,6 +845,10 @@ def gamma_late(ini_path, basis_t, cl_total, basis_e=None, pol_orders=None, spec9
     pol = p0["do_polarisation"] == 1
     if pol and do3d:
         warnings.warn("polarisation currently disabled for 3D gamma calculations: skipping it")
+    if cl_total is None or (pol and not do3d and spec9 is None):
+        sp = load_spectra(ini)
+        cl_total = sp["cl_total"] if cl_total is None else cl_total
+        spec9 = sp.get("spec9") if spec9 is None else spec9
     cl_total = np.asarray(cl_total, dtype=np.float64).ravel()
     if cl_total.size < lmax + 1:
         raise ValueError(f"cl_total has {cl_total.size} values, l = 0..{lmax} needs {lmax + 1}")
@@ -728,14 +908,16 @@ def modes_late(ini_path, basis_t, cl_total, shapes, models, prec=None, device=0,
     the lower triangle of orthol (eigenmodetoday_mpi.c:148-162, 286-316; the
     reference keeps modesR in memory).  models: the model number of each shape
     (the reference's mode argument; 999 and 998 name its ISW and point-source
-    templates, which are not restated).  Returns (written paths, alpha [S][N],
-    modesR [S][N])."""
+    templates, which are not restated).  cl_total None: load_spectra's.
+    Returns (written paths, alpha [S][N], modesR [S][N])."""
     import modal_gb300 as mg
     ini = read_ini(ini_path)
     if len(models) != len(shapes):
         raise ValueError(f"{len(shapes)} shapes but {len(models)} model numbers")
     p, N, tri, basis_t, _, _, _ = _late_setup(ini, basis_t, None, None, spectra, pol=False)
     lmax = p["T_lmax"]
+    if cl_total is None:
+        cl_total = load_spectra(ini)["cl_total"]
     cl_total = np.asarray(cl_total, dtype=np.float64).ravel()
     if cl_total.size < lmax + 1:
         raise ValueError(f"cl_total has {cl_total.size} values, l = 0..{lmax} needs {lmax + 1}")
@@ -758,6 +940,7 @@ def modes_late(ini_path, basis_t, cl_total, shapes, models, prec=None, device=0,
 
 
 BASIS_HELP = "raw FP64 [L_T][P_T] (needs --pt); omitted: create_basis_late's table for basis:order_late"
+CL_HELP = "raw FP64 C_l + N_l/b_l^2 over l = 0..T_lmax; omitted: from the INI's cls/BN/pixel-window files"
 
 
 def main(argv=None):
@@ -774,7 +957,7 @@ def main(argv=None):
     g.add_argument("ini")
     g.add_argument("basis_t", nargs="?", help=BASIS_HELP)
     g.add_argument("--pt", type=int, help="P_T, the number of T basis functions")
-    g.add_argument("--cl", required=True, help="raw FP64 C_l + N_l/b_l^2 over l = 0..T_lmax")
+    g.add_argument("--cl", help=CL_HELP)
     g.add_argument("--basis-e", help="raw FP64 [L_E][P_E]")
     g.add_argument("--pe", type=int, help="P_E")
     g.add_argument("--spec9", help="raw FP64 [9][T_lmax+1] spectra, beams and noise")
@@ -782,7 +965,7 @@ def main(argv=None):
     m.add_argument("ini")
     m.add_argument("basis_t", nargs="?", help=BASIS_HELP)
     m.add_argument("--pt", type=int, help="P_T, the number of T basis functions")
-    m.add_argument("--cl", required=True, help="raw FP64 C_l + N_l/b_l^2 over l = 0..T_lmax")
+    m.add_argument("--cl", help=CL_HELP)
     m.add_argument("--tab", required=True, help=".npy separable shape table [T][3][T_lmax+1]")
     m.add_argument("--model", type=int, required=True, help="model number in the output name")
     a = ap.parse_args(argv)
@@ -792,7 +975,7 @@ def main(argv=None):
     if a.cmd == "modes_late":
         import modal_gb300 as mg
         shape = {"kind": mg.SHAPE_SEPARABLE, "tab": np.load(a.tab)}
-        out, _, _ = modes_late(a.ini, bt, array_read(a.cl), [shape], [a.model])
+        out, _, _ = modes_late(a.ini, bt, array_read(a.cl) if a.cl else None, [shape], [a.model])
         for k, v in out.items():
             print(k, v)
         return
@@ -801,7 +984,7 @@ def main(argv=None):
         out = ortho_late(a.ini, bt, be, None, a.split)
     else:
         sp = array_read(a.spec9).reshape(9, -1) if a.spec9 else None
-        out = gamma_late(a.ini, bt, array_read(a.cl), be, None, sp)
+        out = gamma_late(a.ini, bt, array_read(a.cl) if a.cl else None, be, None, sp)
     for k, v in out.items():
         print(k, v)
 

@@ -292,3 +292,81 @@ def test_basis_late_columns(tmp_path, case):
     with pytest.raises(ValueError):
         (tmp_path / "c.ini").write_text("[model]\nT_lmax = 50\n[basis]\norder_late = 5\n")
         mf.basis_late(mf.read_ini(os.fspath(tmp_path / "c.ini")), 8)
+
+
+def write_spectrum_files(d, lmax, step=1, lmin_tab=2):
+    """Synthetic reference-format tables: lensed and scalar cls (D_l), TT/EE
+    beam-and-noise files and a pixel window, tabulated every `step` l."""
+    l = np.arange(lmin_tab, lmax + 5, step, dtype=np.float64)
+    dl = 1e3 * np.exp(-(l / 900.0) ** 2) * (1 + 0.1 * np.sin(l / 17.0))
+    lens = np.stack([l, dl, 0.05 * dl, 0.01 * dl, 0.3 * dl * np.cos(l / 9.0)], 1)
+    scal = np.stack([l, dl, 0.05 * dl, 0.3 * dl, 0.2 * dl, 1e-3 * dl * l], 1)
+    with open(os.path.join(d, "lensed.txt"), "w") as f:
+        f.write("# l TT EE BB TE\n")
+        np.savetxt(f, lens)
+    np.savetxt(os.path.join(d, "scalar.txt"), scal)
+    np.savetxt(os.path.join(d, "bn_t.txt"), np.stack([l, np.exp(-l * l * 1e-6), 1e-5 + 0 * l], 1))
+    np.savetxt(os.path.join(d, "bn_e.txt"), np.stack([l, np.exp(-l * l * 2e-6), 3e-5 + 0 * l], 1))
+    lp = np.arange(0, lmax + 5, dtype=np.float64)
+    np.savetxt(os.path.join(d, "pixw.txt"), np.stack([lp, 1.0 - 1e-5 * lp], 1))
+    lt = np.arange(0, lmax + 5, step, dtype=np.float64)  # load_TL evaluates from l = 1
+    np.savetxt(os.path.join(d, "tl.txt"), np.stack([lt, 1.0 / (1.0 + lt / 500.0)], 1))
+    return ("cls_lensed_file = lensed.txt\ncls_scalar_file = scalar.txt\nBN_TT_file = bn_t.txt\n"
+            "BN_EE_file = bn_e.txt\npixw_file = pixw.txt\ntransfer_wgt_file = tl.txt\n")
+
+
+def test_load_spectra_tables(tmp_path):
+    """load_cl / load_BN / load_lens / load_TL: D_l -> 2 pi D_l/(l(l+1)) on the
+    tabulated l exactly, natural-spline values in between (scipy's natural
+    CubicSpline to 1e-13), the pixel window by row, zeros below the first
+    tabulated l, TE beam sqrt(b_T b_E) and noise 0, PT/l^3, and the errors for
+    tables that end before l_max."""
+    from scipy.interpolate import CubicSpline
+    d = str(tmp_path) + "/"
+    lmax = 300
+    keys = write_spectrum_files(d, lmax, step=3, lmin_tab=3)
+    (tmp_path / "s.ini").write_text(f"[model]\ndirectory = {d}\nT_lmax = {lmax}\nE_lmax = 250\n"
+                                    f"do_polarisation = 1\n{keys}[basis]\nuselens = 1\n")
+    ini = mf.read_ini(os.fspath(tmp_path / "s.ini"))
+    sp = mf.load_spectra(ini, lens=True, tl=True)
+    lens = np.loadtxt(tmp_path / "lensed.txt")
+    l = np.arange(lmax + 1.0)
+    want = CubicSpline(lens[:, 0], lens[:, 1], bc_type="natural")(l[3:]) * 2 * np.pi / (l[3:] * (l[3:] + 1))
+    assert np.all(sp["cl_tt"][:3] == 0)  # below the first tabulated l (3 - 1/2)
+    assert np.max(np.abs(sp["cl_tt"][3:] - want)) <= 1e-13 * np.max(np.abs(want))
+    i = 6  # a tabulated l: the spline passes through the table value
+    assert abs(sp["cl_tt"][i] - 2 * np.pi * lens[1, 1] / (i * (i + 1))) <= 1e-15 * sp["cl_tt"][i]
+    bn = np.loadtxt(tmp_path / "bn_t.txt")
+    pix = np.loadtxt(tmp_path / "pixw.txt")[:, 1]
+    wb = CubicSpline(bn[:, 0], bn[:, 1], bc_type="natural")(l[3:]) * pix[3:lmax + 1]
+    assert np.max(np.abs(sp["beam_tt"][3:] - wb)) <= 1e-13
+    assert sp["beam_te"].size == 251 and np.allclose(sp["beam_te"], np.sqrt(sp["beam_tt"][:251] * sp["beam_ee"]))
+    assert np.all(sp["noise_te"] == 0) and sp["spec9"].shape == (9, lmax + 1)
+    sc = np.loadtxt(tmp_path / "scalar.txt")
+    tp = CubicSpline(sc[:, 0], sc[:, 5], bc_type="natural")(l[3:]) / l[3:] ** 3
+    assert np.max(np.abs(sp["cl_tp"][3:] - tp)) <= 1e-13 * np.max(np.abs(tp))
+    tl = np.loadtxt(tmp_path / "tl.txt")
+    assert sp["t_wgt"][0] == 0 and abs(sp["t_wgt"][6] - tl[2, 1]) <= 1e-15
+    ct = sp["cl_total"]
+    assert np.allclose(ct[3:], sp["cl_tt"][3:] + sp["noise_tt"][3:] / sp["beam_tt"][3:] ** 2, rtol=1e-15, atol=0)
+    (tmp_path / "t.ini").write_text(f"[model]\ndirectory = {d}\nT_lmax = 400\n{keys}")
+    with pytest.raises(ValueError):  # the tables end at l = 302
+        mf.load_spectra(mf.read_ini(os.fspath(tmp_path / "t.ini")))
+    (tmp_path / "x.txt").write_text("# header\n1 2\n3 4 5\n")
+    assert mf.load_txt_dbl(os.fspath(tmp_path / "x.txt"), 3).tolist() == [[1, 2, 0], [3, 4, 5]]
+
+
+def test_basis_late_order5_uses_t_wgt_by_row(tmp_path):
+    """Order 5: Fourier columns, then t_wgt (row-indexed, as the reference reads
+    it), w/z, w z, t_wgt w/z and t_wgt w z."""
+    import math
+    (tmp_path / "b.ini").write_text("[model]\nT_lmin = 2\nT_lmax = 100\n[basis]\norder_late = 5\n")
+    ini = mf.read_ini(os.fspath(tmp_path / "b.ini"))
+    tw = 1.0 + np.arange(101) * 0.01
+    B, _ = mf.basis_late(ini, 10, spectra={"t_wgt": tw})
+    assert np.array_equal(B[:, :6], mf.basis_fourier(np.arange(2, 101.0), 5, 2.0, 100.0))
+    assert B[0, 6] == tw[0] and np.all(B[0, 7:] == 0)
+    i, T = 40, 42.0
+    x = T * (T + 1) / (100 * 101.0)
+    z, wv = math.sqrt(x), math.pow((2 * T + 1) / 201.0, 1 / 6)
+    assert np.allclose(B[i, 6:], [tw[i], wv / z, wv * z, tw[i] * wv / z, tw[i] * wv * z], rtol=1e-15, atol=0)

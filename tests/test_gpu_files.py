@@ -174,33 +174,37 @@ def test_modes_late_driver_from_files(mg, orc, tmp_path):
         assert rel_max(a[s], a_o) <= 1e-10 and rel_max(mR[s], m_o) <= 1e-10
 
 
-def test_drivers_from_ini_only(mg, tmp_path):
-    """No basis file: the three drivers build create_basis_late's table
-    (order_late 9: shifted Legendre plus the two closed-form columns, with the
-    extra-function triple put in at row 1) and take the mode lists from the
-    INI's order files, through the command line."""
+@pytest.mark.parametrize("order_late", [9, 6])
+def test_drivers_from_ini_only(mg, tmp_path, order_late):
+    """No basis or spectrum file on the command line: the three drivers build
+    create_basis_late's table (order_late 9: shifted Legendre plus two
+    closed-form columns; 6: Fourier plus eight, scaled by the spectra), take
+    the mode lists from the INI's order files (extra-function triples put in)
+    and the spectra from its cls / BN / pixel-window tables (load_spectra)."""
+    from test_files import write_spectrum_files
     lmax, N, xsize = 80, 15, 21
     raw = mf._order_case2(40)
     np.savetxt(tmp_path / "ttt.txt", raw, fmt="%d")
+    keys = write_spectrum_files(str(tmp_path), lmax, step=1, lmin_tab=0)
     ini = tmp_path / "run.ini"
     ini.write_text(f"[model]\ndirectory = {tmp_path}/\nT_lmin = 2\nT_lmax = {lmax}\ndelta_phi = 0.9\n"
-                   f"order_TTT_file_late = ttt.txt\n[basis]\nterms = {N}\norder_late = 9\norder_prim = 2\n"
-                   f"[old]\ngflag_pca = 1\n")
+                   f"order_TTT_file_late = ttt.txt\n{keys}[basis]\nterms = {N}\norder_late = {order_late}\n"
+                   f"order_prim = 2\n[old]\ngflag_pca = 1\n")
     ini = os.fspath(ini)
     ini_d = mf.read_ini(ini)
     lo = mf.late_orders(ini_d, N)
-    assert lo["ttt"][1].tolist() == [lo["pmax_T"] - 1, lo["pmax_T"] - 1, lo["pmax_T"]]
-    B, _ = mf.basis_late(ini_d, lo["pmax_T"])
-    cl = mg.synthetic_cl(lmax)
+    pm = lo["pmax_T"] - (2 if order_late == 9 else 8)
+    assert lo["ttt"][1].tolist() == [pm + 1, pm + 1, pm + 2]
+    sp = mf.load_spectra(ini_d, lens=True)
+    B, _ = mf.basis_late(ini_d, lo["pmax_T"], spectra=sp)
+    cl = sp["cl_total"]
     prim, pmax = mf.prim_order(ini_d, N)
     xvec, qt = mg.transfer_workload(lmax, pmax + 1, xsize)
     mf.write_qtilde(ini_d, xvec, qt)
-    clf = tmp_path / "cl.unf"
-    mf.array_write(os.fspath(clf), cl)
     np.save(tmp_path / "tab.npy", mg.separable_shapes(lmax, 1, seed=9)[0]["tab"])
     mf.main(["ortho_late", ini])
-    mf.main(["gamma_late", ini, "--cl", os.fspath(clf)])
-    mf.main(["modes_late", ini, "--cl", os.fspath(clf), "--tab", os.fspath(tmp_path / "tab.npy"), "--model", "3"])
+    mf.main(["gamma_late", ini])
+    mf.main(["modes_late", ini, "--tab", os.fspath(tmp_path / "tab.npy"), "--model", "3"])
     names = mf.output_names(ini_d)
     o = mf.array_read(names["orthol_TTT"], N * N).reshape(N, N)
     gam = mf.array_read(names["gamma_TTT"], N * N).reshape(N, N)

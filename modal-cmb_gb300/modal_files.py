@@ -827,7 +827,8 @@ def gamma_late(ini_path, basis_t, cl_total, basis_e=None, pol_orders=None, spec9
     fixed_data.c:3077-3091: terms^2 raw FP64, row = late mode).
 
     basis:do3D 0 takes the 3D path (calculate_gamma_TTT_3D_nested; as the
-    reference, polarisation is skipped there with a warning), any other value
+    reference, polarisation is skipped there with a warning and its gamma
+    files are written as zeros), any other value
     the 2D one (calculate_gamma_2d, with TTE/TEE/EEE when
     model:do_polarisation is 1).  The lambdal_XXX files are the ones
     ortho_late wrote for the same INI.  Mode lists and basis tables as for
@@ -886,6 +887,13 @@ def gamma_late(ini_path, basis_t, cl_total, basis_e=None, pol_orders=None, spec9
         lam = array_read(names[f"lambdal_{x}"], N * N).reshape(N, N)
         array_write(names[f"gamma_{x}"], (lam.T @ lam) @ g)
         written[f"gamma_{x}"] = names[f"gamma_{x}"]
+    if do3d and p0["do_polarisation"] == 1:
+        # the 3D path leaves the polarised Gammas at zero and output_gamma still
+        # writes them (gamma_mpi.c:335-355, fixed_data.c:3085-3089)
+        for x in ("TTE", "TEE", "EEE"):
+            if f"gamma_{x}" in names:
+                array_write(names[f"gamma_{x}"], np.zeros((N, N)))
+                written[f"gamma_{x}"] = names[f"gamma_{x}"]
     return written
 
 

@@ -71,6 +71,8 @@ def test_gamma_late_driver_after_ortho_late(mg, orc, tmp_path, do3d):
         mf.ortho_late(_late_ini(tmp_path, lmax, N, name="ortho.ini"), q)
         with pytest.warns(UserWarning, match="polarisation"):
             out = mf.gamma_late(ini, q, cl)
+        for x in ("TTE", "TEE", "EEE"):  # written as zeros, as the reference's 3D path leaves them
+            assert np.all(mf.array_read(out.pop(f"gamma_{x}"), N * N) == 0)
     else:
         mf.main(["ortho_late", ini, os.fspath(bt), "--pt", str(P)])
         mf.main(["gamma_late", ini, os.fspath(bt), "--pt", str(P), "--cl", os.fspath(clf)])

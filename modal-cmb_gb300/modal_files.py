@@ -1,4 +1,4 @@
-"""Reference-compatible file formats and an INI-driven driver for the GPU path.
+"""Reference-compatible file formats and INI-driven drivers for the GPU path.
 
 The reference's drivers read an iniparser INI file (parameter.c:127-980), name
 their outputs from its keys (parameter.c:243-700), and write raw native FP64
@@ -12,7 +12,7 @@ later stages read:
   load_three_int(path)               -> [n][3] mode orderings (io.c:229-257)
   load_spectra(ini, ...)             -> load_cl / load_BN / load_lens / load_TL on integer l
   late_orders(ini, N)                -> set_terms_late orderings 1 to 10 (TTT and polarised)
-  basis_late(ini, pmax_t, ...)       -> create_basis_late's basis tables (orders 1-4, 6-10)
+  basis_late(ini, pmax_t, ...)       -> create_basis_late's basis tables (orders 1-10)
   prim_order(ini, N)                 -> set_terms_prim orderings 1 to 5 and pmax_prim
   proj_names(ini)                    -> the proj_T/E data and size file names
   read_qtilde / write_qtilde         -> the transfer-function files (read_qtilde,
@@ -50,7 +50,8 @@ if HERE not in sys.path:
 
 def read_ini(path):
     """iniparser-style dictionary: keys 'section:key' in lower case, values
-    with surrounding quotes removed; ';' and '#' start comments."""
+    with surrounding quotes removed; ';' and '#' start comment lines and end
+    unquoted values."""
     out, section = {}, ""
     with open(path) as f:
         for raw in f:
@@ -65,14 +66,32 @@ def read_ini(path):
                 continue
             key, val = line.split("=", 1)
             val = val.strip()
-            if val[:1] in "\"'":
+            if val[:1] and val[:1] in "\"'":
                 q = val[0]
                 end = val.find(q, 1)
                 val = val[1:end] if end > 0 else val[1:]
             else:
-                val = re.split(r"\s[;#]", val, maxsplit=1)[0].strip()
+                val = re.split(r"[;#]", val, maxsplit=1)[0].strip()
             out[f"{section}:{key.strip().lower()}"] = val
     return out
+
+
+def _strtol0(v):
+    """C strtol(v, NULL, 0): optional sign, 0x hex, leading-0 octal, else
+    decimal, up to the first character that does not fit (0 if none)."""
+    m = re.match(r"\s*([+-]?)(0[xX][0-9a-fA-F]+|0[0-7]*|[1-9][0-9]*)", v)
+    if not m:
+        return 0
+    digits = m.group(2)
+    base = 16 if digits[:2] in ("0x", "0X") else (8 if digits.startswith("0") and len(digits) > 1 else 10)
+    n = int(digits, base)
+    return -n if m.group(1) == "-" else n
+
+
+def _atof(v):
+    """C atof: the longest decimal floating-point prefix (0.0 if none)."""
+    m = re.match(r"\s*[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?", v)
+    return float(m.group(0)) if m else 0.0
 
 
 def _get(ini, key, default, conv=str):
@@ -86,11 +105,13 @@ def _get(ini, key, default, conv=str):
 
 
 def getint(ini, key, default):
-    return _get(ini, key, default, lambda v: int(float(v)) if v.strip() else default)
+    """iniparser_getint: strtol(value, NULL, 0)."""
+    return _get(ini, key, default, _strtol0)
 
 
 def getdouble(ini, key, default):
-    return _get(ini, key, default, float)
+    """iniparser_getdouble: atof(value)."""
+    return _get(ini, key, default, _atof)
 
 
 def getstring(ini, key, default):

@@ -558,3 +558,82 @@ def ref_basis_prune(gamma, faillist=()):
     order = np.array([int(l.split("\t")[0]) for l in lines])
     lam = np.array([float(l.split("\t")[4]) for l in lines])
     return order, lam
+
+
+# ------------------------------------------------------------------ data store
+
+FILES_SO = os.path.join(HERE, "_ref", "libmodalfiles.so")
+
+
+class RefFiles:
+    """The reference's data-store sources (parameter.c, fixed_data.c, io.c,
+    arrays.c, basis_functions.c) compiled in place into
+    oracle/_ref/libmodalfiles.so, with the iniparser, GSL-spline and MPI
+    stand-ins of refshim/files_glue.c.  One INI file at a time: the reference
+    keeps its state in globals."""
+
+    def __init__(self, path=FILES_SO):
+        if not os.path.exists(path):
+            if build_ref() is None:
+                raise FileNotFoundError("reference checkout not present; oracle/_ref cannot be built")
+        L = ctypes.CDLL(path)
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        for name, args in [("files_init", [ctypes.c_char_p]), ("files_names", [ctypes.c_char_p, i]),
+                           ("files_terms", [vp] * 6), ("files_spectra", [i, i, vp]), ("files_basis", [vp, vp]),
+                           ("files_qtilde", [vp] * 6)]:
+            fn = getattr(L, name)
+            fn.restype, fn.argtypes = i, args
+        self.L = L
+
+    def load(self, ini_path):
+        """initilise(ini): parameters and file names (parameter.c)."""
+        with quiet_stdout():
+            if self.L.files_init(ini_path.encode()) != 0:
+                raise ValueError(f"initilise({ini_path}) failed")
+
+    def names(self):
+        buf = ctypes.create_string_buffer(1 << 16)
+        if self.L.files_names(buf, len(buf)) != 0:
+            raise ValueError("file-name buffer too small")
+        return dict(line.split("=", 1) for line in buf.value.decode().splitlines())
+
+    def terms(self, N, pol):
+        """set_terms_prim + set_terms_late: {prim, ttt[, tte, tee, eee], pmax_prim, pmax_T, pmax_E}."""
+        a = {k: np.zeros((N, 3), dtype=np.int32) for k in ("prim", "ttt", "tte", "tee", "eee")}
+        pm = np.zeros(3, dtype=np.int32)
+        with quiet_stdout():
+            self.L.files_terms(*[_p(a[k]) for k in ("prim", "ttt", "tte", "tee", "eee")], _p(pm))
+        if not pol:
+            for k in ("tte", "tee", "eee"):
+                del a[k]
+        a.update(pmax_prim=int(pm[0]), pmax_T=int(pm[1]), pmax_E=int(pm[2]))
+        return a
+
+    def spectra(self, lmax, lens, tl):
+        """load_cl + load_BN (+ load_lens, load_TL): [11][lmax+1] (see files_glue.c)."""
+        out = np.zeros((11, lmax + 1))
+        with quiet_stdout():
+            if self.L.files_spectra(int(lens), int(tl), _p(out)) != 0:
+                raise ValueError("spectrum tables rejected")
+        return out
+
+    def basis(self, Tsize, PT, Esize=0, PE=0):
+        """create_basis_late: basis_late_T [Tsize][PT] (and basis_late_E)."""
+        bt, be = np.zeros((Tsize, PT)), np.zeros((max(Esize, 1), max(PE, 1)))
+        with quiet_stdout():
+            self.L.files_basis(_p(bt), _p(be))
+        return bt, (be if Esize else None)
+
+    def qtilde(self, P, pol):
+        """read_qtilde: {x, lvec_T, qt_T [P][lsize][xsize] (and E)}."""
+        sizes = np.zeros(3, dtype=np.int32)
+        with quiet_stdout():
+            self.L.files_qtilde(_p(sizes), None, None, None, None, None)
+        LT, LE, X = (int(v) for v in sizes)
+        x, lt, qt = np.zeros(X), np.zeros(LT, dtype=np.int32), np.zeros((P, LT, X))
+        le, qe = np.zeros(max(LE, 1), dtype=np.int32), np.zeros((P, max(LE, 1), X))
+        self.L.files_qtilde(_p(sizes), _p(x), _p(lt), _p(qt), _p(le), _p(qe))
+        out = {"x": x, "lvec_T": lt, "qt_T": qt}
+        if pol:
+            out.update(lvec_E=le, qt_E=qe)
+        return out

@@ -19,6 +19,7 @@ import modal_gb300 as M  # noqa: E402
 import oracle as O  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, OUT)
 
 
 def inputs_digest(q, tr, cl):
@@ -246,6 +247,48 @@ def gamma_3d_golden():
     print("gamma_3d done")
 
 
+def files_golden():
+    """14. The reference's data-store code on the synthetic inputs of
+    tests/golden/files_inputs.py, one INI case per order_late (1-10): file
+    names (initilise), mode lists (set_terms_prim, set_terms_late), spectra
+    (load_cl, load_BN, load_lens, load_TL), basis tables (create_basis_late)
+    and the transfer files read back (read_qtilde; written by
+    modal_files.write_qtilde).  Directory prefixes are stored as {DIR}/."""
+    import json
+    import shutil
+
+    import modal_files as mf
+    from files_inputs import CASES, qtilde_tables, write_case
+    ref = O.RefFiles()
+    out = {}
+    for name, cs in CASES.items():
+        ol, op, pol, lens, tmin, tmax, emin, emax, terms, absolute = cs
+        d = f"/tmp/mfg_{name}/"
+        shutil.rmtree(d, ignore_errors=True)
+        os.makedirs(d)
+        ini = write_case(d, name)
+        ref.load(ini)
+        out[f"{name}_names"] = np.array(json.dumps({k: v.replace(d, "{DIR}/") for k, v in ref.names().items()}))
+        t = ref.terms(terms, pol)
+        for k in ("prim", "ttt", "tte", "tee", "eee"):
+            if k in t:
+                out[f"{name}_{k}"] = t[k]
+        out[f"{name}_pmax"] = np.array([t["pmax_prim"], t["pmax_T"], t["pmax_E"]])
+        x, qt, qe = qtilde_tables(name, t["pmax_prim"] + 1)
+        mf.write_qtilde(mf.read_ini(ini), x, qt, qe if pol else None)
+        out[f"{name}_spectra"] = ref.spectra(tmax, True, True)
+        bt, be = ref.basis(tmax - tmin + 1, t["pmax_T"] + 1, (emax - emin + 1) if pol else 0, t["pmax_E"] + 1)
+        out[f"{name}_basis_T"] = bt
+        if pol:
+            out[f"{name}_basis_E"] = be
+        q = ref.qtilde(t["pmax_prim"] + 1, pol)
+        for k, v in q.items():
+            out[f"{name}_q_{k}"] = v
+        shutil.rmtree(d, ignore_errors=True)
+    np.savez_compressed(os.path.join(OUT, "files_ref.npz"), **out)
+    print("files_ref done")
+
+
 def basis_families_golden():
     """13. basis_functions.c's families (legendre, fourier, sinlog, bi) on
     l = 2..700 and on a grid that starts at 0 (sinlog's small-value branch)."""
@@ -273,6 +316,8 @@ if __name__ == "__main__":
         gamma_3d_golden()
     elif sys.argv[1:] == ["basis"]:
         basis_families_golden()
+    elif sys.argv[1:] == ["files"]:
+        files_golden()
     else:
         main()
         prune_golden()
@@ -281,3 +326,4 @@ if __name__ == "__main__":
         prim_golden()
         gamma_3d_golden()
         basis_families_golden()
+        files_golden()

@@ -3,11 +3,17 @@
 arrays.c, io.c and set_terms_late; the GPU driver end to end is in
 test_gpu_files.py."""
 import os
+import sys
 
 import numpy as np
 import pytest
 
 import modal_files as mf
+
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+from files_inputs import CASES, qtilde_tables, write_case, write_spectrum_tables  # noqa: E402
+
+write_spectrum_files = write_spectrum_tables  # also used by the GPU driver tests
 
 INI = """
 ; comment line
@@ -294,27 +300,6 @@ def test_basis_late_columns(tmp_path, case):
         mf.basis_late(mf.read_ini(os.fspath(tmp_path / "c.ini")), 8)
 
 
-def write_spectrum_files(d, lmax, step=1, lmin_tab=2):
-    """Synthetic reference-format tables: lensed and scalar cls (D_l), TT/EE
-    beam-and-noise files and a pixel window, tabulated every `step` l."""
-    l = np.arange(lmin_tab, lmax + 5, step, dtype=np.float64)
-    dl = 1e3 * np.exp(-(l / 900.0) ** 2) * (1 + 0.1 * np.sin(l / 17.0))
-    lens = np.stack([l, dl, 0.05 * dl, 0.01 * dl, 0.3 * dl * np.cos(l / 9.0)], 1)
-    scal = np.stack([l, dl, 0.05 * dl, 0.3 * dl, 0.2 * dl, 1e-3 * dl * l], 1)
-    with open(os.path.join(d, "lensed.txt"), "w") as f:
-        f.write("# l TT EE BB TE\n")
-        np.savetxt(f, lens)
-    np.savetxt(os.path.join(d, "scalar.txt"), scal)
-    np.savetxt(os.path.join(d, "bn_t.txt"), np.stack([l, np.exp(-l * l * 1e-6), 1e-5 + 0 * l], 1))
-    np.savetxt(os.path.join(d, "bn_e.txt"), np.stack([l, np.exp(-l * l * 2e-6), 3e-5 + 0 * l], 1))
-    lp = np.arange(0, lmax + 5, dtype=np.float64)
-    np.savetxt(os.path.join(d, "pixw.txt"), np.stack([lp, 1.0 - 1e-5 * lp], 1))
-    lt = np.arange(0, lmax + 5, step, dtype=np.float64)  # load_TL evaluates from l = 1
-    np.savetxt(os.path.join(d, "tl.txt"), np.stack([lt, 1.0 / (1.0 + lt / 500.0)], 1))
-    return ("cls_lensed_file = lensed.txt\ncls_scalar_file = scalar.txt\nBN_TT_file = bn_t.txt\n"
-            "BN_EE_file = bn_e.txt\npixw_file = pixw.txt\ntransfer_wgt_file = tl.txt\n")
-
-
 def test_load_spectra_tables(tmp_path):
     """load_cl / load_BN / load_lens / load_TL: D_l -> 2 pi D_l/(l(l+1)) on the
     tabulated l exactly, natural-spline values in between (scipy's natural
@@ -370,3 +355,79 @@ def test_basis_late_order5_uses_t_wgt_by_row(tmp_path):
     x = T * (T + 1) / (100 * 101.0)
     z, wv = math.sqrt(x), math.pow((2 * T + 1) / 201.0, 1 / 6)
     assert np.allclose(B[i, 6:], [tw[i], wv / z, wv * z, tw[i] * wv / z, tw[i] * wv * z], rtol=1e-15, atol=0)
+
+
+SPEC_ROWS = ["cl_tt", "cl_te", "cl_ee", "beam_tt", "beam_te", "beam_ee", "noise_tt", "noise_te", "noise_ee", "cl_tp",
+             "t_wgt"]
+
+
+def _close(a, b, rtol):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    fin = np.isfinite(b)
+    assert np.array_equal(np.isfinite(a), fin) and np.array_equal(a[~fin], b[~fin])  # l = 0 of a D_l table: inf
+    scale = np.max(np.abs(b[fin])) if fin.any() else 1.0
+    assert np.max(np.abs(a[fin] - b[fin]), initial=0.0) <= rtol * scale
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_data_store_matches_reference(tmp_path, golden, name):
+    """modal_files against the reference's own parameter.c / fixed_data.c / io.c
+    compiled in place (golden, one INI case per order_late 1-10): file names,
+    mode lists and pmax values identical; spectra to 1e-13 (the two natural
+    splines round differently); basis tables identical for the Legendre,
+    Fourier and sin-log families and their closed-form columns (1e-13 where the
+    spectra enter), the 'bi' family to 1e-12; transfer files read back
+    identical."""
+    import json
+    g = golden("files_ref")
+    ol, op, pol, lens, tmin, tmax, emin, emax, terms, absolute = CASES[name]
+    d = str(tmp_path) + "/"
+    ini = mf.read_ini(write_case(d, name))
+    # file names
+    ref_names = json.loads(str(g[f"{name}_names"]))
+    ours = {k: v for k, v in mf.output_names(ini).items()}
+    pn = mf.proj_names(ini)
+    ours.update(proj_T_data=pn["T_data"], proj_E_data=pn["E_data"], proj_T_size=pn["T_size"], proj_E_size=pn["E_size"],
+                pixw=mf._ini_path(ini, "model:pixw_file", ""), BN_TT=mf._ini_path(ini, "model:BN_TT_file", ""),
+                BN_EE=mf._ini_path(ini, "model:BN_EE_file", ""),
+                transfer_wgt=mf._ini_path(ini, "model:transfer_wgt_file", ""))
+    for k, v in ref_names.items():
+        assert ours[k].replace(d, "{DIR}/") == v, (k, ours[k], v)
+    # mode lists
+    lo = mf.late_orders(ini, terms)
+    prim, pmax_prim = mf.prim_order(ini, terms)
+    assert np.array_equal(prim, g[f"{name}_prim"]) and np.array_equal(lo["ttt"], g[f"{name}_ttt"])
+    for k in ("tte", "tee", "eee") if pol else ():
+        assert np.array_equal(lo[k], g[f"{name}_{k}"]), k
+    assert [pmax_prim, lo["pmax_T"], lo["pmax_E"]] == g[f"{name}_pmax"].tolist()
+    # spectra
+    sp = mf.load_spectra(ini, lens=True, tl=True)
+    ref = g[f"{name}_spectra"]
+    for r, k in enumerate(SPEC_ROWS):
+        if k in sp:
+            v = np.zeros(tmax + 1)
+            v[:min(tmax + 1, sp[k].size)] = sp[k][:tmax + 1]
+            _close(v, ref[r], 1e-13)
+    # basis tables
+    B, E = mf.basis_late(ini, lo["pmax_T"], lo["pmax_E"] if pol else None, sp)
+    rb = g[f"{name}_basis_T"]
+    if ol == 10:  # row 0 of columns pmax-3, pmax-2: left uninitialised by the reference
+        rb = rb.copy()
+        rb[0, -4:-2] = B[0, -4:-2]
+    if ol in (1, 2, 3, 7):
+        _close(B, rb, 1e-12)
+    elif ol in (5, 6):
+        _close(B, rb, 1e-13)
+    else:
+        assert np.array_equal(B, rb)
+    if pol:
+        _close(E, g[f"{name}_basis_E"], 1e-12)
+    # transfer files: written by write_qtilde, read by the reference's read_qtilde and by ours
+    x, qt, qe = qtilde_tables(name, pmax_prim + 1)
+    mf.write_qtilde(ini, x, qt, qe if pol else None)
+    q = mf.read_qtilde(ini, pmax_prim)
+    assert np.array_equal(q["x"], g[f"{name}_q_x"]) and np.array_equal(q["lvec_T"], g[f"{name}_q_lvec_T"])
+    assert np.array_equal(q["qt_T"], g[f"{name}_q_qt_T"].transpose(2, 0, 1))
+    if pol:
+        assert np.array_equal(q["qt_E"], g[f"{name}_q_qt_E"].transpose(2, 0, 1))

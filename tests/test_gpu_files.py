@@ -183,11 +183,11 @@ def test_drivers_from_ini_only(mg, tmp_path, order_late):
     closed-form columns; 6: Fourier plus eight, scaled by the spectra), take
     the mode lists from the INI's order files (extra-function triples put in)
     and the spectra from its cls / BN / pixel-window tables (load_spectra)."""
-    from test_files import write_spectrum_files
+    from files_inputs import write_spectrum_tables
     lmax, N, xsize = 80, 15, 21
     raw = mf._order_case2(40)
     np.savetxt(tmp_path / "ttt.txt", raw, fmt="%d")
-    keys = write_spectrum_files(str(tmp_path), lmax, step=1, lmin_tab=0)
+    keys = write_spectrum_tables(str(tmp_path), lmax, step=1, lmin_tab=0)
     ini = tmp_path / "run.ini"
     ini.write_text(f"[model]\ndirectory = {tmp_path}/\nT_lmin = 2\nT_lmax = {lmax}\ndelta_phi = 0.9\n"
                    f"order_TTT_file_late = ttt.txt\n{keys}[basis]\nterms = {N}\norder_late = {order_late}\n"

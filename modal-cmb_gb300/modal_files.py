@@ -20,12 +20,14 @@ later stages read:
   ortho_late(ini_path, basis_t, ...) -> ortho_late_mpi.c's outputs from the GPU
   gamma_late(ini_path, basis_t, ...) -> gamma_mpi.c's gamma_XXX files from the GPU
   modes_late(ini_path, basis_t, ...) -> eigenmodetoday_mpi.c's modes_TTT_<model> files
+  prune_late(ini_path, ...)          -> basis_optimisation_mpi.c's elimination order, printed
 
 Command line:
   python modal_files.py ortho_late <ini> [<basis_T.unf> --pt P] [--basis-e <basis_E.unf> --pe PE] [--split]
   python modal_files.py gamma_late <ini> [<basis_T.unf> --pt P] [--cl <cl_total.unf>]
       [--basis-e <basis_E.unf> --pe PE --spec9 <spec9.unf>]
   python modal_files.py modes_late <ini> [<basis_T.unf> --pt P] [--cl <cl_total.unf>] --tab <shape.npy> --model M
+  python modal_files.py prune_late <ini> [--gamma <gamma.unf>] [--faillist <faillist.txt>]
 Mode lists come from the INI file as set_terms_late builds them.  Basis files
 are raw FP64 [L][P] tables (basis_late_T / basis_late_E layouts,
 fixed_data.c:1764); without one the drivers build create_basis_late's table;
@@ -968,6 +970,70 @@ def modes_late(ini_path, basis_t, cl_total, shapes, models, prec=None, device=0,
     return written, alpha, modes_r
 
 
+def load_txt_int(path, columns=1):
+    """load_txt_int (io.c:28-60): '#' lines skipped, the first `columns`
+    numbers of every other line as (int)strtod (a blank line reads as zeros).
+    A missing file gives an empty list (the reference reports the error and
+    reads nothing)."""
+    if not os.path.exists(path):
+        return np.zeros((0, columns), dtype=np.int32)
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.startswith("#"):
+                continue
+            toks = line.split()[:columns]
+            rows.append([int(_atof(t)) for t in toks] + [0] * (columns - len(toks)))
+    return np.array(rows, dtype=np.int32).reshape(-1, columns)
+
+
+def prune_late(ini_path, gamma_path=None, faillist_path=None, out=None, device=0):
+    """basis_optimisation_mpi.c on the GPU: greedy elimination of the late
+    modes that keeps the smallest eigenvalue of the normalised Gamma largest.
+    Gamma is read raw [N][N] from gamma_path (the reference reads a
+    master_orthol_TTT_<T_lmax>_<E_lmax>_<order_late>_<terms>.unf file under a
+    site path; its name under model:directory is the default here) and the
+    modes listed in faillist_path (default faillist_TTT_<T_lmax>_<order_late>_
+    <terms>.txt there; absent: none) are left out.  Prints the reference's lines
+    (basis_optimisation_mpi.c:141-176, 326-343): the left-out and active modes,
+    then per elimination "index i j k lambda_min time" and the survivor with
+    1 and 0.  Returns (order, lambda_min)."""
+    import time
+
+    import modal_gb300 as mg
+    out = sys.stdout if out is None else out
+    ini = read_ini(ini_path)
+    p = _params(ini)
+    N = p["terms"]
+    tri = mode_order(ini, N)
+    d = p["directory"]
+    tag = f"{p['T_lmax']}_{p['order_late']}_{N}"
+    gamma_path = gamma_path or f"{d}master_orthol_TTT_{p['T_lmax']}_{p['E_lmax']}_{p['order_late']}_{N}.unf"
+    faillist_path = faillist_path or f"{d}faillist_TTT_{tag}.txt"
+    G = array_read(gamma_path, N * N).reshape(N, N)
+    fail = load_txt_int(faillist_path)[:, 0][:N]
+    active = [n for n in range(N) if n not in set(fail.tolist())]
+    print(f"terms: {N}", file=out)
+    print(f"modes complete\t{fail.size}", file=out)
+    for n in fail.tolist():
+        print("%d\t%d\t%d\t%d" % (n, *tri[n]), file=out)
+    print(f"modes active\t{len(active)}", file=out)
+    for n in active:
+        print("%d\t%d\t%d\t%d" % (n, *tri[n]), file=out)
+    print("starting reduction", file=out)
+    t0 = time.perf_counter()
+    with mg.Context(device) as c:
+        order, lam = c.basis_prune(G, fail)
+    dt = (time.perf_counter() - t0) / max(1, order.size - 1)
+    for r in range(order.size - 1):
+        n = int(order[r])
+        print("%d\t%d\t%d\t%d\t%e\t%e" % (n, *tri[n], lam[r], dt), file=out)
+    if order.size:
+        n = int(order[-1])
+        print("%d\t%d\t%d\t%d\t%e\t%e" % (n, *tri[n], 1.0, 0.0), file=out)
+    return order, lam
+
+
 BASIS_HELP = "raw FP64 [L_T][P_T] (needs --pt); omitted: create_basis_late's table for basis:order_late"
 CL_HELP = "raw FP64 C_l + N_l/b_l^2 over l = 0..T_lmax; omitted: from the INI's cls/BN/pixel-window files"
 
@@ -990,6 +1056,10 @@ def main(argv=None):
     g.add_argument("--basis-e", help="raw FP64 [L_E][P_E]")
     g.add_argument("--pe", type=int, help="P_E")
     g.add_argument("--spec9", help="raw FP64 [9][T_lmax+1] spectra, beams and noise")
+    pr = sub.add_parser("prune_late", help="greedy mode elimination (basis_optimisation_mpi), printed")
+    pr.add_argument("ini")
+    pr.add_argument("--gamma", help="raw FP64 [N][N] Gamma (default: master_orthol_TTT_... under model:directory)")
+    pr.add_argument("--faillist", help="modes to leave out, one per line (default: faillist_TTT_... there)")
     m = sub.add_parser("modes_late", help="modes of a separable shape with the orthol/lambdal files, modes_TTT written")
     m.add_argument("ini")
     m.add_argument("basis_t", nargs="?", help=BASIS_HELP)
@@ -998,6 +1068,9 @@ def main(argv=None):
     m.add_argument("--tab", required=True, help=".npy separable shape table [T][3][T_lmax+1]")
     m.add_argument("--model", type=int, required=True, help="model number in the output name")
     a = ap.parse_args(argv)
+    if a.cmd == "prune_late":
+        prune_late(a.ini, a.gamma, a.faillist)
+        return
     if a.basis_t is not None and a.pt is None:
         ap.error("a basis file needs --pt")
     bt = array_read(a.basis_t).reshape(-1, a.pt) if a.basis_t is not None else None

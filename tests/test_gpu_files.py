@@ -224,3 +224,28 @@ def test_drivers_from_ini_only(mg, tmp_path, order_late):
     assert np.array_equal(o, o2)
     assert np.array_equal(gam, (lam.T @ lam) @ G)
     assert np.array_equal(modes, a[0])
+
+
+def test_prune_late_driver_matches_prune(mg, golden, tmp_path):
+    """prune_late: Gamma and the left-out list from the files the reference's
+    pruning driver reads, the elimination order equal to the reference's own
+    driver (golden), printed as its lines."""
+    import io
+    g = golden("basis_prune")
+    G, fail, want = g["gamma_a"], g["fail_a"], g["order_a"]
+    N = G.shape[0]
+    ini = tmp_path / "p.ini"
+    ini.write_text(f"[model]\ndirectory = {tmp_path}/\nT_lmax = 100\nE_lmax = 90\n[basis]\nterms = {N}\n"
+                   f"order_late = 2\n")
+    mf.array_write(os.fspath(tmp_path / f"master_orthol_TTT_100_90_2_{N}.unf"), G)
+    (tmp_path / f"faillist_TTT_100_2_{N}.txt").write_text("".join(f"{int(v)}\n" for v in fail))
+    buf = io.StringIO()
+    order, lam = mf.prune_late(os.fspath(ini), out=buf)
+    assert np.array_equal(order, want)
+    lines = buf.getvalue().splitlines()
+    tri = mf.mode_order(mf.read_ini(os.fspath(ini)), N)
+    assert lines[1] == f"modes complete\t{len(fail)}"
+    steps = [ln.split("\t") for ln in lines[lines.index("starting reduction") + 1:]]
+    assert [int(s[0]) for s in steps] == want.tolist()
+    assert all([int(v) for v in s[1:4]] == tri[int(s[0])].tolist() for s in steps)
+    assert float(steps[-1][4]) == 1.0

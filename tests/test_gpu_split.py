@@ -129,3 +129,28 @@ def test_split_projection_vs_fp64(mg, lmin, lmax, P, S):
     tol = 1e-6 if P <= 32 else 2e-6
     for s in range(S):
         assert rel_fro(bs[s], b64[s]) <= tol, (s, rel_fro(bs[s], b64[s]))
+
+
+def test_split_cfg5_largest_config(mg):
+    """The largest configuration, l <= 2500, P = 40 (N = 11480, n_mu = 3751):
+    split Gamma within 1e-6 of FP64 (relative Frobenius and max), symmetric and
+    reproducible; two shapes projected in FP32 within the P = 40 bound (2e-6)
+    of FP64."""
+    lmax, P = 2500, 40
+    q, tr, cl = mg.workload(lmax, P)
+    shapes = mg.separable_shapes(lmax, 1, seed=51, tmin=2, tmax=2) + mg.bump_shapes(1, seed=52)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        c.init_glint()
+        G64 = c.gamma(mg.PREC_FP64)
+        Gs = c.gamma(mg.PREC_SPLIT)
+        Gs2 = c.gamma(mg.PREC_SPLIT)
+        b64 = c.project(shapes, mg.PREC_FP64)
+        bs = c.project(shapes, mg.PREC_SPLIT)
+    assert G64.shape == (11480, 11480)
+    assert rel_fro(Gs, G64) <= 1e-6 and rel_max(Gs, G64) <= 1e-6
+    assert np.array_equal(Gs, Gs.T) and np.array_equal(Gs, Gs2)
+    for s in range(2):
+        assert rel_fro(bs[s], b64[s]) <= 2e-6, (s, rel_fro(bs[s], b64[s]))

@@ -527,7 +527,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                 for (int s = 0; s < SG; s++)
 #pragma unroll
                     for (int cc = 0; cc < CPL; cc++) hA[s][cc] = hB[s][cc] = 0.f;
-#pragma unroll 4
+#pragma unroll 8
                 for (int t = 0; t < nt; t++) {
                     const int kt = kstart + 2 * (kb + t);
                     const float *qrow = qf + (size_t)(kt - lmin) * P;
@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                 for (int x = 0; x < 4; x++)
 #pragma unroll
                     for (int y = 0; y < 4; y++) acc[x][y] = 0.f;
-#pragma unroll 4
+#pragma unroll 16
                 for (int r = 0; r < JC; r++) {
                     const float4 qv = *reinterpret_cast<const float4 *>(&Qs[r][bt * 4]);
                     const float4 hv = *reinterpret_cast<const float4 *>(&Hs[r][sx][ct * 4]);

@@ -381,7 +381,7 @@ __device__ __forceinline__ float shape_f(const FShape &s, const float *__restric
 //   al_t = f_t(i) g_t(j) + f_t(j) g_t(i), be_t = f_t(i) h_t(j) + f_t(j) h_t(i),
 //   ga_t = g_t(i) h_t(j) + g_t(j) h_t(i),
 // so the per-point work is three table reads and three FMAs per term.
-constexpr int PJ_TCOEF = 8;  // terms per shape with precomputed row coefficients
+constexpr int PJ_TCOEF = 4;  // terms per shape with precomputed row coefficients (more: shape_f)
 
 __device__ __forceinline__ float3 sep_row_coef(const FShape &s, const float *__restrict__ tab, int H, int t, int i, int j)
 {
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
     __shared__ __align__(16) float Hs[JC][SG][CW];
     __shared__ __align__(16) float Qs[JC][CW];  // q_b(j) of the chunk's rows, zero beyond P and lmax
     __shared__ FShape sh[SG];
-    __shared__ float3 coef[8][2][SG][PJ_TCOEF];  // row coefficients of separable shapes per (warp, row)
+    __shared__ float4 coef[8][2][SG][PJ_TCOEF];  // row coefficients of separable shapes per (warp, row), one 16-byte load
     __shared__ int item;
     // F_i as Kahan pairs, element-major over the fold's 4 x 4 tiles: entry (4x + y) of
     // tile t at [(4x + y) NT + t], so the threads of a warp (consecutive tiles) touch
@@ -483,7 +483,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                 float3 cv = make_float3(0.f, 0.f, 0.f);
                 if (sx < sgv && sh[sx].kind == MODAL_SHAPE_SEPARABLE && t < sh[sx].nterms && j <= lmax)
                     cv = sep_row_coef(sh[sx], tabf, H, t, i, j);
-                coef[warp][row][sx][t] = cv;
+                coef[warp][row][sx][t] = make_float4(cv.x, cv.y, cv.z, 0.f);
             }
             __syncwarp();
             for (int kb = 0; kb < nk; kb += 32) {
@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
                             float accA = 0.f, accB = 0.f;
                             for (int t = 0; t < sp.nterms; t++) {
                                 const float4 T = tab4(sp, tabf, H, t, k);
-                                const float3 cA = coef[warp][0][s][t], cB = coef[warp][1][s][t];
+                                const float4 cA = coef[warp][0][s][t], cB = coef[warp][1][s][t];
                                 accA += fmaf(cA.x, T.z, fmaf(cA.y, T.y, cA.z * T.x)) * (1.f / 6.f);
                                 accB += fmaf(cB.x, T.z, fmaf(cB.y, T.y, cB.z * T.x)) * (1.f / 6.f);
                             }

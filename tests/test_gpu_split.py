@@ -23,7 +23,7 @@ def _both(mg, lmin, lmax, P, triples=None):
 
 
 def test_split_projection_many_term_shapes(mg):
-    """Separable shapes of more than 8 terms take the FP32 kernel's general
+    """Separable shapes of more than 4 terms take the FP32 kernel's general
     evaluation (all nine table values per term), next to few-term and bump
     shapes in the same group: <= 1e-6 against FP64, and the captured batch
     gives the same bits as the direct call."""

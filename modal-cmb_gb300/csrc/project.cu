@@ -78,32 +78,38 @@ __device__ __forceinline__ double trap_w(const RadialArgs &ra, int x)
 
 constexpr int RAD_X0 = 10;  // samples below this index follow the per-point zeroing rule
 
-// The same radial shape with the samples x >= RAD_X0 sum-factorised over the row:
-// there the integrand is linear in q~(k, x), so with the row factors
-//   V[c][x - RAD_X0] = w_x x^2 / 6 (sum over the orderings with q~_{a_c} at k of the
-//                     q~(i, x) q~(j, x) products),
-// the point's share is sum_x sum_c V[c][x] q~_{a_c}(k, x).  The first samples are
-// evaluated per point, with the reference's rule.  V: [3][XH] for this row.
-__device__ double d_radial_rows(const RadialArgs &ra, int n, int i, int j, int k, const double *V, int XH)
+// The same radial shape, sum-factorised over the row.  The integrand of sample x
+// is linear in q~(k, x): with the row factors
+//   U[c][x] = x^2 / 6 (sum over the orderings with q~_{a_c} at k of the
+//             q~(i, x) q~(j, x) products),
+// y_x = sum_c U[c][x] q~_{a_c}(k, x).  The reference drops y_x for x < 10 when
+// |wq_i wq_j wq_k y_x| > 1e-18; where the factorised y_x lies within 1e-10
+// (relative) of that threshold, the decision is taken on y_x summed as the
+// reference sums it.  tw: [X] trapezium weights; U: [3][X] for this row.
+__device__ double d_radial_rows(const RadialArgs &ra, int n, int i, int j, int k, const double *U, const double *tw)
 {
-    const int a1 = ra.prim[3 * n], a2 = ra.prim[3 * n + 1], a3 = ra.prim[3 * n + 2], L1 = ra.L1;
+    const int a1 = ra.prim[3 * n], a2 = ra.prim[3 * n + 1], a3 = ra.prim[3 * n + 2], L1 = ra.L1, X = ra.xsize;
     const double wp = ra.wq[i] * ra.wq[j] * ra.wq[k];
-    const int xl = min(ra.xsize, RAD_X0);
     double r = 0.0;
-    for (int x = 0; x < xl; x++) {
+    for (int x = 0; x < X; x++) {
         const double *qx = ra.qt + (size_t)x * ra.Pp * L1;
-        const double *q1 = qx + (size_t)a1 * L1, *q2 = qx + (size_t)a2 * L1, *q3 = qx + (size_t)a3 * L1;
-        const double p1 = q1[i], p2 = q2[i], p3 = q3[i], p4 = q1[j], p5 = q2[j], p6 = q3[j], p7 = q1[k], p8 = q2[k],
-                     p9 = q3[k];
-        const double sum = p1 * p5 * p9 + p2 * p6 * p7 + p3 * p4 * p8 + p3 * p5 * p7 + p2 * p4 * p9 + p1 * p6 * p8;
-        const double y = ra.x[x] * ra.x[x] * sum * (1.0 / 6.0);
-        if (!(fabs(wp * y) > 1e-18)) r = fma(trap_w(ra, x), y, r);
-    }
-    for (int h = 0; h < XH; h++) {
-        const double *qx = ra.qt + (size_t)(RAD_X0 + h) * ra.Pp * L1;
-        r = fma(V[h], qx[(size_t)a1 * L1 + k], r);
-        r = fma(V[XH + h], qx[(size_t)a2 * L1 + k], r);
-        r = fma(V[2 * XH + h], qx[(size_t)a3 * L1 + k], r);
+        double y = U[x] * qx[(size_t)a1 * L1 + k];
+        y = fma(U[X + x], qx[(size_t)a2 * L1 + k], y);
+        y = fma(U[2 * X + x], qx[(size_t)a3 * L1 + k], y);
+        if (x < RAD_X0) {
+            const double t = fabs(wp * y);
+            bool drop = t > 1e-18;
+            if (t > 1e-18 * (1.0 - 1e-10) && t < 1e-18 * (1.0 + 1e-10)) {
+                const double *q1 = qx + (size_t)a1 * L1, *q2 = qx + (size_t)a2 * L1, *q3 = qx + (size_t)a3 * L1;
+                const double p1 = q1[i], p2 = q2[i], p3 = q3[i], p4 = q1[j], p5 = q2[j], p6 = q3[j], p7 = q1[k],
+                             p8 = q2[k], p9 = q3[k];
+                const double sum =
+                    p1 * p5 * p9 + p2 * p6 * p7 + p3 * p4 * p8 + p3 * p5 * p7 + p2 * p4 * p9 + p1 * p6 * p8;
+                drop = fabs(wp * (ra.x[x] * ra.x[x] * sum * (1.0 / 6.0))) > 1e-18;
+            }
+            if (drop) continue;
+        }
+        r = fma(tw[x], y, r);
     }
     return r;
 }
@@ -217,8 +223,9 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
     extern __shared__ double sm[];
     double *f = sm;               // [JC][KMAX]
     double *H = sm + JC * KMAX;   // [JC][P]
-    double *V = H + JC * P;       // radial shapes: [JC][3][XH] row factors (d_radial_rows)
-    const int XH = max(ra.xsize - RAD_X0, 0);
+    double *V = H + JC * P;       // radial shapes: [JC][3][X] row factors, then [X] trapezium weights
+    const int XR = ra.xsize;
+    double *TW = V + (size_t)JC * 3 * XR;
     const int slab = slab_order[blockIdx.x];
     const int i = lmin + slab;
     const int tid = threadIdx.x;
@@ -231,20 +238,21 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
         for (int t = 0; t < FPT; t++) Facc[t] = 0.0;
         const bool radial = sh.kind == SHAPE_RADIAL;
         for (int j0 = i; j0 <= lmax; j0 += JC) {
-            if (radial && XH > 0) {
+            if (radial) {
                 const int a1 = ra.prim[3 * sh.nterms], a2 = ra.prim[3 * sh.nterms + 1], a3 = ra.prim[3 * sh.nterms + 2];
-                for (int e = tid; e < JC * XH; e += 256) {
-                    const int jj = e / XH, h = e - jj * XH, j = min(j0 + jj, lmax), x = RAD_X0 + h;
+                for (int e = tid; e < JC * XR; e += 256) {
+                    const int jj = e / XR, x = e - jj * XR, j = min(j0 + jj, lmax);
                     const double *qx = ra.qt + (size_t)x * ra.Pp * ra.L1;
                     const double p1 = qx[(size_t)a1 * ra.L1 + i], p2 = qx[(size_t)a2 * ra.L1 + i],
                                  p3 = qx[(size_t)a3 * ra.L1 + i], p4 = qx[(size_t)a1 * ra.L1 + j],
                                  p5 = qx[(size_t)a2 * ra.L1 + j], p6 = qx[(size_t)a3 * ra.L1 + j];
-                    const double g = trap_w(ra, x) * ra.x[x] * ra.x[x] * (1.0 / 6.0);
-                    double *v = V + (size_t)jj * 3 * XH;
-                    v[h] = g * (p2 * p6 + p3 * p5);           // with q~_{a1}(k)
-                    v[XH + h] = g * (p3 * p4 + p1 * p6);      // with q~_{a2}(k)
-                    v[2 * XH + h] = g * (p1 * p5 + p2 * p4);  // with q~_{a3}(k)
+                    const double g = ra.x[x] * ra.x[x] * (1.0 / 6.0);
+                    double *u = V + (size_t)jj * 3 * XR;
+                    u[x] = g * (p2 * p6 + p3 * p5);           // with q~_{a1}(k)
+                    u[XR + x] = g * (p3 * p4 + p1 * p6);      // with q~_{a2}(k)
+                    u[2 * XR + x] = g * (p1 * p5 + p2 * p4);  // with q~_{a3}(k)
                 }
+                for (int x = tid; x < XR; x += 256) TW[x] = trap_w(ra, x);
                 __syncthreads();
             }
             for (int e = tid; e < JC * KMAX; e += 256) {
@@ -254,7 +262,7 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
                     int k = j + par + 2 * kk, k1 = min(i + j, lmax);
                     if (k <= k1)
                         val = Wd[sbase[slab] + tet_row_offset(i, j, lmax) + kk] *
-                              (radial ? d_radial_rows(ra, sh.nterms, i, j, k, V + (size_t)jj * 3 * XH, XH)
+                              (radial ? d_radial_rows(ra, sh.nterms, i, j, k, V + (size_t)jj * 3 * XR, TW)
                                       : d_shape(sh, tab, stride, i, j, k, ra));
                 }
                 f[e] = val;
@@ -989,7 +997,7 @@ extern "C" modal_status modal_gamma_transfer_3d(modal_ctx *c, double deltaphi, d
     pl.ra.Pp = c->tr_Pp;
     pl.ra.L1 = lmax + 1;
     // the row factors of d_radial_rows sit after the kernel's f and H tiles
-    pl.smem += sizeof(double) * (size_t)JC * 3 * std::max(c->tr_xsize - RAD_X0, 0);
+    pl.smem += sizeof(double) * ((size_t)JC * 3 * c->tr_xsize + c->tr_xsize);
     if (pl.smem > 220 * 1024) { set_error("modal_gamma_transfer_3d: lmax=%d, xsize=%d too large for the slab tile", lmax, c->tr_xsize); return MODAL_ERR_ARG; }
     {
         auto attr = [&](auto kern) -> modal_status {

@@ -134,6 +134,25 @@ __device__ __forceinline__ double d_shape(const DShape &s, const double *__restr
     return exp(-(x1 * x1 + x2 * x2 + x3 * x3) / (2.0 * s.sigma * s.sigma));
 }
 
+// A separable shape on a fixed row (i, j), FP64: with the row coefficients
+//   c[t] = (f_t(i) g_t(j) + f_t(j) g_t(i), f_t(i) h_t(j) + f_t(j) h_t(i), g_t(i) h_t(j) + g_t(j) h_t(i))
+// the value at k is (1/6) sum_t (c0 h_t(k) + c1 g_t(k) + c2 f_t(k)): three loads
+// and three FMAs per term instead of the six-ordering sum.
+constexpr int PJ_TCOEF64 = 8;  // terms per shape with row coefficients (more: d_shape)
+
+__device__ __forceinline__ double d_sep_rows(const DShape &s, const double *__restrict__ tab, int stride, int k,
+                                             const double *c)
+{
+    double acc = 0.0;
+    for (int t = 0; t < s.nterms; t++) {
+        const double *f = tab + s.tab_off + (long)t * 3 * stride;
+        acc = fma(c[3 * t], f[2 * stride + k], acc);
+        acc = fma(c[3 * t + 1], f[stride + k], acc);
+        acc = fma(c[3 * t + 2], f[k], acc);
+    }
+    return acc * (1.0 / 6.0);
+}
+
 // v_l = (2l+1)^{-1/3} w_l, w_l = (2l+1)^{1/6}/sqrt(C_l + N_l/b_l^2), w_0 = w_1 = 0
 // (calculate_mode_3D.c:53-62, get_weight :283-290).
 __global__ void k_vl(int lmax, const double *__restrict__ cl, double *__restrict__ vl)
@@ -223,7 +242,8 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
     extern __shared__ double sm[];
     double *f = sm;               // [JC][KMAX]
     double *H = sm + JC * KMAX;   // [JC][P]
-    double *V = H + JC * P;       // radial shapes: [JC][3][X] row factors, then [X] trapezium weights
+    double *Cf = H + JC * P;      // separable shapes: [JC][PJ_TCOEF64][3] row coefficients (d_sep_rows)
+    double *V = Cf + JC * PJ_TCOEF64 * 3;  // radial shapes: [JC][3][X] row factors, then [X] trapezium weights
     const int XR = ra.xsize;
     double *TW = V + (size_t)JC * 3 * XR;
     const int slab = slab_order[blockIdx.x];
@@ -237,7 +257,19 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
 #pragma unroll
         for (int t = 0; t < FPT; t++) Facc[t] = 0.0;
         const bool radial = sh.kind == SHAPE_RADIAL;
+        const bool rowc = sh.kind == MODAL_SHAPE_SEPARABLE && sh.nterms <= PJ_TCOEF64;
         for (int j0 = i; j0 <= lmax; j0 += JC) {
+            if (rowc) {
+                for (int e = tid; e < JC * sh.nterms; e += 256) {
+                    const int jj = e / sh.nterms, t = e - jj * sh.nterms, j = min(j0 + jj, lmax);
+                    const double *f = tab + sh.tab_off + (long)t * 3 * stride, *g = f + stride, *h = g + stride;
+                    double *c = Cf + ((size_t)jj * PJ_TCOEF64 + t) * 3;
+                    c[0] = f[i] * g[j] + f[j] * g[i];  // with h(k)
+                    c[1] = f[i] * h[j] + f[j] * h[i];  // with g(k)
+                    c[2] = g[i] * h[j] + g[j] * h[i];  // with f(k)
+                }
+                __syncthreads();
+            }
             if (radial) {
                 const int a1 = ra.prim[3 * sh.nterms], a2 = ra.prim[3 * sh.nterms + 1], a3 = ra.prim[3 * sh.nterms + 2];
                 for (int e = tid; e < JC * XR; e += 256) {
@@ -263,6 +295,7 @@ __global__ void __launch_bounds__(256) k_project_slab_fp64(int lmin, int lmax, i
                     if (k <= k1)
                         val = Wd[sbase[slab] + tet_row_offset(i, j, lmax) + kk] *
                               (radial ? d_radial_rows(ra, sh.nterms, i, j, k, V + (size_t)jj * 3 * XR, TW)
+                               : rowc ? d_sep_rows(sh, tab, stride, k, Cf + (size_t)jj * PJ_TCOEF64 * 3)
                                       : d_shape(sh, tab, stride, i, j, k, ra));
                 }
                 f[e] = val;
@@ -827,7 +860,7 @@ modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_p
         else MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_f32<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
     } else {
         const int KMAX = (lmax - lmin) / 2 + 2;
-        pl.smem = sizeof(double) * ((size_t)JC * KMAX + (size_t)JC * P);
+        pl.smem = sizeof(double) * ((size_t)JC * KMAX + (size_t)JC * P + (size_t)JC * PJ_TCOEF64 * 3);
         if (pl.smem > 220 * 1024) { set_error("project: lmax=%d too large for the slab tile", lmax); return MODAL_ERR_ARG; }
         pl.fpt = ceil_div(PP, 256);
         if (pl.fpt > 16) { set_error("project: P=%d too large", P); return MODAL_ERR_ARG; }

@@ -255,6 +255,26 @@ def test_projection_edge_sizes_vs_oracle(mg, orc, lmin, lmax, P):
         assert rel_fro(beta[s], bo) <= 1e-12
 
 
+def test_projection_term_counts_vs_oracle(mg, orc):
+    """FP64 separable shapes at the row-coefficient boundary: 1, 8 (row
+    coefficients) and 9 terms (the six-ordering sum) against the oracle, 1e-12,
+    in one call with a bump; odd l_max and l_min > 2."""
+    lmin, lmax, P = 3, 71, 5
+    cl = mg.synthetic_cl(lmax)
+    q = mg.weighted_q(mg.legendre_q(lmin, lmax, P), cl, lmin)
+    tr = mg.mode_triples(P)
+    shapes = (mg.separable_shapes(lmax, 1, seed=31, tmin=1, tmax=1) + mg.separable_shapes(lmax, 1, seed=32, tmin=8, tmax=8)
+              + mg.separable_shapes(lmax, 1, seed=33, tmin=9, tmax=9) + mg.bump_shapes(1, seed=34))
+    assert [sh["tab"].shape[0] for sh in shapes[:3]] == [1, 8, 9]
+    with mg.Context(0) as c:
+        c.set_basis(lmin, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        beta = c.project(shapes)
+    for s, sh in enumerate(shapes):
+        assert rel_fro(beta[s], orc.project(lmin, lmax, q, tr, cl, sh, nthreads=2)) <= 1e-12, s
+
+
 # --------------------------------------------------------------------- alpha
 
 def test_alpha_vs_oracle(mg, orc, golden):

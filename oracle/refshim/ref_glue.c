@@ -154,13 +154,15 @@ double get_noise_TE(int l) { return g_spec ? SPEC(7, l) : 0.0; }
 double get_noise_EE(int l) { return g_spec ? SPEC(8, l) : 0.0; }
 /* GSL cubic-spline link stubs (calculate_gamma() is not exercised) */
 #include <stdio.h>
-const struct refshim_interp_type *gsl_interp_cspline = NULL;
-struct refshim_spline *gsl_spline_alloc(const struct refshim_interp_type *T, size_t n) { (void)T; (void)n; fprintf(stderr, "gsl_spline stub called\n"); abort(); }
-int gsl_spline_init(struct refshim_spline *s, const double xa[], const double ya[], size_t n) { (void)s; (void)xa; (void)ya; (void)n; abort(); }
-double gsl_spline_eval_integ(const struct refshim_spline *s, double a, double b, struct refshim_interp_accel *acc) { (void)s; (void)a; (void)b; (void)acc; abort(); }
-struct refshim_interp_accel *gsl_interp_accel_alloc(void) { abort(); }
-void gsl_interp_accel_free(struct refshim_interp_accel *a) { (void)a; }
-void gsl_spline_free(struct refshim_spline *s) { (void)s; }
+#include "gsl/gsl_spline.h"
+const gsl_interp_type *gsl_interp_cspline = NULL;
+gsl_spline *gsl_spline_alloc(const gsl_interp_type *T, size_t n) { (void)T; (void)n; fprintf(stderr, "gsl_spline stub called\n"); abort(); }
+int gsl_spline_init(gsl_spline *s, const double xa[], const double ya[], size_t n) { (void)s; (void)xa; (void)ya; (void)n; abort(); }
+double gsl_spline_eval_integ(const gsl_spline *s, double a, double b, gsl_interp_accel *acc) { (void)s; (void)a; (void)b; (void)acc; abort(); }
+double gsl_spline_eval(const gsl_spline *s, double x, gsl_interp_accel *acc) { (void)s; (void)x; (void)acc; abort(); }
+gsl_interp_accel *gsl_interp_accel_alloc(void) { abort(); }
+void gsl_interp_accel_free(gsl_interp_accel *a) { (void)a; }
+void gsl_spline_free(gsl_spline *s) { (void)s; }
 int read_eigen(int a, int b, int c) { (void)a; (void)b; (void)c; return 0; }
 double get_eigen(int i) { return i == 0 ? 1.0 : 0.0; }
 double get_cl_TT(int l) { return g_spec ? SPEC(0, l) : g_cl[l]; }

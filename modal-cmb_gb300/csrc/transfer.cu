@@ -133,7 +133,9 @@ __global__ void __launch_bounds__(256) k_mij_transfer(int nmu, int lmin, int lma
 
 // One CTA per 32 (n: primordial) x 32 (m: late) tile; thread (tx, ty) owns
 // n = n0 + tx and m = m0 + ty + 8 r.
-__global__ void __launch_bounds__(256) k_gamma_transfer(int N, int Nprim, int P, int Pp, int nmu, int xsize, int KC,
+// blockIdx.z takes the radial samples [z xs, min(xsize, (z + 1) xs)); its partial
+// sum goes to out + z N Nprim (k_sum_groups adds the groups in a fixed order).
+__global__ void __launch_bounds__(256) k_gamma_transfer(int N, int Nprim, int P, int Pp, int nmu, int xsize, int xs, int KC,
                                                         const int *__restrict__ triples, const int *__restrict__ prim,
                                                         const double *__restrict__ mt2, const double *__restrict__ w,
                                                         const double *__restrict__ xvec, const double *__restrict__ cx,
@@ -154,7 +156,9 @@ __global__ void __launch_bounds__(256) k_gamma_transfer(int N, int Nprim, int P,
         for (int b = 0; b < 3; b++) qm[r][b] = (m < N) ? triples[3 * m + b] : 0;
     }
     double res[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int xi = 0; xi < xsize; xi++) {
+    const int xb = blockIdx.z * xs, xe = min(xsize, xb + xs);
+    out += (size_t)blockIdx.z * N * Nprim;
+    for (int xi = xb; xi < xe; xi++) {
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
         const double *src0 = mt2 + (size_t)xi * nmu * nu;
         for (int k0 = 0; k0 < nmu; k0 += KC) {
@@ -194,6 +198,16 @@ __global__ void __launch_bounds__(256) k_gamma_transfer(int N, int Nprim, int P,
         int m = blockIdx.y * 32 + ty + 8 * r;
         if (m < N) out[(size_t)m * Nprim + n] = res[r] * scale;
     }
+}
+
+// out[e] = sum over the G groups of part[g][e], g ascending (in place: part = out).
+__global__ void k_sum_groups(long n, int G, double *__restrict__ out)
+{
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= n) return;
+    double s = out[e];
+    for (int g = 1; g < G; g++) s += out[(size_t)g * n + e];
+    out[e] = s;
 }
 
 // Polarised points (gamma_2d_pt_TTE/TEE/EEE, calculate_gamma.c:558-687): the
@@ -338,13 +352,28 @@ extern "C" modal_status modal_gamma_transfer(modal_ctx *c, double deltaphi, doub
     const size_t smem = sizeof(double) * ((size_t)KC + (size_t)KC * nu);
     if (smem > 200 * 1024) { set_error("modal_gamma_transfer: Pp*P=%d too large for the tile", nu); return MODAL_ERR_ARG; }
     MODAL_CUDA(cudaFuncSetAttribute(k_gamma_transfer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 gg(ceil_div(Nprim, 32), ceil_div(N, 32));
+    // the (primordial x late) tiles alone fill about two thirds of the SMs at the
+    // benchmark sizes: split the radial samples into groups so that the grid holds
+    // about four CTAs per SM, and add the groups' partial sums afterwards
+    int nsm = 0;
+    MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    const long tiles = (long)ceil_div(Nprim, 32) * ceil_div(N, 32);
+    int XG = (int)std::min<long>(xsize, std::max<long>(1, (4L * nsm + tiles - 1) / tiles));
+    const int xs = ceil_div(xsize, XG);
+    XG = ceil_div(xsize, xs);
+    MODAL_TRY(ensure(c->tr_out, sizeof(double) * (size_t)XG * N * Nprim));
+    dim3 gg(ceil_div(Nprim, 32), ceil_div(N, 32), XG);
     const double scale = deltaphi * deltaphi / (8.0 * 3.14159265358979323846);
-    k_gamma_transfer<<<gg, 256, smem, c->stream>>>(N, Nprim, P, Pp, nmu, xsize, KC, c->triples.as<int>(),
+    k_gamma_transfer<<<gg, 256, smem, c->stream>>>(N, Nprim, P, Pp, nmu, xsize, xs, KC, c->triples.as<int>(),
                                                    c->tr_prim.as<int>(), c->tr_mt.as<double>(), c->w.as<double>(),
                                                    c->tr_x.as<double>(), c->tr_x.as<double>() + xsize, scale,
                                                    c->tr_out.as<double>());
     MODAL_TRY(launched(c, "gamma_transfer"));
+    if (XG > 1) {
+        const long n = (long)N * Nprim;
+        k_sum_groups<<<ceil_div(n, 256), 256, 0, c->stream>>>(n, XG, c->tr_out.as<double>());
+        MODAL_TRY(launched(c, "sum_groups"));
+    }
     t.stop();
     if (gamma_t)
         MODAL_CUDA(cudaMemcpyAsync(gamma_t, c->tr_out.ptr, sizeof(double) * (size_t)N * Nprim, cudaMemcpyDeviceToHost,

@@ -200,13 +200,13 @@ __global__ void __launch_bounds__(256) k_gamma_transfer(int N, int Nprim, int P,
     }
 }
 
-// out[e] = sum over the G groups of part[g][e], g ascending (in place: part = out).
-__global__ void k_sum_groups(long n, int G, double *__restrict__ out)
+// out[e] = sum over the G groups of out[g stride + e], g ascending (in place).
+__global__ void k_sum_groups(long n, int G, long stride, double *__restrict__ out)
 {
     const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= n) return;
     double s = out[e];
-    for (int g = 1; g < G; g++) s += out[(size_t)g * n + e];
+    for (int g = 1; g < G; g++) s += out[(size_t)g * stride + e];
     out[e] = s;
 }
 
@@ -216,7 +216,8 @@ __global__ void k_sum_groups(long n, int G, double *__restrict__ out)
 // table (FORM 3 EEE: all E); its permanent, weighted, summed over mu.
 template <int FORM>
 __global__ void __launch_bounds__(256) k_gamma_transfer_pol(int N, int Nprim, int P, int PE, int Pp, int nmu,
-                                                            int xsize, int KC, const int *__restrict__ triples,
+                                                            int xsize, int xs, long gstride, int KC,
+                                                            const int *__restrict__ triples,
                                                             const int *__restrict__ prim,
                                                             const double *__restrict__ mtT,
                                                             const double *__restrict__ mtE,
@@ -242,7 +243,9 @@ __global__ void __launch_bounds__(256) k_gamma_transfer_pol(int N, int Nprim, in
         for (int b = 0; b < 3; b++) qm[r][b] = (m < N) ? triples[3 * m + b] : 0;
     }
     double res[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int xi = 0; xi < xsize; xi++) {
+    const int xb = blockIdx.z * xs, xe = min(xsize, xb + xs);  // this CTA's radial samples (as k_gamma_transfer)
+    out += (size_t)blockIdx.z * gstride;
+    for (int xi = xb; xi < xe; xi++) {
         double acc[4] = {0.0, 0.0, 0.0, 0.0};
         for (int k0 = 0; k0 < nmu; k0 += KC) {
             const int kc = min(KC, nmu - k0);
@@ -371,7 +374,7 @@ extern "C" modal_status modal_gamma_transfer(modal_ctx *c, double deltaphi, doub
     MODAL_TRY(launched(c, "gamma_transfer"));
     if (XG > 1) {
         const long n = (long)N * Nprim;
-        k_sum_groups<<<ceil_div(n, 256), 256, 0, c->stream>>>(n, XG, c->tr_out.as<double>());
+        k_sum_groups<<<ceil_div(n, 256), 256, 0, c->stream>>>(n, XG, n, c->tr_out.as<double>());
         MODAL_TRY(launched(c, "sum_groups"));
     }
     t.stop();
@@ -462,15 +465,29 @@ extern "C" modal_status modal_gamma_transfer_pol(modal_ctx *c, double deltaphi, 
                                               wq, c->tr_qte.as<double>(), c->tr_mte.as<double>(), wl,
                                               c->tr_qt.as<double>(), c->lmax + 1);
     MODAL_TRY(launched(c, "mij_transfer_e"));
-    dim3 gg(ceil_div(Nprim, 32), ceil_div(N, 32));
+    int nsm = 0;
+    MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
+    const long tiles = (long)ceil_div(Nprim, 32) * ceil_div(N, 32);
+    int XG = (int)std::min<long>(xsize, std::max<long>(1, (4L * nsm + tiles - 1) / tiles));
+    const int xs = ceil_div(xsize, XG);
+    XG = ceil_div(xsize, xs);
+    MODAL_TRY(ensure(c->tr_out, sizeof(double) * 3 * (size_t)XG * NP));  // group g of form f at (3 g + f) NP
+    dim3 gg(ceil_div(Nprim, 32), ceil_div(N, 32), XG);
     const double scale = deltaphi * deltaphi / (8.0 * 3.14159265358979323846);
     auto run = [&](auto kern, int f) -> modal_status {
         MODAL_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        kern<<<gg, 256, smem, c->stream>>>(N, Nprim, P, PE, Pp, nmu, xsize, KC, c->tri_pol.as<int>() + 3 * (size_t)N * f,
+        kern<<<gg, 256, smem, c->stream>>>(N, Nprim, P, PE, Pp, nmu, xsize, xs, 3 * (long)NP, KC,
+                                           c->tri_pol.as<int>() + 3 * (size_t)N * f,
                                            c->tr_prim.as<int>(), c->tr_mt.as<double>(), c->tr_mte.as<double>(),
                                            c->w.as<double>(), c->tr_x.as<double>(), c->tr_x.as<double>() + xsize, scale,
                                            c->tr_out.as<double>() + f * NP);
-        return launched(c, "gamma_transfer_pol");
+        MODAL_TRY(launched(c, "gamma_transfer_pol"));
+        if (XG > 1) {
+            k_sum_groups<<<ceil_div((long)NP, 256), 256, 0, c->stream>>>((long)NP, XG, 3 * (long)NP,
+                                                                          c->tr_out.as<double>() + f * NP);
+            MODAL_TRY(launched(c, "sum_groups"));
+        }
+        return MODAL_OK;
     };
     MODAL_TRY(run(k_gamma_transfer_pol<1>, 0));
     MODAL_TRY(run(k_gamma_transfer_pol<2>, 1));

@@ -357,11 +357,12 @@ extern "C" modal_status modal_gamma_transfer(modal_ctx *c, double deltaphi, doub
     MODAL_CUDA(cudaFuncSetAttribute(k_gamma_transfer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // the (primordial x late) tiles alone fill about two thirds of the SMs at the
     // benchmark sizes: split the radial samples into groups so that the grid holds
-    // about four CTAs per SM, and add the groups' partial sums afterwards
+    // about 16 CTAs per SM (measured: 4 -> 67 ms, 8 -> 59 ms, 16 -> 57 ms at l <= 600),
+    // and add the groups' partial sums afterwards
     int nsm = 0;
     MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     const long tiles = (long)ceil_div(Nprim, 32) * ceil_div(N, 32);
-    int XG = (int)std::min<long>(xsize, std::max<long>(1, (4L * nsm + tiles - 1) / tiles));
+    int XG = (int)std::min<long>(xsize, std::max<long>(1, (16L * nsm + tiles - 1) / tiles));
     const int xs = ceil_div(xsize, XG);
     XG = ceil_div(xsize, xs);
     MODAL_TRY(ensure(c->tr_out, sizeof(double) * (size_t)XG * N * Nprim));
@@ -468,7 +469,7 @@ extern "C" modal_status modal_gamma_transfer_pol(modal_ctx *c, double deltaphi, 
     int nsm = 0;
     MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c->device));
     const long tiles = (long)ceil_div(Nprim, 32) * ceil_div(N, 32);
-    int XG = (int)std::min<long>(xsize, std::max<long>(1, (4L * nsm + tiles - 1) / tiles));
+    int XG = (int)std::min<long>(xsize, std::max<long>(1, (16L * nsm + tiles - 1) / tiles));
     const int xs = ceil_div(xsize, XG);
     XG = ceil_div(xsize, xs);
     MODAL_TRY(ensure(c->tr_out, sizeof(double) * 3 * (size_t)XG * NP));  // group g of form f at (3 g + f) NP

@@ -85,7 +85,10 @@ typedef enum {
     MODAL_T_LIFT = 7,     /* split form: the tensor-core GEMM of the mu-contraction alone */
     MODAL_T_ADJOINT = 8,  /* gradients with respect to the basis values */
     MODAL_T_PRUNE = 9,    /* greedy basis pruning */
-    MODAL_T_COUNT = 10
+    MODAL_T_EIG_TRD = 10, /* eigensolver: Householder tridiagonalisation */
+    MODAL_T_EIG_DC = 11,  /* eigensolver: divide and conquer on the tridiagonal matrix */
+    MODAL_T_EIG_BACK = 12, /* eigensolver: back-transformation of the kept eigenvectors */
+    MODAL_T_COUNT = 13
 } modal_timer;
 modal_status modal_ctx_profile(modal_ctx *ctx, int enable);
 modal_status modal_ctx_timer(modal_ctx *ctx, int timer, double *ms, long *count);
@@ -244,6 +247,16 @@ modal_status modal_set_ortho(modal_ctx *ctx, const double *orthol, const double 
  * relative error of Gamma (about 1e-7 for the split form) makes alpha
  * reproducible.  Takes effect at the next modal_orthogonalise. */
 modal_status modal_set_pca_floor(modal_ctx *ctx, double floor);
+
+/* Eigen-decomposition of the symmetric n x n matrix a (host, row-major; only
+ * read): every eigenvalue in ascending order in w[n], and, when v is not NULL,
+ * the eigenvectors as rows of v[n][n] (row j belongs to w[j]).  FP64 on the
+ * GPU (Householder tridiagonalisation, divide and conquer, back-
+ * transformation).  Replaces gsl_eigen_symmv + gsl_eigen_symmv_sort
+ * (ortho_late_mpi.c:775-776, which sorts descending) and LAPACKE_dsyevr
+ * (basis_optimisation_mpi.c:279); the PCA branch of modal_orthogonalise and
+ * modal_basis_prune use the same solver. */
+modal_status modal_eigh(modal_ctx *ctx, int n, const double *a, double *w, double *v);
 
 /* Batched projection replayed from a captured CUDA graph.  Same inputs,
  * result and FP64/FP32 forms as modal_project (beta: host [S][N], required;

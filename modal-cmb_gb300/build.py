@@ -63,7 +63,7 @@ def build(verbose=False):
         raise RuntimeError("nvcc failed for: " + ", ".join(os.path.basename(f) for f in failed))
     objs = [os.path.join(BUILD, os.path.basename(s)[:-3] + ".o") for s in sources]
     if _newer(objs, LIB):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcusolver"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

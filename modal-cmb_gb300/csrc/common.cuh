@@ -101,7 +101,7 @@ struct modal_ctx {
     // primordial k-space side (prim.cu): grid offsets, basis, chunk buffers
     modal::DevBuf prim;
     double *h_info = nullptr;  // pinned readback
-    void *solver = nullptr;    // cusolverDn handle on `stream`, made on first use (eig.cu)
+    modal::DevBuf eigw;        // eigensolver workspace (syev.cu)
 
     // profiling: event pairs per stage, summed on read
     bool profile = false;
@@ -114,8 +114,12 @@ namespace modal {
 
 modal_status ensure(DevBuf &b, size_t bytes);
 void release(DevBuf &b);
-modal_status solver_handle(modal_ctx *ctx, void **h);  // eig.cu
-void solver_release(modal_ctx *ctx);
+// FP64 symmetric eigen-decomposition (syev.cu).  A [n][n] (device, row-major,
+// overwritten); W [n] ascending; select(W_host, n, arg, &first) -> number of
+// eigenvectors wanted from ascending index first on; V rows hold them.
+typedef int (*SyevSelect)(const double *w, int n, void *arg, int *first);
+modal_status syev_dev(modal_ctx *ctx, int n, double *A, double *W, double *V, SyevSelect select, void *arg,
+                      int *nvec, int *first);
 
 #define MODAL_CUDA(call)                                                                  \
     do {                                                                                  \

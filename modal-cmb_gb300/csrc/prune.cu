@@ -16,10 +16,10 @@
 // smallest root lies in (lambda_1, lambda_2) (interlacing), where g_m increases
 // from -inf to +inf, so bisection on delta = mu - lambda_1 in (0, lambda_2 -
 // lambda_1) finds it to the last bit; with V[m][1] = 0 or lambda_1 = lambda_2 it
-// is lambda_1 itself.  Per step: one cusolverDnDsyevd of size n (FP64) and one
-// warp per candidate for the root, O(n^3) instead of the reference's O(n^4).
+// is lambda_1 itself.  Per step: one eigen-decomposition of size n (the
+// library's own FP64 eigensolver, syev.cu) and one warp per candidate for the
+// root, O(n^3) instead of the reference's O(n^4).
 // The argmax and the list update run on the host, exactly as the reference's.
-#include <cusolverDn.h>
 #include <vector>
 #include "common.cuh"
 
@@ -56,8 +56,8 @@ __device__ __forceinline__ double warp_sum(double v)
 }
 
 // One warp per candidate m: smallest eigenvalue of the minor without m.
-// V: eigenvectors from syevd, column-major [n][n] (V[m + i*n] = component m of
-// eigenvector i), W: eigenvalues ascending.  n == 2: the 1x1 minor's entry.
+// V: eigenvectors as rows [n][n] (V[m + i*n] = component m of eigenvector i),
+// W: eigenvalues ascending.  n == 2: the 1x1 minor's entry.
 __global__ void k_prune_secular(int n, int N, const double *__restrict__ V, const double *__restrict__ W,
                                 const double *__restrict__ Ahat, const int *__restrict__ list,
                                 double *__restrict__ lam)
@@ -110,17 +110,11 @@ __global__ void k_lmin_upstream(int N, const double *__restrict__ gamma, const d
     G[e] = g;
 }
 
-struct Solver {
-    cusolverDnHandle_t h = nullptr;
-};
-
-// the context's cached handle (made on first use, bound to its stream)
-modal_status get_solver(modal_ctx *c, Solver &sv)
+// every eigenvector (pruning reads them all)
+int select_all(const double *, int n, void *, int *first)
 {
-    void *hv = nullptr;
-    MODAL_TRY(solver_handle(c, &hv));
-    sv.h = static_cast<cusolverDnHandle_t>(hv);
-    return MODAL_OK;
+    *first = 0;
+    return n;
 }
 
 }  // namespace
@@ -158,50 +152,31 @@ modal_status modal_basis_prune(modal_ctx *c, int N, const double *gamma, int nfa
     MODAL_CUDA(cudaSetDevice(c->device));
     StageTimer t(c, MODAL_T_PRUNE);
     const size_t NN = (size_t)N * N, nn0 = (size_t)n0 * n0;
-    Solver sv;
-    MODAL_TRY(get_solver(c, sv));
-    int lwork = 0;
-    if (n0 > 2 && cusolverDnDsyevd_bufferSize(sv.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n0, nullptr, n0,
-                                              nullptr, &lwork) != CUSOLVER_STATUS_SUCCESS) {
-        set_error("syevd_bufferSize failed");
-        return MODAL_ERR_CUDA;
-    }
-    // layout: Ahat [N][N] | gamma copy [N][N] | A [n0][n0] | W [n0] | lam [n0] | work [lwork] | info, list [n0]
-    const size_t o_ahat = 0, o_g = o_ahat + NN, o_a = o_g + NN, o_w = o_a + nn0, o_lam = o_w + n0, o_work = o_lam + n0,
-                 o_end = o_work + (size_t)lwork;
+    // layout: Ahat [N][N] | gamma copy [N][N] | A [n0][n0] | V [n0][n0] | W [n0] | lam [n0] | list [n0]
+    const size_t o_ahat = 0, o_g = o_ahat + NN, o_a = o_g + NN, o_v = o_a + nn0, o_w = o_v + nn0, o_lam = o_w + n0,
+                 o_end = o_lam + n0;
     MODAL_TRY(ensure(c->prune, sizeof(double) * o_end + sizeof(int) * (2 + (size_t)n0) + 256));
     double *base = c->prune.as<double>();
-    double *Ahat = base + o_ahat, *A = base + o_a, *W = base + o_w, *lam = base + o_lam, *work = base + o_work;
-    int *dinfo = reinterpret_cast<int *>(base + o_end), *dlist = dinfo + 2;
+    double *Ahat = base + o_ahat, *A = base + o_a, *Vv = base + o_v, *W = base + o_w, *lam = base + o_lam;
+    int *dlist = reinterpret_cast<int *>(base + o_end) + 2;
     const double *g = gamma ? base + o_g : c->gamma.as<double>();
     if (gamma) MODAL_CUDA(cudaMemcpyAsync(base + o_g, gamma, sizeof(double) * NN, cudaMemcpyHostToDevice, c->stream));
     k_prune_normalise<<<ceil_div((long)NN, 256), 256, 0, c->stream>>>(N, g, Ahat);
     MODAL_TRY(launched(c, "prune_normalise"));
     std::vector<double> hl(n0);
-    int hinfo = 0;
     int step = 0;
     for (int n = n0; n >= 2; n--, step++) {
         MODAL_CUDA(cudaMemcpyAsync(dlist, list.data(), sizeof(int) * n, cudaMemcpyHostToDevice, c->stream));
         if (n > 2) {
-            int need = 0;
-            if (cusolverDnDsyevd_bufferSize(sv.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, nullptr, n,
-                                            nullptr, &need) != CUSOLVER_STATUS_SUCCESS ||
-                need > lwork) {
-                set_error("modal_basis_prune: syevd workspace for n=%d (%d) exceeds the reserved %d", n, need, lwork);
-                return MODAL_ERR_CUDA;
-            }
             k_prune_gather<<<ceil_div((long)n * n, 256), 256, 0, c->stream>>>(n, N, Ahat, dlist, A);
             MODAL_TRY(launched(c, "prune_gather"));
-            const cusolverStatus_t cs = cusolverDnDsyevd(sv.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, A,
-                                                         n, W, work, lwork, dinfo);
-            if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return MODAL_ERR_CUDA; }
+            int nv = 0, first = 0;
+            MODAL_TRY(syev_dev(c, n, A, W, Vv, select_all, nullptr, &nv, &first));
         }
-        k_prune_secular<<<ceil_div((long)n * 32, 256), 256, 0, c->stream>>>(n, N, A, W, Ahat, dlist, lam);
+        k_prune_secular<<<ceil_div((long)n * 32, 256), 256, 0, c->stream>>>(n, N, Vv, W, Ahat, dlist, lam);
         MODAL_TRY(launched(c, "prune_secular"));
         MODAL_CUDA(cudaMemcpyAsync(hl.data(), lam, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-        if (n > 2) MODAL_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         MODAL_CUDA(cudaStreamSynchronize(c->stream));
-        if (hinfo != 0) { set_error("modal_basis_prune: syevd info=%d at %d active modes", hinfo, n); return MODAL_ERR_NOCONV; }
         // first maximum (basis_optimisation_mpi.c:287-297)
         int index = 0;
         double best = hl[0];
@@ -224,38 +199,25 @@ modal_status modal_lambda_min(modal_ctx *c, double *lambda_min, double *eigvec, 
     const int N = c->N;
     const size_t NN = (size_t)N * N;
     StageTimer t(c, MODAL_T_ADJOINT);
-    Solver sv;
-    MODAL_TRY(get_solver(c, sv));
-    int lwork = 0;
-    if (cusolverDnDsyevd_bufferSize(sv.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, nullptr, N, nullptr,
-                                    &lwork) != CUSOLVER_STATUS_SUCCESS) {
-        set_error("syevd_bufferSize failed");
-        return MODAL_ERR_CUDA;
-    }
-    // layout: A [N][N] | G [N][N] | W [N] | work | dq [L][P] | info
+    // layout: A [N][N] | G [N][N] | V [N][N] | W [N] | dq [L][P]
     const size_t LP = (size_t)c->L * c->P;
-    const size_t o_a = 0, o_gu = NN, o_w = 2 * NN, o_work = o_w + N, o_dq = o_work + lwork, o_end = o_dq + LP;
+    const size_t o_a = 0, o_gu = NN, o_v = 2 * NN, o_w = 3 * NN, o_dq = o_w + N, o_end = o_dq + LP;
     MODAL_TRY(ensure(c->prune, sizeof(double) * o_end + 64));
     double *base = c->prune.as<double>();
-    double *A = base + o_a, *G = base + o_gu, *W = base + o_w, *dq = base + o_dq;
-    int *dinfo = reinterpret_cast<int *>(base + o_end);
+    double *A = base + o_a, *G = base + o_gu, *Vv = base + o_v, *W = base + o_w, *dq = base + o_dq;
     k_prune_normalise<<<ceil_div((long)NN, 256), 256, 0, c->stream>>>(N, c->gamma.as<double>(), A);
     MODAL_TRY(launched(c, "prune_normalise"));
-    const cusolverStatus_t cs = cusolverDnDsyevd(sv.h, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, N, A, N, W,
-                                                 base + o_work, lwork, dinfo);
-    if (cs != CUSOLVER_STATUS_SUCCESS) { set_error("cusolverDnDsyevd failed (%d)", (int)cs); return MODAL_ERR_CUDA; }
+    int nv = 0, first = 0;
+    MODAL_TRY(syev_dev(c, N, A, W, Vv, select_all, nullptr, &nv, &first));
     double lam = 0.0;
-    int hinfo = 0;
     MODAL_CUDA(cudaMemcpyAsync(&lam, W, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    MODAL_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MODAL_CUDA(cudaStreamSynchronize(c->stream));
-    if (hinfo != 0) { set_error("modal_lambda_min: syevd info=%d", hinfo); return MODAL_ERR_NOCONV; }
     *lambda_min = lam;
-    // eigenvector of the smallest eigenvalue: column 0 of the column-major result
-    if (eigvec) MODAL_CUDA(cudaMemcpyAsync(eigvec, A, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
+    // eigenvector of the smallest eigenvalue: row 0 of the result
+    if (eigvec) MODAL_CUDA(cudaMemcpyAsync(eigvec, Vv, sizeof(double) * N, cudaMemcpyDeviceToHost, c->stream));
     if (dlam_dq) {
         if (!c->have_glint) { set_error("modal_lambda_min: no quadrature state for the gradient"); return MODAL_ERR_STATE; }
-        k_lmin_upstream<<<ceil_div((long)NN, 256), 256, 0, c->stream>>>(N, c->gamma.as<double>(), A, lam, G);
+        k_lmin_upstream<<<ceil_div((long)NN, 256), 256, 0, c->stream>>>(N, c->gamma.as<double>(), Vv, lam, G);
         MODAL_TRY(launched(c, "lmin_upstream"));
         MODAL_CUDA(cudaMemsetAsync(dq, 0, sizeof(double) * LP, c->stream));
         MODAL_TRY(gamma_vjp_accum_dev(c, G, dq));

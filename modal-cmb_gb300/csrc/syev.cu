@@ -1,0 +1,1036 @@
+// syev.cu -- FP64 symmetric eigen-decomposition on the GPU, the library's own.
+//
+// It stands in for the reference's gsl_eigen_symmv + gsl_eigen_symmv_sort
+// (ortho_late_mpi.c:775-776, PCA branch :784-805) and LAPACKE_dsyevr
+// (basis_optimisation_mpi.c:279).  Three stages, all FP64:
+//
+// 1. Householder tridiagonalisation A = Q T Q^T (lower, blocked; the algorithm
+//    of LAPACK's dsytrd/dlatrd).  Each panel of TRD_NB columns is one
+//    cooperative launch, one CTA per SM, whose CTAs meet at a software grid
+//    barrier twice per column: (a) finish the previous column's w vector and
+//    update the next column with the panel's rank-2c correction, reduce its
+//    norm; (b) form the reflector and the product y = A v over the trailing
+//    matrix (the FP64 matrix-vector product that bounds this stage).  The
+//    panel's compact-WY factor T (dlarft, forward) is built from the same
+//    inner products.  After a panel, A22 -= V W^T + W V^T on the lower
+//    triangle by the tiled FP64 GEMM, mirrored to the upper one.
+// 2. Divide and conquer on T (Cuppen; Dongarra-Sorensen deflation; Gu-Eisenstat
+//    eigenvectors).  The tree is split down to single rows; every level's
+//    merges run batched: sort and deflate (one CTA per merge), secular roots
+//    (one warp per root, rational two-pole steps safeguarded by bisection),
+//    zhat and the eigenvectors of the rank-one problem (one warp per row),
+//    then the vector update as a grouped FP64 GEMM.
+// 3. Back-transformation of the wanted eigenvectors, X <- X Q^T, by the
+//    panels' compact-WY blocks in reverse order (FP64 GEMMs).
+//
+// Layout: row-major; eigenvectors are stored as rows (row j of V is the
+// eigenvector of W[j]).  Every spin-wait is bounded; on expiry a device error
+// word is set and every CTA returns (MODAL_ERR_TIMEOUT on the host).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+#include "common.cuh"
+
+namespace modal {
+
+namespace {
+
+constexpr int TRD_NB = 32;                 // panel width
+constexpr int TRD_THREADS = 512;           // 16 warps per CTA
+constexpr int TRD_WARPS = TRD_THREADS / 32;
+constexpr int PCOMP = 2 * TRD_NB + 2;      // partial components: p[NB], q[NB], y.v, |x|^2
+constexpr long long BAR_CYCLES = 1ll << 32;  // ~2 s of clock64 per barrier wait
+constexpr double EPS = 1.1102230246251565e-16;  // 2^-53
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_prod(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v *= __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Software grid barrier for a cooperative launch (all CTAs co-resident).
+// bar[0] counts arrivals, bar[1] is the generation.  Bounded: a wait that runs
+// out of its clock64 budget sets *err; every CTA returns false once *err is set.
+__device__ bool grid_barrier(unsigned *bar, int *err)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g) {
+                if (*(volatile int *)err) break;
+                if (clock64() - t0 > BAR_CYCLES) {
+                    atomicExch(err, 1);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int *)err == 0;
+}
+
+// Rows [lo, hi) split in equal contiguous parts over the grid.
+__device__ __forceinline__ void my_rows(int lo, int hi, int &r0, int &r1)
+{
+    const int cnt = hi - lo;
+    const int per = (cnt + (int)gridDim.x - 1) / (int)gridDim.x;
+    r0 = min(hi, lo + (int)blockIdx.x * per);
+    r1 = min(hi, r0 + per);
+}
+
+// ------------------------------------------------------------------ stage 1
+
+struct TrdArgs {
+    double *A;
+    int n, j0, nbp;
+    double *V, *W;  // panel: [n][TRD_NB] row-major, zero outside the reflectors
+    double *T;      // [TRD_NB][TRD_NB] upper-triangular compact-WY factor
+    double *d, *e, *tau;
+    double *a, *y;  // [n] work vectors
+    double *part;   // [PCOMP][grid] per-CTA partial sums
+    unsigned *bar;
+    int *err;
+};
+
+// Sum over the grid of component `comp` of the partials, by one warp (fixed order).
+__device__ __forceinline__ double grid_total(const double *part, int comp, int lane)
+{
+    double s = 0.0;
+    const double *p = part + (size_t)comp * gridDim.x;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += p[b];
+    return warp_sum(s);
+}
+
+__global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
+{
+    extern __shared__ double sv[];  // v of the current column, indexed from row i+1
+    __shared__ double s_pq[2 * TRD_NB + 2];
+    __shared__ double s_vi[TRD_NB], s_wi[TRD_NB];
+    __shared__ double s_red[TRD_WARPS];
+    __shared__ double s_scal[4];
+
+    const int n = g.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int G = gridDim.x;
+    for (int c = 0; c <= g.nbp; c++) {
+        const int i = g.j0 + c;  // column reduced now; head row of reflector c - 1
+        int r0, r1;
+        my_rows(i, n, r0, r1);
+        // ---------------- phase X: finish w of column c - 1, update column i
+        if (c > 0) {
+            const int cp = c - 1;
+            const int ncomp = 2 * cp + 1;
+            for (int t = warp; t < ncomp; t += TRD_WARPS) {
+                const int comp = t < cp ? t : (t < 2 * cp ? TRD_NB + (t - cp) : 2 * TRD_NB);
+                const double v = grid_total(g.part, comp, lane);
+                if (lane == 0) s_pq[t] = v;  // p[0..cp), q[0..cp), y.v
+            }
+            __syncthreads();
+            const double taup = g.tau[i - 1];
+            if (tid == 0) {
+                double pq = 0.0;
+                for (int t = 0; t < cp; t++) pq += s_pq[t] * s_pq[cp + t];
+                s_scal[0] = s_pq[2 * cp] - 2.0 * pq;  // (corrected y).v
+            }
+            __syncthreads();
+            const double yvc = s_scal[0];
+            const double *p = s_pq, *q = s_pq + cp;
+            // w of row i (head row), computed by every CTA alike
+            if (tid == 0) {
+                double s = g.y[i];
+                for (int t = 0; t < cp; t++) s -= g.V[(size_t)i * TRD_NB + t] * q[t] + g.W[(size_t)i * TRD_NB + t] * p[t];
+                s_scal[1] = taup * s - 0.5 * taup * taup * yvc * 1.0;
+            }
+            if (blockIdx.x == 0) {
+                // T[0:cp, cp] = -tau T[0:cp, 0:cp] p ; T[cp][cp] = tau  (dlarft, forward columnwise)
+                for (int t = tid; t < cp; t += blockDim.x) {
+                    double s = 0.0;
+                    for (int u = t; u < cp; u++) s += g.T[t * TRD_NB + u] * p[u];
+                    g.T[t * TRD_NB + cp] = -taup * s;
+                }
+                if (tid == 0) g.T[cp * TRD_NB + cp] = taup;
+            }
+            __syncthreads();
+            const double whead = s_scal[1];
+            // rows of this CTA: w (stored), then the column update of column i
+            if (c < g.nbp) {
+                for (int t = tid; t < c; t += blockDim.x) {
+                    s_vi[t] = g.V[(size_t)i * TRD_NB + t];
+                    s_wi[t] = (t == cp) ? whead : g.W[(size_t)i * TRD_NB + t];
+                }
+            }
+            __syncthreads();
+            double nrm = 0.0;
+            for (int r = r0 + tid; r < r1; r += blockDim.x) {
+                double s = g.y[r];
+                const double *Vr = g.V + (size_t)r * TRD_NB, *Wr = g.W + (size_t)r * TRD_NB;
+                for (int t = 0; t < cp; t++) s -= Vr[t] * q[t] + Wr[t] * p[t];
+                const double wr = (r == i) ? whead : taup * s - 0.5 * taup * taup * yvc * Vr[cp];
+                g.W[(size_t)r * TRD_NB + cp] = wr;
+                if (c < g.nbp) {
+                    double x = g.A[(size_t)r * n + i];
+                    for (int t = 0; t < cp; t++) x -= Vr[t] * s_wi[t] + Wr[t] * s_vi[t];
+                    x -= Vr[cp] * whead + wr * s_vi[cp];
+                    g.a[r] = x;
+                    if (r >= i + 2) nrm += x * x;
+                }
+            }
+            if (c == g.nbp) break;
+            nrm = warp_sum(nrm);
+            if (lane == 0) s_red[warp] = nrm;
+            __syncthreads();
+            if (tid == 0) {
+                double s = 0.0;
+                for (int w = 0; w < TRD_WARPS; w++) s += s_red[w];
+                g.part[(size_t)(2 * TRD_NB + 1) * G + blockIdx.x] = s;
+            }
+        } else {
+            double nrm = 0.0;
+            for (int r = r0 + tid; r < r1; r += blockDim.x) {
+                const double x = g.A[(size_t)r * n + i];
+                g.a[r] = x;
+                if (r >= i + 2) nrm += x * x;
+            }
+            nrm = warp_sum(nrm);
+            if (lane == 0) s_red[warp] = nrm;
+            __syncthreads();
+            if (tid == 0) {
+                double s = 0.0;
+                for (int w = 0; w < TRD_WARPS; w++) s += s_red[w];
+                g.part[(size_t)(2 * TRD_NB + 1) * G + blockIdx.x] = s;
+            }
+        }
+        if (!grid_barrier(g.bar, g.err)) return;
+
+        // ---------------- phase Y: reflector of column i, y = A v on the trailing matrix
+        if (warp == 0) {
+            const double sig = grid_total(g.part, 2 * TRD_NB + 1, lane);
+            if (lane == 0) {
+                const double alpha = g.a[i + 1];
+                double beta, tau, scale;
+                if (sig == 0.0) {
+                    beta = alpha; tau = 0.0; scale = 0.0;
+                } else {
+                    beta = -copysign(sqrt(alpha * alpha + sig), alpha);
+                    tau = (beta - alpha) / beta;
+                    scale = 1.0 / (alpha - beta);
+                }
+                s_scal[2] = scale;
+                if (blockIdx.x == 0) {
+                    g.d[i] = g.a[i];
+                    g.e[i] = beta;
+                    g.tau[i] = tau;
+                }
+            }
+        }
+        __syncthreads();
+        const double scale = s_scal[2];
+        const int m = n - i - 1;  // trailing size
+        for (int k = tid; k < m; k += blockDim.x) sv[k] = (k == 0) ? 1.0 : g.a[i + 1 + k] * scale;
+        __syncthreads();
+        my_rows(i + 1, n, r0, r1);
+        // warp per row: y[r] = sum_k A[r][i+1+k] v[k]
+        for (int r = r0 + warp; r < r1; r += TRD_WARPS) {
+            const double *Ar = g.A + (size_t)r * n + i + 1;
+            double s0 = 0.0, s1 = 0.0;
+            int k = lane;
+            for (; k + 32 < m; k += 64) {
+                s0 = fma(Ar[k], sv[k], s0);
+                s1 = fma(Ar[k + 32], sv[k + 32], s1);
+            }
+            if (k < m) s0 = fma(Ar[k], sv[k], s0);
+            const double s = warp_sum(s0 + s1);
+            if (lane == 0) {
+                g.y[r] = s;
+                g.V[(size_t)r * TRD_NB + c] = sv[r - i - 1];
+            }
+        }
+        __syncthreads();
+        // partials over this CTA's rows: p_t = V[:,t].v, q_t = W[:,t].v (t < c), y.v
+        const int ncomp = 2 * c + 1;
+        for (int t = warp; t < ncomp; t += TRD_WARPS) {
+            double s = 0.0;
+            for (int r = r0 + lane; r < r1; r += 32) {
+                const double vr = sv[r - i - 1];
+                const double x = t < c ? g.V[(size_t)r * TRD_NB + t]
+                                       : (t < 2 * c ? g.W[(size_t)r * TRD_NB + (t - c)] : g.y[r]);
+                s += x * vr;
+            }
+            s = warp_sum(s);
+            const int comp = t < c ? t : (t < 2 * c ? TRD_NB + (t - c) : 2 * TRD_NB);
+            if (lane == 0) g.part[(size_t)comp * G + blockIdx.x] = s;
+        }
+        if (!grid_barrier(g.bar, g.err)) return;
+    }
+}
+
+// Upper triangle of the trailing block [s, n) x [s, n) := its lower triangle.
+__global__ void k_mirror_lower(double *A, int n, int s)
+{
+    __shared__ double tile[32][33];
+    const int tr = blockIdx.y, tc = blockIdx.x;  // tile row, tile column (upper: tc >= tr)
+    if (tc < tr) return;
+    const int r0 = s + tr * 32, c0 = s + tc * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+    // read the transposed source tile: rows c0.., columns r0..
+    for (int k = ty; k < 32; k += 8) {
+        const int rr = c0 + k, cc = r0 + tx;
+        tile[k][tx] = (rr < n && cc < n) ? A[(size_t)rr * n + cc] : 0.0;
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        const int rr = r0 + k, cc = c0 + tx;
+        if (rr < n && cc < n && cc > rr) A[(size_t)rr * n + cc] = tile[tx][k];
+    }
+}
+
+__global__ void k_copy_last_diag(const double *A, int n, double *d)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)];
+}
+
+// ------------------------------------------------------------------ stage 2
+
+struct MergeInfo {
+    int a, m, b;                 // segment [a, b) = [a, m) + [m, b)
+    int kk, k1, k2, nd, ng;      // kept (non-deflated): k1 supported on the first half only, k2 on
+                                 // both (rotated across the halves), the rest on the second half;
+                                 // deflated; rotations
+    double rho;
+};
+
+__global__ void k_dc_leaves(int n, const double *__restrict__ d, const double *__restrict__ e, double *__restrict__ lam)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = d[i];
+    if (i > 0) v -= fabs(e[i - 1]);
+    if (i < n - 1) v -= fabs(e[i]);
+    lam[i] = v;
+}
+
+__global__ void k_dc_eye(int n, double *Z)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * n) return;
+    Z[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
+}
+
+struct DcWork {
+    double *lam, *Z, *Zn, *U, *Zc, *e;
+    int n;
+    int *srt;        // [n] sorted slot -> source row
+    double *Ds, *zs; // [n] sorted values and z after deflation
+    int *kl;         // [n] kept j -> sorted slot (ascending)
+    int *kci;        // [n] kept j -> grouped column (first-half, both-halves, second-half support)
+    int *flg;        // [n] sorted slot -> support: 1 first half, 2 second half, 3 both
+    int *dl;         // [n] deflated t -> sorted slot
+    int2 *grot;      // [n] rotations (slot p, slot q)
+    double2 *gcs;    // [n] (c, s)
+    double *kd, *kw; // [n] kept values and z, compact
+    int *org;        // [n] root j -> origin kept index
+    double *rtau;    // [n] root j -> offset from its origin
+    double *zh;      // [n] zhat of kept j
+    int *rank;       // [n] root j (pos a+j) / deflated t (pos a+kk+t) -> final position in [a, b)
+    MergeInfo *mi;   // per merge of the level
+    int *pos2m;      // [n] position -> merge index of the level
+    int *err;
+};
+
+// Sort, deflate and compact one merge (one CTA per merge).
+__global__ void __launch_bounds__(256) k_dc_deflate(DcWork w)
+{
+    MergeInfo &M = w.mi[blockIdx.x];
+    const int a = M.a, m = M.m, b = M.b, k = b - a, n = w.n;
+    const int tid = threadIdx.x;
+    const double em = w.e[m - 1];
+    const double rho = 2.0 * fabs(em);
+    const double sg = em >= 0.0 ? 1.0 : -1.0;
+    const double rs = 0.70710678118654752440;
+    // merge the two ascending halves (stable: ties take the first half first)
+    for (int t = tid; t < k; t += blockDim.x) {
+        const int src = a + t;
+        const double v = w.lam[src];
+        int lo, hi, rk;
+        if (src < m) {
+            lo = m; hi = b;  // count of second-half values < v
+            while (lo < hi) { const int md = (lo + hi) >> 1; if (w.lam[md] < v) lo = md + 1; else hi = md; }
+            rk = (src - a) + (lo - m);
+        } else {
+            lo = a; hi = m;  // count of first-half values <= v
+            while (lo < hi) { const int md = (lo + hi) >> 1; if (w.lam[md] <= v) lo = md + 1; else hi = md; }
+            rk = (src - m) + (lo - a);
+        }
+        w.srt[a + rk] = src;
+        w.flg[a + rk] = src < m ? 1 : 2;
+        w.Ds[a + rk] = v;
+        w.zs[a + rk] = (src < m ? w.Z[(size_t)src * n + (m - 1)] : sg * w.Z[(size_t)src * n + m]) * rs;
+    }
+    __syncthreads();
+    __shared__ double s_mx[2][8];
+    double dm = 0.0, zm = 0.0;
+    for (int t = tid; t < k; t += blockDim.x) {
+        dm = fmax(dm, fabs(w.Ds[a + t]));
+        zm = fmax(zm, fabs(w.zs[a + t]));
+    }
+    dm = warp_max(dm);
+    zm = warp_max(zm);
+    if ((tid & 31) == 0) { s_mx[0][tid >> 5] = dm; s_mx[1][tid >> 5] = zm; }
+    __syncthreads();
+    if (tid != 0) return;
+    for (int t = 1; t < (int)(blockDim.x >> 5); t++) { dm = fmax(dm, s_mx[0][t]); zm = fmax(zm, s_mx[1][t]); }
+    const double tol = 8.0 * EPS * fmax(dm, zm);
+    int kk = 0, nd = 0, ng = 0;
+    double *D = w.Ds + a, *z = w.zs + a;
+    if (rho * zm <= tol) {
+        for (int s = 0; s < k; s++) w.dl[a + nd++] = a + s;
+    } else {
+        int pj = -1;
+        for (int nj = 0; nj < k; nj++) {
+            if (rho * fabs(z[nj]) <= tol) { w.dl[a + nd++] = a + nj; continue; }
+            if (pj < 0) { pj = nj; continue; }
+            double s = z[pj], c = z[nj];
+            const double tau = hypot(c, s);
+            const double t = D[nj] - D[pj];
+            c /= tau;
+            s = -s / tau;
+            if (fabs(t * c * s) <= tol) {
+                w.flg[a + nj] |= w.flg[a + pj];  // the rotated vector has support on both halves
+                z[nj] = tau;
+                z[pj] = 0.0;
+                w.grot[a + ng] = make_int2(a + pj, a + nj);
+                w.gcs[a + ng] = make_double2(c, s);
+                ng++;
+                const double t2 = D[pj] * c * c + D[nj] * s * s;
+                D[nj] = D[pj] * s * s + D[nj] * c * c;
+                D[pj] = t2;
+                w.dl[a + nd++] = a + pj;
+                pj = nj;
+            } else {
+                w.kl[a + kk++] = a + pj;
+                pj = nj;
+            }
+        }
+        if (pj >= 0) w.kl[a + kk++] = a + pj;
+    }
+    // compact kept values; grouped columns: first-half support, both halves, second half
+    int k1 = 0, k2 = 0;
+    for (int j = 0; j < kk; j++) {
+        const int f = w.flg[w.kl[a + j]];
+        k1 += (f == 1);
+        k2 += (f == 3);
+    }
+    int cg[4] = {0, 0, k1 + k2, k1};
+    for (int j = 0; j < kk; j++) {
+        const int sl = w.kl[a + j];
+        w.kd[a + j] = w.Ds[sl];
+        w.kw[a + j] = w.zs[sl];
+        w.kci[a + j] = cg[w.flg[sl]]++;
+    }
+    M.kk = kk; M.k1 = k1; M.k2 = k2; M.nd = nd; M.ng = ng; M.rho = rho;
+}
+
+// Apply the deflation rotations of each merge to its eigenvector rows (one
+// thread per component column; rotations in order).
+__global__ void k_dc_rotate(DcWork w)
+{
+    const MergeInfo M = w.mi[blockIdx.y];
+    const int col = M.a + blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= M.b || M.ng == 0) return;
+    const int n = w.n;
+    for (int r = 0; r < M.ng; r++) {
+        const int2 pq = w.grot[M.a + r];
+        const double2 cs = w.gcs[M.a + r];
+        double *xp = w.Z + (size_t)w.srt[pq.x] * n + col, *xq = w.Z + (size_t)w.srt[pq.y] * n + col;
+        const double x = *xp, y = *xq;
+        *xp = cs.x * x + cs.y * y;
+        *xq = cs.x * y - cs.y * x;
+    }
+}
+
+// Secular roots: one warp per position p; root j = p - a of the merge holding p.
+__global__ void __launch_bounds__(256) k_dc_secular(DcWork w)
+{
+    const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (p >= w.n) return;
+    const int mix = w.pos2m[p];
+    if (mix < 0) return;
+    const MergeInfo M = w.mi[mix];
+    const int j = p - M.a, kk = M.kk;
+    if (j >= kk) return;
+    const double *dl = w.kd + M.a, *z = w.kw + M.a;
+    const double rho = M.rho;
+    int o;
+    double lo, hi;
+    if (kk == 1) {
+        if (lane == 0) { w.org[M.a] = 0; w.rtau[M.a] = rho * z[0] * z[0]; }
+        return;
+    }
+    if (j < kk - 1) {
+        const double half = 0.5 * (dl[j + 1] - dl[j]);
+        double s = 0.0;
+        for (int i = lane; i < kk; i += 32) s += z[i] * z[i] / ((dl[i] - dl[j]) - half);
+        s = warp_sum(s);
+        const double fmid = 1.0 + rho * s;
+        if (fmid >= 0.0) { o = j; lo = 0.0; hi = half; }
+        else { o = j + 1; lo = -half; hi = 0.0; }
+    } else {
+        double s = 0.0;
+        for (int i = lane; i < kk; i += 32) s += z[i] * z[i];
+        s = warp_sum(s);
+        o = kk - 1; lo = 0.0; hi = rho * s;
+    }
+    const double dorg = dl[o];
+    double tau = 0.5 * (lo + hi);
+    for (int it = 0; it < 100; it++) {
+        double psi = 0.0, phi = 0.0, dpsi = 0.0, dphi = 0.0;
+        for (int i = lane; i < kk; i += 32) {
+            const double dlt = (dl[i] - dorg) - tau;
+            const double t = z[i] * z[i] / dlt;
+            if (i <= j) { psi += t; dpsi += t / dlt; }
+            else { phi += t; dphi += t / dlt; }
+        }
+        psi = rho * warp_sum(psi);
+        phi = rho * warp_sum(phi);
+        dpsi = rho * warp_sum(dpsi);
+        dphi = rho * warp_sum(dphi);
+        const double f = 1.0 + psi + phi;
+        if (f < 0.0) lo = tau; else hi = tau;
+        if (fabs(f) <= 8.0 * EPS * (1.0 + fabs(psi) + fabs(phi))) break;
+        if (hi - lo <= 4.0 * EPS * fmax(fabs(lo), fabs(hi))) break;
+        double tn = 0.0;
+        bool ok = false;
+        if (j < kk - 1) {
+            const double Dj = (dl[j] - dorg) - tau, Dj1 = (dl[j + 1] - dorg) - tau;
+            const double cc = f - Dj * dpsi - Dj1 * dphi;
+            const double s1 = Dj * Dj * dpsi, s2 = Dj1 * Dj1 * dphi;
+            const double A = cc, B = cc * (Dj + Dj1) + s1 + s2, C = cc * Dj * Dj1 + s1 * Dj1 + s2 * Dj;
+            double eta = 0.0;
+            bool have = false;
+            if (fabs(A) <= EPS * fabs(B)) {
+                if (B != 0.0) { eta = C / B; have = true; }
+            } else {
+                const double disc = B * B - 4.0 * A * C;
+                if (disc >= 0.0) {
+                    const double r1 = (B + copysign(sqrt(disc), B)) / (2.0 * A);
+                    const double r2 = (r1 != 0.0) ? C / (A * r1) : 0.0;
+                    const bool in1 = (r1 > Dj && r1 < Dj1), in2 = (r2 > Dj && r2 < Dj1);
+                    if (in1 && in2) { eta = fabs(r1) < fabs(r2) ? r1 : r2; have = true; }
+                    else if (in1) { eta = r1; have = true; }
+                    else if (in2) { eta = r2; have = true; }
+                }
+            }
+            if (have) { tn = tau + eta; ok = true; }
+        } else {
+            const double Dk = (dl[kk - 1] - dorg) - tau;
+            const double cc = f - Dk * dpsi;
+            if (cc > 0.0) { tn = tau + Dk + Dk * Dk * dpsi / cc; ok = true; }
+        }
+        if (!ok || !(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
+        tau = tn;
+    }
+    if (lane == 0) { w.org[M.a + j] = o; w.rtau[M.a + j] = tau; }
+}
+
+// Gu-Eisenstat: zhat_i^2 = -Delta_ii / rho * prod_{j != i} Delta_ij / (d_i - d_j),
+// Delta_ij = d_i - lambda_j = (d_i - d_org(j)) - tau_j.  One warp per kept i.
+__global__ void __launch_bounds__(256) k_dc_zhat(DcWork w)
+{
+    const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (p >= w.n) return;
+    const int mix = w.pos2m[p];
+    if (mix < 0) return;
+    const MergeInfo M = w.mi[mix];
+    const int i = p - M.a, kk = M.kk;
+    if (i >= kk) return;
+    const double *dl = w.kd + M.a;
+    const int *org = w.org + M.a;
+    const double *rt = w.rtau + M.a;
+    const double di = dl[i];
+    double pr = 1.0;
+    for (int j = lane; j < kk; j += 32) {
+        const double dij = (di - dl[org[j]]) - rt[j];
+        pr *= (j == i) ? -dij / M.rho : dij / (di - dl[j]);
+    }
+    pr = warp_prod(pr);
+    if (lane == 0) w.zh[M.a + i] = copysign(sqrt(fabs(pr)), w.kw[M.a + i]);
+}
+
+// Row j of U (the eigenvector of root j in the kept basis, grouped columns):
+// U[a+j][a+kci(i)] = zhat_i / Delta_ij, normalised.  One warp per root.
+__global__ void __launch_bounds__(256) k_dc_vectors(DcWork w)
+{
+    const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (p >= w.n) return;
+    const int mix = w.pos2m[p];
+    if (mix < 0) return;
+    const MergeInfo M = w.mi[mix];
+    const int j = p - M.a, kk = M.kk, n = w.n;
+    if (j >= kk) return;
+    const double *dl = w.kd + M.a;
+    const double dorg = dl[w.org[M.a + j]], tau = w.rtau[M.a + j];
+    double *Ur = w.U + (size_t)(M.a + j) * n + M.a;
+    double s = 0.0;
+    for (int i = lane; i < kk; i += 32) {
+        const double v = w.zh[M.a + i] / ((dl[i] - dorg) - tau);
+        Ur[w.kci[M.a + i]] = v;
+        s += v * v;
+    }
+    s = warp_sum(s);
+    const double inv = 1.0 / sqrt(s);
+    __syncwarp();
+    for (int i = lane; i < kk; i += 32) Ur[w.kci[M.a + i]] *= inv;
+}
+
+// Final positions: roots (ascending) and deflated values merged by rank; new
+// eigenvalues written; the gathered kept rows Zc[a + kci] = Z[srt[kept]].
+__global__ void __launch_bounds__(256) k_dc_rank(DcWork w)
+{
+    const MergeInfo M = w.mi[blockIdx.y];
+    const int k = M.b - M.a, kk = M.kk, nd = M.nd;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= k) return;
+    auto val = [&](int x) -> double {
+        if (x < kk) return w.kd[M.a + w.org[M.a + x]] + w.rtau[M.a + x];
+        return w.Ds[w.dl[M.a + (x - kk)]];
+    };
+    const double v = val(t);
+    int r = 0;
+    for (int x = 0; x < kk + nd; x++) {
+        const double u = val(x);
+        r += (u < v) || (u == v && x < t);
+    }
+    w.rank[M.a + t] = M.a + r;
+}
+
+__global__ void k_dc_lam(DcWork w)
+{
+    const MergeInfo M = w.mi[blockIdx.y];
+    const int k = M.b - M.a, kk = M.kk;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= k) return;
+    const double v = t < kk ? w.kd[M.a + w.org[M.a + t]] + w.rtau[M.a + t] : w.Ds[w.dl[M.a + (t - kk)]];
+    w.lam[w.rank[M.a + t]] = v;
+}
+
+// Gather kept rows into Zc (grouped order) and copy deflated rows to their
+// final positions in Zn.  Grid: (column blocks, rows of the merge, merges).
+__global__ void k_dc_gather(DcWork w)
+{
+    const MergeInfo M = w.mi[blockIdx.z];
+    const int t = blockIdx.y, n = w.n;
+    const int col = M.a + blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= M.b || t >= M.b - M.a) return;
+    if (t < M.kk) {
+        const int src = w.srt[w.kl[M.a + t]];
+        w.Zc[(size_t)(M.a + w.kci[M.a + t]) * n + col] = w.Z[(size_t)src * n + col];
+    } else {
+        const int dt = t - M.kk;
+        const int src = w.srt[w.dl[M.a + dt]];
+        w.Zn[(size_t)w.rank[M.a + t] * n + col] = w.Z[(size_t)src * n + col];
+    }
+}
+
+// Grouped FP64 GEMM for the merges of a level: for merge g and half h,
+//   Zn[rank[a+j]][cols of half h] = sum_c U[a+j][a+c0+c] Zc[a+c0+c][cols of half h]
+// with c over the kept vectors supported on that half (first half: groups
+// first-only and both; second half: both and second-only).  64x64 tiles, 4x4
+// per thread.
+constexpr int DT = 64, DK = 16;
+__global__ void __launch_bounds__(256) k_dc_gemm(DcWork w)
+{
+    const MergeInfo M = w.mi[blockIdx.z >> 1];
+    const int h = blockIdx.z & 1;
+    const int n = w.n;
+    const int kk = M.kk;
+    const int c0 = h ? M.k1 : 0, K = h ? kk - M.k1 : M.k1 + M.k2;
+    const int colb = h ? M.m : M.a, ncol = h ? M.b - M.m : M.m - M.a;
+    const int ntn = (ncol + DT - 1) / DT;
+    const int tm = blockIdx.x / ntn, tn = blockIdx.x % ntn;
+    if (tm * DT >= kk || tn >= ntn || K == 0) return;
+    __shared__ double As[DK][DT + 1];
+    __shared__ double Bs[DK][DT + 1];
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += DK) {
+        for (int e = tid; e < DK * DT; e += 256) {
+            const int kq = e % DK, mm = e / DK;
+            const int r = tm * DT + mm, kx = k0 + kq;
+            As[kq][mm] = (r < kk && kx < K) ? w.U[(size_t)(M.a + r) * n + M.a + c0 + kx] : 0.0;
+        }
+        for (int e = tid; e < DK * DT; e += 256) {
+            const int nn = e % DT, kq = e / DT;
+            const int cc = tn * DT + nn, kx = k0 + kq;
+            Bs[kq][nn] = (cc < ncol && kx < K) ? w.Zc[(size_t)(M.a + c0 + kx) * n + colb + cc] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kq = 0; kq < DK; kq++) {
+            double av[4], bv[4];
+#pragma unroll
+            for (int x = 0; x < 4; x++) av[x] = As[kq][ty + 16 * x];
+#pragma unroll
+            for (int y = 0; y < 4; y++) bv[y] = Bs[kq][tx + 16 * y];
+#pragma unroll
+            for (int x = 0; x < 4; x++)
+#pragma unroll
+                for (int y = 0; y < 4; y++) acc[x][y] = fma(av[x], bv[y], acc[x][y]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+        const int r = tm * DT + ty + 16 * x;
+        if (r >= kk) continue;
+        double *dst = w.Zn + (size_t)w.rank[M.a + r] * n + colb;
+#pragma unroll
+        for (int y = 0; y < 4; y++) {
+            const int cc = tn * DT + tx + 16 * y;
+            if (cc < ncol) dst[cc] = acc[x][y];
+        }
+    }
+}
+
+// A half with no kept column leaves its part of the new rows zero.
+__global__ void k_dc_zero_half(DcWork w)
+{
+    const MergeInfo M = w.mi[blockIdx.z >> 1];
+    const int h = blockIdx.z & 1, n = w.n;
+    const int K = h ? M.kk - M.k1 : M.k1 + M.k2;
+    if (K != 0) return;
+    const int colb = h ? M.m : M.a, ncol = h ? M.b - M.m : M.m - M.a;
+    const int r = blockIdx.y, c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= M.kk || c >= ncol) return;
+    w.Zn[(size_t)w.rank[M.a + r] * n + colb + c] = 0.0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+
+static void build_tree(int a, int b, int lev, std::vector<std::vector<int3>> &out)
+{
+    if (b - a <= 1) return;
+    const int m = (a + b) / 2;
+    if ((int)out.size() <= lev) out.resize(lev + 1);
+    build_tree(a, m, lev + 1, out);
+    build_tree(m, b, lev + 1, out);
+    out[lev].push_back(make_int3(a, m, b));
+}
+
+// Carve the eigensolver's workspace out of ctx->eigw for size n.
+struct SyevPtrs {
+    double *VS, *Wp, *TS, *d, *e, *tau, *a, *y, *part;
+    unsigned *bar;
+    int *err;
+    double *lam, *Z, *Zn, *U, *Zc;
+    int *srt, *kl, *kci, *flg, *dl, *org, *rank, *pos2m;
+    double *Ds, *zs, *kd, *kw, *rtau, *zh;
+    int2 *grot;
+    double2 *gcs;
+    MergeInfo *mi;
+    int nmerge_total;
+};
+
+static size_t carve(uint8_t *base, int n, int npanel, int nlev, int nmerge, SyevPtrs &p)
+{
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 255) & ~(size_t)255; return base ? (void *)(base + r) : nullptr; };
+    const size_t NN = (size_t)n * n;
+    p.VS = (double *)take(sizeof(double) * (size_t)npanel * n * TRD_NB);
+    p.Wp = (double *)take(sizeof(double) * (size_t)n * TRD_NB);
+    p.TS = (double *)take(sizeof(double) * (size_t)npanel * TRD_NB * TRD_NB);
+    p.d = (double *)take(sizeof(double) * n);
+    p.e = (double *)take(sizeof(double) * n);
+    p.tau = (double *)take(sizeof(double) * n);
+    p.a = (double *)take(sizeof(double) * n);
+    p.y = (double *)take(sizeof(double) * n);
+    p.part = (double *)take(sizeof(double) * PCOMP * 1024);
+    p.bar = (unsigned *)take(sizeof(unsigned) * 2);
+    p.err = (int *)take(sizeof(int) * 2);
+    p.lam = (double *)take(sizeof(double) * n);
+    p.Z = (double *)take(sizeof(double) * NN);
+    p.Zn = (double *)take(sizeof(double) * NN);
+    p.U = (double *)take(sizeof(double) * NN);
+    p.Zc = (double *)take(sizeof(double) * NN);
+    p.srt = (int *)take(sizeof(int) * n);
+    p.kl = (int *)take(sizeof(int) * n);
+    p.kci = (int *)take(sizeof(int) * n);
+    p.flg = (int *)take(sizeof(int) * n);
+    p.dl = (int *)take(sizeof(int) * n);
+    p.org = (int *)take(sizeof(int) * n);
+    p.rank = (int *)take(sizeof(int) * n);
+    p.pos2m = (int *)take(sizeof(int) * (size_t)n * std::max(1, nlev));
+    p.Ds = (double *)take(sizeof(double) * n);
+    p.zs = (double *)take(sizeof(double) * n);
+    p.kd = (double *)take(sizeof(double) * n);
+    p.kw = (double *)take(sizeof(double) * n);
+    p.rtau = (double *)take(sizeof(double) * n);
+    p.zh = (double *)take(sizeof(double) * n);
+    p.grot = (int2 *)take(sizeof(int2) * n);
+    p.gcs = (double2 *)take(sizeof(double2) * n);
+    p.mi = (MergeInfo *)take(sizeof(MergeInfo) * std::max(1, nmerge));
+    p.nmerge_total = nmerge;
+    return o;
+}
+
+struct SyevState {
+    int n = -1;
+    std::vector<std::vector<int3>> levels;
+    std::vector<int> level_off;
+    int nmerge = 0;
+};
+
+static modal_status dc_setup(modal_ctx *ctx, int n, SyevState &st, SyevPtrs &p, int npanel)
+{
+    st.levels.clear();
+    build_tree(0, n, 0, st.levels);
+    std::reverse(st.levels.begin(), st.levels.end());  // deepest first
+    st.level_off.assign(st.levels.size(), 0);
+    int nm = 0;
+    for (size_t l = 0; l < st.levels.size(); l++) { st.level_off[l] = nm; nm += (int)st.levels[l].size(); }
+    st.nmerge = nm;
+    const int nlev = (int)st.levels.size();
+    size_t need = carve(nullptr, n, npanel, nlev, nm, p);
+    MODAL_TRY(ensure(ctx->eigw, need));
+    carve(ctx->eigw.as<uint8_t>(), n, npanel, nlev, nm, p);
+    // merge descriptors and position -> merge maps for every level
+    std::vector<MergeInfo> mi(std::max(1, nm));
+    std::vector<int> pos2m((size_t)n * std::max(1, nlev), -1);
+    for (int l = 0; l < nlev; l++) {
+        for (size_t x = 0; x < st.levels[l].size(); x++) {
+            const int3 t = st.levels[l][x];
+            MergeInfo M{};
+            M.a = t.x; M.m = t.y; M.b = t.z;
+            mi[st.level_off[l] + x] = M;
+            for (int q = t.x; q < t.z; q++) pos2m[(size_t)l * n + q] = (int)x;
+        }
+    }
+    if (nm > 0)
+        MODAL_CUDA(cudaMemcpyAsync(p.mi, mi.data(), sizeof(MergeInfo) * nm, cudaMemcpyHostToDevice, ctx->stream));
+    if (nlev > 0)
+        MODAL_CUDA(cudaMemcpyAsync(p.pos2m, pos2m.data(), sizeof(int) * pos2m.size(), cudaMemcpyHostToDevice, ctx->stream));
+    // the host vectors must outlive the copies
+    MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
+    return MODAL_OK;
+}
+
+static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int npanel)
+{
+    int dev = ctx->device, nsm = 0, coop = 0;
+    MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    MODAL_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop) { set_error("eigensolver: the device has no cooperative launch"); return MODAL_ERR_CUDA; }
+    const size_t smem = sizeof(double) * (size_t)std::max(1, n);
+    if (smem > 200 * 1024) { set_error("eigensolver: n = %d exceeds the panel kernel's shared-memory vector", n); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaFuncSetAttribute(k_trd_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    MODAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trd_panel, TRD_THREADS, smem));
+    if (per_sm < 1) { set_error("eigensolver: panel kernel does not fit on an SM"); return MODAL_ERR_CUDA; }
+    int G = std::min(nsm, std::max(1, (n + 15) / 16));
+    G = std::min(G, 1024);
+    MODAL_CUDA(cudaMemsetAsync(p.err, 0, 2 * sizeof(int), ctx->stream));
+    MODAL_CUDA(cudaMemsetAsync(p.VS, 0, sizeof(double) * (size_t)npanel * n * TRD_NB, ctx->stream));
+    MODAL_CUDA(cudaMemsetAsync(p.TS, 0, sizeof(double) * (size_t)npanel * TRD_NB * TRD_NB, ctx->stream));
+    for (int pi = 0; pi < npanel; pi++) {
+        const int j0 = pi * TRD_NB;
+        const int nbp = std::min(TRD_NB, n - 1 - j0);  // reflectors 0 .. n-2
+        MODAL_CUDA(cudaMemsetAsync(p.Wp, 0, sizeof(double) * (size_t)n * TRD_NB, ctx->stream));
+        MODAL_CUDA(cudaMemsetAsync(p.bar, 0, 2 * sizeof(unsigned), ctx->stream));
+        TrdArgs g;
+        g.A = A; g.n = n; g.j0 = j0; g.nbp = nbp;
+        g.V = p.VS + (size_t)pi * n * TRD_NB;
+        g.W = p.Wp;
+        g.T = p.TS + (size_t)pi * TRD_NB * TRD_NB;
+        g.d = p.d; g.e = p.e; g.tau = p.tau; g.a = p.a; g.y = p.y; g.part = p.part; g.bar = p.bar; g.err = p.err;
+        void *args[] = {&g};
+        MODAL_CUDA(cudaLaunchCooperativeKernel((const void *)k_trd_panel, dim3(G), dim3(TRD_THREADS), args, smem, ctx->stream));
+        MODAL_TRY(launched(ctx, "trd_panel"));
+        const int s = j0 + nbp, rest = n - s;
+        if (rest > 0) {
+            const double *Vs = g.V + (size_t)s * TRD_NB, *Ws = p.Wp + (size_t)s * TRD_NB;
+            double *A22 = A + (size_t)s * n + s;
+            MODAL_TRY(dgemm(ctx, rest, rest, nbp, -1.0, Vs, TRD_NB, false, Ws, TRD_NB, true, 1.0, A22, n, 1));
+            MODAL_TRY(dgemm(ctx, rest, rest, nbp, -1.0, Ws, TRD_NB, false, Vs, TRD_NB, true, 1.0, A22, n, 1));
+            const int nt = ceil_div(rest, 32);
+            k_mirror_lower<<<dim3(nt, nt), 256, 0, ctx->stream>>>(A, n, s);
+            MODAL_TRY(launched(ctx, "mirror_lower"));
+        }
+    }
+    k_copy_last_diag<<<1, 32, 0, ctx->stream>>>(A, n, p.d);
+    return launched(ctx, "copy_last_diag");
+}
+
+static modal_status dc_run(modal_ctx *ctx, int n, SyevState &st, SyevPtrs &p)
+{
+    k_dc_leaves<<<ceil_div(n, 256), 256, 0, ctx->stream>>>(n, p.d, p.e, p.lam);
+    MODAL_TRY(launched(ctx, "dc_leaves"));
+    // both buffers start as the identity: a row that is still a single-row
+    // segment at some level is not written by that level's merges, and its
+    // parent reads it from whichever buffer is current then
+    k_dc_eye<<<ceil_div((long)n * n, 256), 256, 0, ctx->stream>>>(n, p.Z);
+    MODAL_TRY(launched(ctx, "dc_eye"));
+    k_dc_eye<<<ceil_div((long)n * n, 256), 256, 0, ctx->stream>>>(n, p.Zn);
+    MODAL_TRY(launched(ctx, "dc_eye"));
+    double *Z = p.Z, *Zn = p.Zn;
+    const int nlev = (int)st.levels.size();
+    for (int l = 0; l < nlev; l++) {
+        const int nm = (int)st.levels[l].size();
+        int kmax = 0, hmax = 0;
+        for (const int3 &t : st.levels[l]) { kmax = std::max(kmax, t.z - t.x); hmax = std::max(hmax, std::max(t.y - t.x, t.z - t.y)); }
+        DcWork w;
+        w.lam = p.lam; w.Z = Z; w.Zn = Zn; w.U = p.U; w.Zc = p.Zc; w.e = p.e; w.n = n;
+        w.srt = p.srt; w.Ds = p.Ds; w.zs = p.zs; w.kl = p.kl; w.kci = p.kci; w.flg = p.flg; w.dl = p.dl; w.grot = p.grot; w.gcs = p.gcs;
+        w.kd = p.kd; w.kw = p.kw; w.org = p.org; w.rtau = p.rtau; w.zh = p.zh; w.rank = p.rank;
+        w.mi = p.mi + st.level_off[l];
+        w.pos2m = p.pos2m + (size_t)l * n;
+        w.err = p.err;
+        k_dc_deflate<<<nm, 256, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_deflate"));
+        k_dc_rotate<<<dim3(ceil_div(kmax, 128), nm), 128, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_rotate"));
+        const int wblocks = ceil_div((long)n * 32, 256);
+        k_dc_secular<<<wblocks, 256, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_secular"));
+        k_dc_zhat<<<wblocks, 256, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_zhat"));
+        k_dc_vectors<<<wblocks, 256, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_vectors"));
+        k_dc_rank<<<dim3(ceil_div(kmax, 256), nm), 256, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_rank"));
+        k_dc_gather<<<dim3(ceil_div(kmax, 128), kmax, nm), 128, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_gather"));
+        const long tiles = (long)ceil_div(kmax, DT) * ceil_div(hmax, DT);
+        k_dc_gemm<<<dim3((unsigned)tiles, 1, 2 * nm), 256, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_gemm"));
+        k_dc_zero_half<<<dim3(ceil_div(hmax, 128), kmax, 2 * nm), 128, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_zero_half"));
+        k_dc_lam<<<dim3(ceil_div(kmax, 256), nm), 256, 0, ctx->stream>>>(w);
+        MODAL_TRY(launched(ctx, "dc_lam"));
+        std::swap(Z, Zn);
+    }
+    if (Z != p.Z) {
+        MODAL_CUDA(cudaMemcpyAsync(p.Z, Z, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    return MODAL_OK;
+}
+
+// X[m][n] (rows = vectors in the tridiagonal basis) := X Q^T.
+static modal_status backtransform(modal_ctx *ctx, int n, int m, double *X, int ldx, SyevPtrs &p, int npanel)
+{
+    if (m <= 0) return MODAL_OK;
+    // work: X V (m x NB) and its product with T^T
+    MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)m * TRD_NB * 2));
+    double *XV = ctx->scratch2.as<double>(), *XT = XV + (size_t)m * TRD_NB;
+    for (int pi = npanel - 1; pi >= 0; pi--) {
+        const int j0 = pi * TRD_NB;
+        const int nbp = std::min(TRD_NB, n - 1 - j0);
+        const int r = j0 + 1, K = n - r;
+        const double *V = p.VS + (size_t)pi * n * TRD_NB + (size_t)r * TRD_NB;
+        const double *T = p.TS + (size_t)pi * TRD_NB * TRD_NB;
+        MODAL_TRY(dgemm_splitk(ctx, m, nbp, K, X + r, ldx, false, V, TRD_NB, false, XV, TRD_NB, 0, false));
+        MODAL_TRY(dgemm(ctx, m, nbp, nbp, 1.0, XV, TRD_NB, false, T, TRD_NB, true, 0.0, XT, TRD_NB, 0));
+        MODAL_TRY(dgemm(ctx, m, K, nbp, -1.0, XT, TRD_NB, false, V, TRD_NB, true, 1.0, X + r, ldx, 0));
+    }
+    return MODAL_OK;
+}
+
+// Eigen-decomposition of the symmetric n x n matrix A (device, row-major,
+// overwritten).  W[n] (device) receives every eigenvalue in ascending order.
+// select(W_host, n, arg, &first) returns how many eigenvectors are wanted,
+// starting at ascending index `first`; those are written as rows of V (device,
+// ld n): row t holds the eigenvector of W[first + t].  *nvec = that count,
+// *first_out = first.
+modal_status syev_dev(modal_ctx *ctx, int n, double *A, double *W, double *V, SyevSelect select, void *arg,
+                      int *nvec, int *first_out)
+{
+    *nvec = 0;
+    if (first_out) *first_out = 0;
+    if (n <= 0) return MODAL_OK;
+    static thread_local SyevState st;
+    SyevPtrs p{};
+    const int npanel = n > 1 ? ceil_div(n - 1, TRD_NB) : 0;
+    MODAL_TRY(dc_setup(ctx, n, st, p, npanel));
+    if (n > 1) {
+        {
+            StageTimer tt(ctx, MODAL_T_EIG_TRD);
+            MODAL_TRY(trd_run(ctx, n, A, p, npanel));
+        }
+        StageTimer td(ctx, MODAL_T_EIG_DC);
+        MODAL_TRY(dc_run(ctx, n, st, p));
+    } else {
+        MODAL_CUDA(cudaMemcpyAsync(p.lam, A, sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+        MODAL_CUDA(cudaMemsetAsync(p.err, 0, 2 * sizeof(int), ctx->stream));
+        k_dc_eye<<<1, 32, 0, ctx->stream>>>(1, p.Z);
+        MODAL_TRY(launched(ctx, "dc_eye"));
+    }
+    MODAL_CUDA(cudaMemcpyAsync(W, p.lam, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    std::vector<double> hw(n);
+    int herr[2] = {0, 0};
+    MODAL_CUDA(cudaMemcpyAsync(hw.data(), p.lam, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    MODAL_CUDA(cudaMemcpyAsync(herr, p.err, sizeof(herr), cudaMemcpyDeviceToHost, ctx->stream));
+    MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (herr[0]) { set_error("eigensolver: a bounded grid-barrier wait expired"); return MODAL_ERR_TIMEOUT; }
+    for (int i = 0; i < n; i++)
+        if (!std::isfinite(hw[i])) { set_error("eigensolver: non-finite eigenvalue"); return MODAL_ERR_NOCONV; }
+    int first = 0;
+    int c = select ? select(hw.data(), n, arg, &first) : n;
+    if (first < 0 || first > n) first = 0;
+    c = std::max(0, std::min(n - first, c));
+    *nvec = c;
+    if (first_out) *first_out = first;
+    if (c == 0) return MODAL_OK;
+    MODAL_CUDA(cudaMemcpyAsync(V, p.Z + (size_t)first * n, sizeof(double) * (size_t)c * n, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+    StageTimer tb(ctx, MODAL_T_EIG_BACK);
+    return backtransform(ctx, n, c, V, n, p, npanel);
+}
+
+}  // namespace modal
+
+using namespace modal;
+
+extern "C" modal_status modal_eigh(modal_ctx *c, int n, const double *a, double *w, double *v)
+{
+    if (!c || n < 1 || !a || !w) { set_error("modal_eigh: bad arguments (n=%d)", n); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaSetDevice(c->device));
+    const size_t NN = (size_t)n * n;
+    MODAL_TRY(ensure(c->scratch, sizeof(double) * (2 * NN + (size_t)n)));
+    double *A = c->scratch.as<double>(), *V = A + NN, *W = V + NN;
+    MODAL_CUDA(cudaMemcpyAsync(A, a, sizeof(double) * NN, cudaMemcpyHostToDevice, c->stream));
+    int nv = 0, first = 0;
+    struct Want { bool vectors; } want{v != nullptr};
+    auto sel = [](const double *, int nn, void *arg, int *f) -> int {
+        *f = 0;
+        return static_cast<Want *>(arg)->vectors ? nn : 0;
+    };
+    MODAL_TRY(syev_dev(c, n, A, W, V, sel, &want, &nv, &first));
+    MODAL_CUDA(cudaMemcpyAsync(w, W, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    if (v) MODAL_CUDA(cudaMemcpyAsync(v, V, sizeof(double) * NN, cudaMemcpyDeviceToHost, c->stream));
+    MODAL_CUDA(cudaStreamSynchronize(c->stream));
+    return MODAL_OK;
+}

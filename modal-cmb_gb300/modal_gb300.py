@@ -36,9 +36,11 @@ EXPORTS = [
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
     "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol", "modal_set_transfer_pol",
     "modal_gamma_transfer_pol", "modal_prim_points", "modal_prim_ortho", "modal_prim_eigen", "modal_set_ortho",
+    "modal_eigh",
 ]
 
-TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9}
+TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9,
+          "eig_trd": 10, "eig_dc": 11, "eig_back": 12}
 
 
 class ModalError(RuntimeError):
@@ -112,6 +114,7 @@ def lib():
             "modal_basis_prune": (i, [vp, i, vp, i, vp, vp, vp]),
             "modal_lambda_min": (i, [vp, ctypes.POINTER(d), vp, vp]),
             "modal_set_pca_floor": (i, [vp, d]),
+            "modal_eigh": (i, [vp, i, vp, vp, vp]),
             "modal_project_batch": (i, [vp, i, vp, i, vp]),
             "modal_ctx_captures": (l, [vp]),
             "modal_autotune": (i, [vp, ctypes.c_char_p]),
@@ -344,6 +347,17 @@ class Context:
 
     def set_pca_floor(self, floor):
         _check(lib().modal_set_pca_floor(self.h, float(floor)))
+
+    def eigh(self, a, vectors=True):
+        """(w ascending, v with eigenvectors as rows or None) of the symmetric matrix a
+        (modal_eigh: the library's own FP64 eigensolver on the GPU)."""
+        a = _f64(a)
+        n = a.shape[0]
+        assert a.shape == (n, n)
+        w = np.empty(n)
+        v = np.empty((n, n)) if vectors else None
+        _check(lib().modal_eigh(self.h, n, _ptr(a), _ptr(w), _ptr(v)))
+        return w, v
 
     def set_spectrum(self, cl):
         cl = _f64(cl)

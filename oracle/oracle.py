@@ -298,17 +298,19 @@ class Oracle:
         return a, m
 
 
-def ortho_pca(gamma):
+def ortho_pca(gamma, floor=0.0):
     """PCA branch of ortho_late_mpi.c:775-805 with numpy.linalg.eigh standing
-    in for gsl_eigen_symmv (eigenvalues sorted descending).  Returns
-    (lambdainv, lambda, r)."""
+    in for gsl_eigen_symmv (eigenvalues sorted descending).  floor > 0 keeps
+    only eigenvalues above floor * e_max (the reference's rule is floor 0).
+    Returns (lambdainv, lambda, r)."""
     norm = np.sqrt(np.diag(gamma))
     gh = gamma / np.outer(norm, norm)
     e, V = np.linalg.eigh(gh)
     e, V = e[::-1], V[:, ::-1]
+    cut = floor * e[0] if floor > 0.0 else 0.0
     r = 0
     for i in range(len(e)):
-        if e[i] > 0.0:
+        if e[i] > cut:
             r = i + 1
         else:
             break

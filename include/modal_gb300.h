@@ -258,6 +258,17 @@ modal_status modal_set_pca_floor(modal_ctx *ctx, double floor);
  * modal_basis_prune use the same solver. */
 modal_status modal_eigh(modal_ctx *ctx, int n, const double *a, double *w, double *v);
 
+/* C = beta C + alpha op(A) op(B) for row-major host arrays (op(A) M x K,
+ * op(B) K x N, C M x N; trans* != 0 takes the transpose), with FP64
+ * accuracy on the FP16 tensor cores: each row of op(A) and column of op(B) is
+ * scaled by a power of two and cut into `slices` (2..8) exact 7-bit integer
+ * digits, the digit products are summed exactly in the tensor memory over
+ * blocks of 512 terms and the blocks in double-FP32.  slices = 8 gives the
+ * accuracy class of an FP64 product.  No reference counterpart: the library's
+ * eigensolver and Gamma use the same products internally. */
+modal_status modal_gemm_f64(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, int transA,
+                            const double *B, int transB, double beta, double *C, int slices);
+
 /* Batched projection replayed from a captured CUDA graph.  Same inputs,
  * result and FP64/FP32 forms as modal_project (beta: host [S][N], required;
  * it also stays on the device for modal_alpha).  The first call for a batch

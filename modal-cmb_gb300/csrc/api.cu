@@ -165,7 +165,7 @@ void modal_ctx_destroy(modal_ctx *c)
                       &c->modesr, &c->scratch, &c->scratch2, &c->shape_tab, &c->shape_desc, &c->slab_order,
                       &c->split, &c->tr_x, &c->tr_qt, &c->tr_prim, &c->tr_mt, &c->tr_v, &c->tr_out,
                       &c->adj, &c->adj2, &c->adj3, &c->prune, &c->gemm_part, &c->qe, &c->me, &c->tri_pol, &c->gamma_pol,
-                      &c->tr_qte, &c->tr_we, &c->tr_mte, &c->prim, &c->eigw};
+                      &c->tr_qte, &c->tr_we, &c->tr_mte, &c->prim, &c->eigw, &c->ozw, &c->ozerr};
     batch_release(c);
     for (DevBuf *b : bufs) release(*b);
     timers_clear(c);

@@ -102,6 +102,8 @@ struct modal_ctx {
     modal::DevBuf prim;
     double *h_info = nullptr;  // pinned readback
     modal::DevBuf eigw;        // eigensolver workspace (syev.cu)
+    modal::DevBuf ozw;         // tensor-core FP64 products: operand slices, exponents, tiles (ozgemm.cu)
+    modal::DevBuf ozerr;       // their sticky error word
 
     // profiling: event pairs per stage, summed on read
     bool profile = false;
@@ -229,6 +231,22 @@ void batch_release(modal_ctx *ctx);
 //   lower != 0: only entries with n <= m (tiles above the diagonal skipped).
 modal_status dgemm(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, int lda, bool transA,
                    const double *B, int ldb, bool transB, double beta, double *C, int ldc, int lower);
+// FP64-accuracy product on the FP16 tensor cores by exact integer slices
+// (ozgemm.cu): C = beta C + alpha op(A) op(B), s slices of 7 bits (2..8).
+//   op(A)(m,k) = transA ? A[k*lda+m] : A[m*lda+k];  op(B)(k,n) = transB ? B[n*ldb+k] : B[k*ldb+n]
+modal_status oz_gemm(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, long lda, bool transA,
+                     const double *B, long ldb, bool transB, double beta, double *C, long ldc, int lower, int s);
+struct OzOpts {
+    int slices = 8;      // 7-bit digits per operand (8: the FP64 accuracy class)
+    int lower = 0;       // square C: only n <= m
+    int diag_tiles = 0;  // > 0: only the diagonal blocks of that many 128-tiles
+    int ksplit = 0;      // K split over work items (0: fill the GPU)
+    bool check = true;   // synchronise and report an expired wait now (else: oz_check later)
+};
+modal_status oz_reset(modal_ctx *ctx);  // clear the sticky error word of unchecked calls
+modal_status oz_check(modal_ctx *ctx);  // synchronise; MODAL_ERR_TIMEOUT if any call's wait expired
+modal_status oz_gemm_ex(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, long lda, bool transA,
+                        const double *B, long ldb, bool transB, double beta, double *C, long ldc, const OzOpts &o);
 // C (+)= A op(B) for A [S][K] with few rows S: skinny kernels for S <= 32 (alpha 1; accumulate: C +=)
 modal_status dgemm_rows(modal_ctx *ctx, int S, int N, int K, const double *A, int lda, const double *B, int ldb,
                         bool transB, double *C, int ldc, bool accumulate);

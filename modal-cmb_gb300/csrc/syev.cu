@@ -38,7 +38,10 @@ namespace {
 constexpr int TRD_NB = 32;                 // panel width
 constexpr int TRD_THREADS = 512;           // 16 warps per CTA
 constexpr int TRD_WARPS = TRD_THREADS / 32;
+constexpr int LDP = 2 * TRD_NB;            // panel row: V (TRD_NB columns) then W
 constexpr int PCOMP = 2 * TRD_NB + 2;      // partial components: p[NB], q[NB], y.v, |x|^2
+constexpr int NBB = 256;                   // reflectors per block of the back-transformation
+constexpr int OZ_SLICES = 8;               // 7-bit slices of the tensor-core FP64 products
 constexpr long long BAR_CYCLES = 1ll << 32;  // ~2 s of clock64 per barrier wait
 constexpr double EPS = 1.1102230246251565e-16;  // 2^-53
 
@@ -108,8 +111,7 @@ __device__ __forceinline__ void my_rows(int lo, int hi, int &r0, int &r1)
 struct TrdArgs {
     double *A;
     int n, j0, nbp;
-    double *V, *W;  // panel: [n][TRD_NB] row-major, zero outside the reflectors
-    double *T;      // [TRD_NB][TRD_NB] upper-triangular compact-WY factor
+    double *V, *W;  // panel: rows of LDP doubles, V in columns [0, NB), W in [NB, 2 NB); zero outside the reflectors
     double *d, *e, *tau;
     double *a, *y;  // [n] work vectors
     double *part;   // [PCOMP][grid] per-CTA partial sums
@@ -162,35 +164,26 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             // w of row i (head row), computed by every CTA alike
             if (tid == 0) {
                 double s = g.y[i];
-                for (int t = 0; t < cp; t++) s -= g.V[(size_t)i * TRD_NB + t] * q[t] + g.W[(size_t)i * TRD_NB + t] * p[t];
+                for (int t = 0; t < cp; t++) s -= g.V[(size_t)i * LDP + t] * q[t] + g.W[(size_t)i * LDP + t] * p[t];
                 s_scal[1] = taup * s - 0.5 * taup * taup * yvc * 1.0;
-            }
-            if (blockIdx.x == 0) {
-                // T[0:cp, cp] = -tau T[0:cp, 0:cp] p ; T[cp][cp] = tau  (dlarft, forward columnwise)
-                for (int t = tid; t < cp; t += blockDim.x) {
-                    double s = 0.0;
-                    for (int u = t; u < cp; u++) s += g.T[t * TRD_NB + u] * p[u];
-                    g.T[t * TRD_NB + cp] = -taup * s;
-                }
-                if (tid == 0) g.T[cp * TRD_NB + cp] = taup;
             }
             __syncthreads();
             const double whead = s_scal[1];
             // rows of this CTA: w (stored), then the column update of column i
             if (c < g.nbp) {
                 for (int t = tid; t < c; t += blockDim.x) {
-                    s_vi[t] = g.V[(size_t)i * TRD_NB + t];
-                    s_wi[t] = (t == cp) ? whead : g.W[(size_t)i * TRD_NB + t];
+                    s_vi[t] = g.V[(size_t)i * LDP + t];
+                    s_wi[t] = (t == cp) ? whead : g.W[(size_t)i * LDP + t];
                 }
             }
             __syncthreads();
             double nrm = 0.0;
             for (int r = r0 + tid; r < r1; r += blockDim.x) {
                 double s = g.y[r];
-                const double *Vr = g.V + (size_t)r * TRD_NB, *Wr = g.W + (size_t)r * TRD_NB;
+                const double *Vr = g.V + (size_t)r * LDP, *Wr = g.W + (size_t)r * LDP;
                 for (int t = 0; t < cp; t++) s -= Vr[t] * q[t] + Wr[t] * p[t];
                 const double wr = (r == i) ? whead : taup * s - 0.5 * taup * taup * yvc * Vr[cp];
-                g.W[(size_t)r * TRD_NB + cp] = wr;
+                g.W[(size_t)r * LDP + cp] = wr;
                 if (c < g.nbp) {
                     double x = g.A[(size_t)r * n + i];
                     for (int t = 0; t < cp; t++) x -= Vr[t] * s_wi[t] + Wr[t] * s_vi[t];
@@ -266,7 +259,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             const double s = warp_sum(s0 + s1);
             if (lane == 0) {
                 g.y[r] = s;
-                g.V[(size_t)r * TRD_NB + c] = sv[r - i - 1];
+                g.V[(size_t)r * LDP + c] = sv[r - i - 1];
             }
         }
         __syncthreads();
@@ -276,8 +269,8 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             double s = 0.0;
             for (int r = r0 + lane; r < r1; r += 32) {
                 const double vr = sv[r - i - 1];
-                const double x = t < c ? g.V[(size_t)r * TRD_NB + t]
-                                       : (t < 2 * c ? g.W[(size_t)r * TRD_NB + (t - c)] : g.y[r]);
+                const double x = t < c ? g.V[(size_t)r * LDP + t]
+                                       : (t < 2 * c ? g.W[(size_t)r * LDP + (t - c)] : g.y[r]);
                 s += x * vr;
             }
             s = warp_sum(s);
@@ -311,6 +304,44 @@ __global__ void k_mirror_lower(double *A, int n, int s)
 __global__ void k_copy_last_diag(const double *A, int n, double *d)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)];
+}
+
+// After a panel: Psw = [W V] (the halves of the panel rows swapped, for
+// A22 -= [V W] [W V]^T) and the panel's reflectors into columns j0.. of VA.
+__global__ void k_panel_post(int n, int j0, int nbp, const double *__restrict__ P, double *__restrict__ Psw,
+                             double *__restrict__ VA, long ldva)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)n * LDP) return;
+    const int r = (int)(e / LDP), c = (int)(e % LDP);
+    Psw[e] = P[(size_t)r * LDP + (c < TRD_NB ? c + TRD_NB : c - TRD_NB)];
+    if (c < nbp) VA[(size_t)r * ldva + j0 + c] = P[e];
+}
+
+// Compact-WY factor of a block of reflectors (LAPACK dlarft, forward, columnwise):
+// T[:, c] = -tau_c T[0:c, 0:c] G[0:c, c],  T[c][c] = tau_c, with G = V^T V the
+// block's Gram matrix (T: NBB x NBB per block; one CTA per block, columns in order).
+__global__ void __launch_bounds__(256) k_larft(int nv, const double *__restrict__ G, long ldg,
+                                               const double *__restrict__ tau, double *__restrict__ T)
+{
+    const int bb = blockIdx.x, j0 = bb * NBB, w = min(NBB, nv - j0);
+    const double *Gb = G + (size_t)j0 * ldg + j0;
+    double *Tb = T + (size_t)bb * NBB * NBB;
+    __shared__ double col[NBB];
+    for (int e = threadIdx.x; e < NBB * NBB; e += blockDim.x) Tb[e] = 0.0;
+    __syncthreads();
+    for (int c = 0; c < w; c++) {
+        const double tc = tau[j0 + c];
+        for (int u = threadIdx.x; u < c; u += blockDim.x) col[u] = Gb[(size_t)u * ldg + c];
+        __syncthreads();
+        for (int t = threadIdx.x; t < c; t += blockDim.x) {
+            double s = 0.0;
+            for (int u = t; u < c; u++) s = fma(Tb[(size_t)t * NBB + u], col[u], s);
+            Tb[(size_t)t * NBB + c] = -tc * s;
+        }
+        if (threadIdx.x == 0) Tb[(size_t)c * NBB + c] = tc;
+        __syncthreads();
+    }
 }
 
 // ------------------------------------------------------------------ stage 2
@@ -744,7 +775,8 @@ static void build_tree(int a, int b, int lev, std::vector<std::vector<int3>> &ou
 
 // Carve the eigensolver's workspace out of ctx->eigw for size n.
 struct SyevPtrs {
-    double *VS, *Wp, *TS, *d, *e, *tau, *a, *y, *part;
+    double *P, *Psw, *VA, *GB, *TB, *d, *e, *tau, *a, *y, *part;
+    long ldva;
     unsigned *bar;
     int *err;
     double *lam, *Z, *Zn, *U, *Zc;
@@ -761,9 +793,13 @@ static size_t carve(uint8_t *base, int n, int npanel, int nlev, int nmerge, Syev
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 255) & ~(size_t)255; return base ? (void *)(base + r) : nullptr; };
     const size_t NN = (size_t)n * n;
-    p.VS = (double *)take(sizeof(double) * (size_t)npanel * n * TRD_NB);
-    p.Wp = (double *)take(sizeof(double) * (size_t)n * TRD_NB);
-    p.TS = (double *)take(sizeof(double) * (size_t)npanel * TRD_NB * TRD_NB);
+    const long nvpad = (long)std::max(1, ceil_div(std::max(1, n - 1), NBB)) * NBB;
+    p.ldva = nvpad;
+    p.P = (double *)take(sizeof(double) * (size_t)n * LDP);
+    p.Psw = (double *)take(sizeof(double) * (size_t)n * LDP);
+    p.VA = (double *)take(sizeof(double) * (size_t)n * nvpad);          // every reflector, column j = v_j
+    p.GB = (double *)take(sizeof(double) * (size_t)nvpad * nvpad);      // diagonal NBB blocks of VA^T VA
+    p.TB = (double *)take(sizeof(double) * (size_t)(nvpad / NBB) * NBB * NBB);
     p.d = (double *)take(sizeof(double) * n);
     p.e = (double *)take(sizeof(double) * n);
     p.tau = (double *)take(sizeof(double) * n);
@@ -854,28 +890,33 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
     int G = std::min(nsm, std::max(1, (n + 15) / 16));
     G = std::min(G, 1024);
     MODAL_CUDA(cudaMemsetAsync(p.err, 0, 2 * sizeof(int), ctx->stream));
-    MODAL_CUDA(cudaMemsetAsync(p.VS, 0, sizeof(double) * (size_t)npanel * n * TRD_NB, ctx->stream));
-    MODAL_CUDA(cudaMemsetAsync(p.TS, 0, sizeof(double) * (size_t)npanel * TRD_NB * TRD_NB, ctx->stream));
+    MODAL_CUDA(cudaMemsetAsync(p.VA, 0, sizeof(double) * (size_t)n * p.ldva, ctx->stream));
+    MODAL_TRY(oz_reset(ctx));
+    OzOpts oz;
+    oz.slices = OZ_SLICES;
+    oz.lower = 1;
+    oz.check = false;
     for (int pi = 0; pi < npanel; pi++) {
         const int j0 = pi * TRD_NB;
         const int nbp = std::min(TRD_NB, n - 1 - j0);  // reflectors 0 .. n-2
-        MODAL_CUDA(cudaMemsetAsync(p.Wp, 0, sizeof(double) * (size_t)n * TRD_NB, ctx->stream));
+        MODAL_CUDA(cudaMemsetAsync(p.P, 0, sizeof(double) * (size_t)n * LDP, ctx->stream));
         MODAL_CUDA(cudaMemsetAsync(p.bar, 0, 2 * sizeof(unsigned), ctx->stream));
         TrdArgs g;
         g.A = A; g.n = n; g.j0 = j0; g.nbp = nbp;
-        g.V = p.VS + (size_t)pi * n * TRD_NB;
-        g.W = p.Wp;
-        g.T = p.TS + (size_t)pi * TRD_NB * TRD_NB;
+        g.V = p.P;
+        g.W = p.P + TRD_NB;
         g.d = p.d; g.e = p.e; g.tau = p.tau; g.a = p.a; g.y = p.y; g.part = p.part; g.bar = p.bar; g.err = p.err;
         void *args[] = {&g};
         MODAL_CUDA(cudaLaunchCooperativeKernel((const void *)k_trd_panel, dim3(G), dim3(TRD_THREADS), args, smem, ctx->stream));
         MODAL_TRY(launched(ctx, "trd_panel"));
+        k_panel_post<<<ceil_div((long)n * LDP, 256), 256, 0, ctx->stream>>>(n, j0, nbp, p.P, p.Psw, p.VA, p.ldva);
+        MODAL_TRY(launched(ctx, "panel_post"));
         const int s = j0 + nbp, rest = n - s;
         if (rest > 0) {
-            const double *Vs = g.V + (size_t)s * TRD_NB, *Ws = p.Wp + (size_t)s * TRD_NB;
+            // A22 -= V W^T + W V^T = [V W] [W V]^T on the lower triangle (tensor cores, FP64 accuracy)
             double *A22 = A + (size_t)s * n + s;
-            MODAL_TRY(dgemm(ctx, rest, rest, nbp, -1.0, Vs, TRD_NB, false, Ws, TRD_NB, true, 1.0, A22, n, 1));
-            MODAL_TRY(dgemm(ctx, rest, rest, nbp, -1.0, Ws, TRD_NB, false, Vs, TRD_NB, true, 1.0, A22, n, 1));
+            MODAL_TRY(oz_gemm_ex(ctx, rest, rest, LDP, -1.0, p.P + (size_t)s * LDP, LDP, false, p.Psw + (size_t)s * LDP,
+                                 LDP, true, 1.0, A22, n, oz));
             const int nt = ceil_div(rest, 32);
             k_mirror_lower<<<dim3(nt, nt), 256, 0, ctx->stream>>>(A, n, s);
             MODAL_TRY(launched(ctx, "mirror_lower"));
@@ -939,24 +980,43 @@ static modal_status dc_run(modal_ctx *ctx, int n, SyevState &st, SyevPtrs &p)
     return MODAL_OK;
 }
 
-// X[m][n] (rows = vectors in the tridiagonal basis) := X Q^T.
-static modal_status backtransform(modal_ctx *ctx, int n, int m, double *X, int ldx, SyevPtrs &p, int npanel)
+// Compact-WY factors of the blocks of NBB reflectors: the diagonal blocks of
+// the Gram matrix VA^T VA (tensor-core products), then dlarft per block.
+static modal_status wy_blocks(modal_ctx *ctx, int n, SyevPtrs &p)
 {
-    if (m <= 0) return MODAL_OK;
-    // work: X V (m x NB) and its product with T^T
-    MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)m * TRD_NB * 2));
-    double *XV = ctx->scratch2.as<double>(), *XT = XV + (size_t)m * TRD_NB;
-    for (int pi = npanel - 1; pi >= 0; pi--) {
-        const int j0 = pi * TRD_NB;
-        const int nbp = std::min(TRD_NB, n - 1 - j0);
+    const int nv = n - 1, nbig = ceil_div(nv, NBB);
+    OzOpts o;
+    o.slices = OZ_SLICES;
+    o.diag_tiles = NBB / 128;
+    o.check = false;
+    MODAL_TRY(oz_gemm_ex(ctx, nv, nv, n, 1.0, p.VA, p.ldva, true, p.VA, p.ldva, false, 0.0, p.GB, p.ldva, o));
+    k_larft<<<nbig, 256, 0, ctx->stream>>>(nv, p.GB, p.ldva, p.tau, p.TB);
+    return launched(ctx, "larft");
+}
+
+// X[m][n] (rows = vectors in the tridiagonal basis) := X Q^T, Q = H_0 ... H_{n-2}.
+// Per block of NBB reflectors, last block first (block = I - V T V^T):
+//   X[:, r:] -= ((X[:, r:] V) T^T) V^T,  r = first row where the block's V is nonzero.
+static modal_status backtransform(modal_ctx *ctx, int n, int m, double *X, int ldx, SyevPtrs &p)
+{
+    if (m <= 0 || n < 2) return MODAL_OK;
+    MODAL_TRY(wy_blocks(ctx, n, p));
+    MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)m * NBB * 2));
+    double *XV = ctx->scratch2.as<double>(), *XT = XV + (size_t)m * NBB;
+    const int nv = n - 1, nbig = ceil_div(nv, NBB);
+    OzOpts o;
+    o.slices = OZ_SLICES;
+    o.check = false;
+    for (int bb = nbig - 1; bb >= 0; bb--) {
+        const int j0 = bb * NBB, w = std::min(NBB, nv - j0);
         const int r = j0 + 1, K = n - r;
-        const double *V = p.VS + (size_t)pi * n * TRD_NB + (size_t)r * TRD_NB;
-        const double *T = p.TS + (size_t)pi * TRD_NB * TRD_NB;
-        MODAL_TRY(dgemm_splitk(ctx, m, nbp, K, X + r, ldx, false, V, TRD_NB, false, XV, TRD_NB, 0, false));
-        MODAL_TRY(dgemm(ctx, m, nbp, nbp, 1.0, XV, TRD_NB, false, T, TRD_NB, true, 0.0, XT, TRD_NB, 0));
-        MODAL_TRY(dgemm(ctx, m, K, nbp, -1.0, XT, TRD_NB, false, V, TRD_NB, true, 1.0, X + r, ldx, 0));
+        const double *V = p.VA + (size_t)r * p.ldva + j0;
+        const double *T = p.TB + (size_t)bb * NBB * NBB;
+        MODAL_TRY(oz_gemm_ex(ctx, m, w, K, 1.0, X + r, ldx, false, V, p.ldva, false, 0.0, XV, NBB, o));
+        MODAL_TRY(oz_gemm_ex(ctx, m, w, w, 1.0, XV, NBB, false, T, NBB, true, 0.0, XT, NBB, o));
+        MODAL_TRY(oz_gemm_ex(ctx, m, K, w, -1.0, XT, NBB, false, V, p.ldva, true, 1.0, X + r, ldx, o));
     }
-    return MODAL_OK;
+    return oz_check(ctx);
 }
 
 // Eigen-decomposition of the symmetric n x n matrix A (device, row-major,
@@ -988,6 +1048,7 @@ modal_status syev_dev(modal_ctx *ctx, int n, double *A, double *W, double *V, Sy
         k_dc_eye<<<1, 32, 0, ctx->stream>>>(1, p.Z);
         MODAL_TRY(launched(ctx, "dc_eye"));
     }
+    MODAL_TRY(oz_check(ctx));
     MODAL_CUDA(cudaMemcpyAsync(W, p.lam, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     std::vector<double> hw(n);
     int herr[2] = {0, 0};
@@ -1007,7 +1068,7 @@ modal_status syev_dev(modal_ctx *ctx, int n, double *A, double *W, double *V, Sy
     MODAL_CUDA(cudaMemcpyAsync(V, p.Z + (size_t)first * n, sizeof(double) * (size_t)c * n, cudaMemcpyDeviceToDevice,
                                ctx->stream));
     StageTimer tb(ctx, MODAL_T_EIG_BACK);
-    return backtransform(ctx, n, c, V, n, p, npanel);
+    return backtransform(ctx, n, c, V, n, p);
 }
 
 }  // namespace modal

@@ -36,7 +36,7 @@ EXPORTS = [
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
     "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol", "modal_set_transfer_pol",
     "modal_gamma_transfer_pol", "modal_prim_points", "modal_prim_ortho", "modal_prim_eigen", "modal_set_ortho",
-    "modal_eigh",
+    "modal_eigh", "modal_gemm_f64",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9,
@@ -115,6 +115,7 @@ def lib():
             "modal_lambda_min": (i, [vp, ctypes.POINTER(d), vp, vp]),
             "modal_set_pca_floor": (i, [vp, d]),
             "modal_eigh": (i, [vp, i, vp, vp, vp]),
+            "modal_gemm_f64": (i, [vp, i, i, i, d, vp, i, vp, i, d, vp, i]),
             "modal_project_batch": (i, [vp, i, vp, i, vp]),
             "modal_ctx_captures": (l, [vp]),
             "modal_autotune": (i, [vp, ctypes.c_char_p]),
@@ -347,6 +348,19 @@ class Context:
 
     def set_pca_floor(self, floor):
         _check(lib().modal_set_pca_floor(self.h, float(floor)))
+
+    def gemm_f64(self, A, B, transA=False, transB=False, alpha=1.0, beta=0.0, C=None, slices=8):
+        """alpha op(A) op(B) + beta C in FP64 accuracy on the tensor cores
+        (modal_gemm_f64: exact 7-bit integer slices of the operands)."""
+        A, B = _f64(A), _f64(B)
+        M = A.shape[1] if transA else A.shape[0]
+        K = A.shape[0] if transA else A.shape[1]
+        N = B.shape[0] if transB else B.shape[1]
+        assert (B.shape[1] if transB else B.shape[0]) == K
+        C = np.zeros((M, N)) if C is None else _f64(C).copy()
+        _check(lib().modal_gemm_f64(self.h, M, N, K, float(alpha), _ptr(A), int(transA), _ptr(B), int(transB),
+                                    float(beta), _ptr(C), int(slices)))
+        return C
 
     def eigh(self, a, vectors=True):
         """(w ascending, v with eigenvectors as rows or None) of the symmetric matrix a

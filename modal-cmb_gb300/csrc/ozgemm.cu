@@ -10,7 +10,8 @@
 //   every row r of op(A) (and every column of op(B)) is scaled by a power of
 //   two 2^e_r so that its entries lie in (-1, 1), then written as s balanced
 //   7-bit digits:  x = 2^e sum_p d_p 2^{-6-7p},  d_p integer in [-64, 64],
-//   exact in FP16.  A digit product is at most 2^12 in size, so the FP32
+//   exact in FP16 (x 2^{6-e+7(s-1)} rounded once to a 55-bit integer, its
+//   digits split off with integer arithmetic).  A digit product is at most 2^12 in size, so the FP32
 //   tensor-memory accumulator sums up to 4096 of them without rounding; the
 //   K dimension is cut into blocks of OZ_KB = 512, and the products of one
 //   block with equal p + q = g (at most s of them) share one accumulator,
@@ -52,7 +53,8 @@ constexpr int OZ_MAXS = 8;
 constexpr uint32_t OZ_A_BYTES = OZ_BM * OZ_BK * 2;  // 8 KB
 constexpr uint32_t OZ_B_BYTES = OZ_BN * OZ_BK * 2;  // 8 KB
 constexpr uint32_t OZ_STAGE_BYTES = OZ_A_BYTES + OZ_B_BYTES;
-constexpr uint32_t OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024 + 256;
+constexpr uint32_t OZ_STAGING = 4 * 32 * 33 * 8;  // epilogue: 32 x 32 FP64 per warp (+1 column pad)
+constexpr uint32_t OZ_SMEM = OZ_STAGES * OZ_STAGE_BYTES + 1024 + 256 + OZ_STAGING;
 constexpr uint32_t OZ_TMEM_COLS = 512;
 constexpr uint32_t OZ_SUM_COL = 256;  // first column of the double-float sums
 constexpr long long OZ_WAIT = 1ll << 31;  // ~1 s of clock64 per wait
@@ -114,14 +116,17 @@ __global__ void __launch_bounds__(256) k_oz_slice(int R, int K, int Rpad, int Kp
         for (int rr = ty; rr < 32; rr += 8) {
             const int r = r0 + rr, k = k0 + tx;
             if (r >= Rpad) continue;
-            double y = (k0 < K) ? ldexp(tile[rr][tx], 6 - sexp[rr]) : 0.0;
-            if (!isfinite(y)) y = 0.0;
+            // F = x 2^{6 - e + 7(s-1)} rounded to an integer, |F| < 2^55; its balanced
+            // base-128 digits, least significant first, are exact integer operations
+            const double y = (k0 < K) ? ldexp(tile[rr][tx], 6 - sexp[rr] + 7 * (s - 1)) : 0.0;
+            long long F = isfinite(y) ? __double2ll_rn(y) : 0ll;
             __half *o = out + (size_t)r * Kpad + k;
-            for (int p = 0; p < s; p++) {
-                const double d = rint(y);
-                o[p * plane] = __double2half(d);
-                y = (y - d) * 128.0;
+            for (int p = s - 1; p > 0; p--) {
+                const long long d = ((F + 64) & 127) - 64;
+                o[p * plane] = __int2half_rn((int)d);
+                F = (F - d) >> 7;
             }
+            o[0] = __int2half_rn((int)F);
         }
         __syncthreads();
     }
@@ -159,6 +164,7 @@ __global__ void __launch_bounds__(192, 1) k_oz_gemm(const __grid_constant__ CUte
     uint64_t *full = bars, *empty = bars + OZ_STAGES, *afull = bars + 2 * OZ_STAGES, *aempty = afull + 2;
     volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(bars + 2 * OZ_STAGES + 4);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 2 * OZ_STAGES + 5);
+    double *stage = reinterpret_cast<double *>(smem + OZ_STAGES * OZ_STAGE_BYTES + 256);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int s = a.s;
@@ -324,28 +330,40 @@ __global__ void __launch_bounds__(192, 1) k_oz_gemm(const __grid_constant__ CUte
             }
             if (stop) break;
             // the tile's result: C = beta C + alpha 2^{eA + eB - 12} (head + tail), or the
-            // unscaled partial of this K split
+            // unscaled partial of this K split.  Each warp stages its 32 rows x 32
+            // columns in shared memory and writes them row by row, coalesced.
             const int4 tile = a.tiles[t];
-            const int m = tile.x * OZ_BM + lb + lane;
+            const int mrow = tile.x * OZ_BM + lb;
             const int n0 = tile.y * OZ_BN;
-            const int em = (m < a.M) ? a.ea[m] : 0;
+            const int m = mrow + lane;
+            const double rs = ldexp(1.0, ((m < a.M) ? a.ea[m] : 0) - 12);
             const bool split = a.part != nullptr;
-            for (int c0 = 0; c0 < OZ_BN; c0 += 16) {
-                uint32_t hl[32];
-                tmem_ld32(tmem + trow + OZ_SUM_COL + (uint32_t)(2 * c0), hl);
+            double *st = stage + (size_t)(warp - 2) * 32 * 33;
+            for (int c0 = 0; c0 < OZ_BN; c0 += 32) {
+                uint32_t h1[32], h2[32];
+                tmem_ld32(tmem + trow + OZ_SUM_COL + (uint32_t)(2 * c0), h1);
+                tmem_ld32(tmem + trow + OZ_SUM_COL + (uint32_t)(2 * c0 + 32), h2);
                 tmem_wait_ld();
-                if (m < a.M) {
-                    double *crow = split ? a.part + ((size_t)tile.z * a.M + m) * a.N : a.C + (size_t)m * a.ldc;
-#pragma unroll 4
-                    for (int j = 0; j < 16; j++) {
-                        const int n = n0 + c0 + j;
-                        if (n >= a.N || (a.lower && n > m)) continue;
-                        const double v = ((double)__uint_as_float(hl[2 * j]) + (double)__uint_as_float(hl[2 * j + 1]));
-                        const double r = ldexp(v, em + a.eb[n] - 12);
-                        if (split) crow[n] = r;
-                        else crow[n] = (a.beta == 0.0) ? a.alpha * r : fma(a.beta, crow[n], a.alpha * r);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    st[lane * 33 + j] = ((double)__uint_as_float(h1[2 * j]) + (double)__uint_as_float(h1[2 * j + 1])) * rs;
+                    st[lane * 33 + 16 + j] = ((double)__uint_as_float(h2[2 * j]) + (double)__uint_as_float(h2[2 * j + 1])) * rs;
+                }
+                __syncwarp();
+                const int n = n0 + c0 + lane;
+                const double cs = (n < a.N) ? ldexp(1.0, a.eb[n]) : 0.0;
+                for (int rr = 0; rr < 32; rr++) {
+                    const int mm = mrow + rr;
+                    if (mm >= a.M || n >= a.N || (a.lower && n > mm)) continue;
+                    const double v = st[rr * 33 + lane] * cs;
+                    if (split) {
+                        a.part[((size_t)tile.z * a.M + mm) * a.N + n] = v;
+                    } else {
+                        double *cp = a.C + (size_t)mm * a.ldc + n;
+                        *cp = (a.beta == 0.0) ? a.alpha * v : fma(a.beta, *cp, a.alpha * v);
                     }
                 }
+                __syncwarp();
             }
             tc_fence_before();
             __syncwarp();

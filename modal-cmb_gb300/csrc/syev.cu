@@ -6,22 +6,23 @@
 //
 // 1. Householder tridiagonalisation A = Q T Q^T (lower, blocked; the algorithm
 //    of LAPACK's dsytrd/dlatrd).  Each panel of TRD_NB columns is one
-//    cooperative launch, one CTA per SM, whose CTAs meet at a software grid
-//    barrier twice per column: (a) finish the previous column's w vector and
-//    update the next column with the panel's rank-2c correction, reduce its
-//    norm; (b) form the reflector and the product y = A v over the trailing
-//    matrix (the FP64 matrix-vector product that bounds this stage).  The
-//    panel's compact-WY factor T (dlarft, forward) is built from the same
-//    inner products.  After a panel, A22 -= V W^T + W V^T on the lower
-//    triangle by the tiled FP64 GEMM, mirrored to the upper one.
+//    cooperative launch, one CTA per SM, each CTA owning a block of rows kept
+//    in shared memory; the CTAs meet at a grid barrier twice per column: (a) finish the previous column's w vector and update the
+//    next column with the panel's rank-2c correction, reduce its norm; (b)
+//    form the reflector and the product y = A v over the trailing matrix (the
+//    FP64 matrix-vector product that bounds this stage).  After a panel,
+//    A22 -= V W^T + W V^T on the lower triangle as an FP64-accurate
+//    tensor-core product (ozgemm.cu), mirrored to the upper one.
 // 2. Divide and conquer on T (Cuppen; Dongarra-Sorensen deflation; Gu-Eisenstat
 //    eigenvectors).  The tree is split down to single rows; every level's
 //    merges run batched: sort and deflate (one CTA per merge), secular roots
 //    (one warp per root, rational two-pole steps safeguarded by bisection),
 //    zhat and the eigenvectors of the rank-one problem (one warp per row),
-//    then the vector update as a grouped FP64 GEMM.
-// 3. Back-transformation of the wanted eigenvectors, X <- X Q^T, by the
-//    panels' compact-WY blocks in reverse order (FP64 GEMMs).
+//    then the vector update: a grouped FP64 GEMM for small merges, the
+//    tensor-core FP64-accurate product for merges of DC_OZ_MIN rows or more.
+// 3. Back-transformation of the wanted eigenvectors, X <- X Q^T, by compact-WY
+//    blocks of NBB reflectors in reverse order (dlarft on the blocks' Gram
+//    matrices; tensor-core FP64-accurate products).
 //
 // Layout: row-major; eigenvectors are stored as rows (row j of V is the
 // eigenvector of W[j]).  Every spin-wait is bounded; on expiry a device error
@@ -42,6 +43,7 @@ constexpr int LDP = 2 * TRD_NB;            // panel row: V (TRD_NB columns) then
 constexpr int PCOMP = 2 * TRD_NB + 2;      // partial components: p[NB], q[NB], y.v, |x|^2
 constexpr int NBB = 256;                   // reflectors per block of the back-transformation
 constexpr int OZ_SLICES = 8;               // 7-bit slices of the tensor-core FP64 products
+constexpr int DC_OZ_MIN = 1024;            // merges of at least this size update their vectors on the tensor cores
 constexpr long long BAR_CYCLES = 1ll << 32;  // ~2 s of clock64 per barrier wait
 constexpr double EPS = 1.1102230246251565e-16;  // 2^-53
 
@@ -66,9 +68,11 @@ __device__ __forceinline__ double warp_max(double v)
     return v;
 }
 
-// Software grid barrier for a cooperative launch (all CTAs co-resident).
-// bar[0] counts arrivals, bar[1] is the generation.  Bounded: a wait that runs
-// out of its clock64 budget sets *err; every CTA returns false once *err is set.
+// Grid barrier for a cooperative launch (all CTAs co-resident), one per phase:
+// bar[0] counts arrivals, bar[1] is the generation.  Measured faster here
+// than per-CTA flag words that every CTA polls (152 x 152 pollers on a few L2
+// lines).  Bounded: a wait that runs out of its clock64 budget sets *err, and
+// every CTA returns false once *err is set.
 __device__ bool grid_barrier(unsigned *bar, int *err)
 {
     __syncthreads();
@@ -97,15 +101,6 @@ __device__ bool grid_barrier(unsigned *bar, int *err)
     return *(volatile int *)err == 0;
 }
 
-// Rows [lo, hi) split in equal contiguous parts over the grid.
-__device__ __forceinline__ void my_rows(int lo, int hi, int &r0, int &r1)
-{
-    const int cnt = hi - lo;
-    const int per = (cnt + (int)gridDim.x - 1) / (int)gridDim.x;
-    r0 = min(hi, lo + (int)blockIdx.x * per);
-    r1 = min(hi, r0 + per);
-}
-
 // ------------------------------------------------------------------ stage 1
 
 struct TrdArgs {
@@ -115,7 +110,7 @@ struct TrdArgs {
     double *d, *e, *tau;
     double *a, *y;  // [n] work vectors
     double *part;   // [PCOMP][grid] per-CTA partial sums
-    unsigned *bar;
+    unsigned *bar;  // grid barrier: arrivals, generation
     int *err;
 };
 
@@ -128,94 +123,104 @@ __device__ __forceinline__ double grid_total(const double *part, int comp, int l
     return warp_sum(s);
 }
 
+// Panel of the tridiagonalisation (dlatrd, lower) as one cooperative launch.
+// The CTA owns a fixed block of rows [rb0, rb1) of [j0, n) for the whole panel
+// and keeps their V, W, y and updated-column entries in shared memory; only
+// reductions over all rows and the head row of each reflector go through
+// global memory.  Shared memory: v (n doubles) | V rows | W rows (R x NB each) | y | a.
 __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
 {
-    extern __shared__ double sv[];  // v of the current column, indexed from row i+1
+    extern __shared__ double sm[];
     __shared__ double s_pq[2 * TRD_NB + 2];
     __shared__ double s_vi[TRD_NB], s_wi[TRD_NB];
     __shared__ double s_red[TRD_WARPS];
     __shared__ double s_scal[4];
 
     const int n = g.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int G = gridDim.x;
+    const int G = gridDim.x, b = blockIdx.x;
+    const int R = (n - g.j0 + G - 1) / G;
+    const int rb0 = min(n, g.j0 + b * R), rb1 = min(n, rb0 + R);
+    double *sv = sm, *Vs = sv + n, *Ws = Vs + (size_t)R * TRD_NB, *ys = Ws + (size_t)R * TRD_NB, *as = ys + R;
+    for (int e = tid; e < 2 * R * TRD_NB; e += blockDim.x) Vs[e] = 0.0;
+    __syncthreads();
+
     for (int c = 0; c <= g.nbp; c++) {
         const int i = g.j0 + c;  // column reduced now; head row of reflector c - 1
-        int r0, r1;
-        my_rows(i, n, r0, r1);
+        const int x0 = max(rb0, i);
+        double nrm = 0.0;
         // ---------------- phase X: finish w of column c - 1, update column i
         if (c > 0) {
             const int cp = c - 1;
             const int ncomp = 2 * cp + 1;
-            for (int t = warp; t < ncomp; t += TRD_WARPS) {
-                const int comp = t < cp ? t : (t < 2 * cp ? TRD_NB + (t - cp) : 2 * TRD_NB);
-                const double v = grid_total(g.part, comp, lane);
-                if (lane == 0) s_pq[t] = v;  // p[0..cp), q[0..cp), y.v
+            {   // grid sums of the previous phase's partials, 8 threads per component
+                const int ci = tid >> 3, sub = tid & 7;
+                double s = 0.0;
+                if (ci < ncomp) {
+                    const int comp = ci < cp ? ci : (ci < 2 * cp ? TRD_NB + (ci - cp) : 2 * TRD_NB);
+                    const double *pp = g.part + (size_t)comp * G;
+#pragma unroll 4
+                    for (int bb = sub; bb < G; bb += 8) s += pp[bb];
+                }
+                s += __shfl_xor_sync(0xffffffffu, s, 1);
+                s += __shfl_xor_sync(0xffffffffu, s, 2);
+                s += __shfl_xor_sync(0xffffffffu, s, 4);
+                if (ci < ncomp && sub == 0) s_pq[ci] = s;  // p[0..cp), q[0..cp), y.v
             }
             __syncthreads();
             const double taup = g.tau[i - 1];
-            if (tid == 0) {
-                double pq = 0.0;
-                for (int t = 0; t < cp; t++) pq += s_pq[t] * s_pq[cp + t];
-                s_scal[0] = s_pq[2 * cp] - 2.0 * pq;  // (corrected y).v
-            }
-            __syncthreads();
-            const double yvc = s_scal[0];
             const double *p = s_pq, *q = s_pq + cp;
-            // w of row i (head row), computed by every CTA alike
-            if (tid == 0) {
-                double s = g.y[i];
-                for (int t = 0; t < cp; t++) s -= g.V[(size_t)i * LDP + t] * q[t] + g.W[(size_t)i * LDP + t] * p[t];
-                s_scal[1] = taup * s - 0.5 * taup * taup * yvc * 1.0;
-            }
-            __syncthreads();
-            const double whead = s_scal[1];
-            // rows of this CTA: w (stored), then the column update of column i
-            if (c < g.nbp) {
-                for (int t = tid; t < c; t += blockDim.x) {
-                    s_vi[t] = g.V[(size_t)i * LDP + t];
-                    s_wi[t] = (t == cp) ? whead : g.W[(size_t)i * LDP + t];
+            if (warp == 0) {
+                const double *Vi = g.V + (size_t)i * LDP, *Wi = g.W + (size_t)i * LDP;
+                double pq = 0.0, hv = 0.0;
+                if (lane < cp) {
+                    pq = p[lane] * q[lane];
+                    hv = Vi[lane] * q[lane] + Wi[lane] * p[lane];
+                }
+                pq = warp_sum(pq);
+                hv = warp_sum(hv);
+                const double yvc = s_pq[2 * cp] - 2.0 * pq;  // (corrected y).v
+                // w of row i (head row: v = 1 there), computed by every CTA alike
+                const double whead = taup * (g.y[i] - hv) - 0.5 * taup * taup * yvc;
+                if (lane == 0) { s_scal[0] = yvc; s_scal[1] = whead; }
+                if (c < g.nbp && lane < c) {
+                    s_vi[lane] = Vi[lane];
+                    s_wi[lane] = (lane == cp) ? whead : Wi[lane];
                 }
             }
             __syncthreads();
-            double nrm = 0.0;
-            for (int r = r0 + tid; r < r1; r += blockDim.x) {
-                double s = g.y[r];
-                const double *Vr = g.V + (size_t)r * LDP, *Wr = g.W + (size_t)r * LDP;
+            const double yvc = s_scal[0], whead = s_scal[1];
+            for (int r = x0 + tid; r < rb1; r += blockDim.x) {
+                const int lr = r - rb0;
+                double *Vr = Vs + (size_t)lr * TRD_NB, *Wr = Ws + (size_t)lr * TRD_NB;
+                double s = ys[lr];
                 for (int t = 0; t < cp; t++) s -= Vr[t] * q[t] + Wr[t] * p[t];
                 const double wr = (r == i) ? whead : taup * s - 0.5 * taup * taup * yvc * Vr[cp];
+                Wr[cp] = wr;
                 g.W[(size_t)r * LDP + cp] = wr;
                 if (c < g.nbp) {
                     double x = g.A[(size_t)r * n + i];
-                    for (int t = 0; t < cp; t++) x -= Vr[t] * s_wi[t] + Wr[t] * s_vi[t];
-                    x -= Vr[cp] * whead + wr * s_vi[cp];
+                    for (int t = 0; t < c; t++) x -= Vr[t] * s_wi[t] + Wr[t] * s_vi[t];
+                    as[lr] = x;
                     g.a[r] = x;
                     if (r >= i + 2) nrm += x * x;
                 }
             }
             if (c == g.nbp) break;
-            nrm = warp_sum(nrm);
-            if (lane == 0) s_red[warp] = nrm;
-            __syncthreads();
-            if (tid == 0) {
-                double s = 0.0;
-                for (int w = 0; w < TRD_WARPS; w++) s += s_red[w];
-                g.part[(size_t)(2 * TRD_NB + 1) * G + blockIdx.x] = s;
-            }
         } else {
-            double nrm = 0.0;
-            for (int r = r0 + tid; r < r1; r += blockDim.x) {
+            for (int r = x0 + tid; r < rb1; r += blockDim.x) {
                 const double x = g.A[(size_t)r * n + i];
+                as[r - rb0] = x;
                 g.a[r] = x;
                 if (r >= i + 2) nrm += x * x;
             }
-            nrm = warp_sum(nrm);
-            if (lane == 0) s_red[warp] = nrm;
-            __syncthreads();
-            if (tid == 0) {
-                double s = 0.0;
-                for (int w = 0; w < TRD_WARPS; w++) s += s_red[w];
-                g.part[(size_t)(2 * TRD_NB + 1) * G + blockIdx.x] = s;
-            }
+        }
+        nrm = warp_sum(nrm);
+        if (lane == 0) s_red[warp] = nrm;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0.0;
+            for (int w = 0; w < TRD_WARPS; w++) s += s_red[w];
+            g.part[(size_t)(2 * TRD_NB + 1) * G + b] = s;
         }
         if (!grid_barrier(g.bar, g.err)) return;
 
@@ -233,7 +238,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                     scale = 1.0 / (alpha - beta);
                 }
                 s_scal[2] = scale;
-                if (blockIdx.x == 0) {
+                if (b == 0) {
                     g.d[i] = g.a[i];
                     g.e[i] = beta;
                     g.tau[i] = tau;
@@ -245,21 +250,30 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         const int m = n - i - 1;  // trailing size
         for (int k = tid; k < m; k += blockDim.x) sv[k] = (k == 0) ? 1.0 : g.a[i + 1 + k] * scale;
         __syncthreads();
-        my_rows(i + 1, n, r0, r1);
+        const int y0 = max(rb0, i + 1);
         // warp per row: y[r] = sum_k A[r][i+1+k] v[k]
-        for (int r = r0 + warp; r < r1; r += TRD_WARPS) {
+        for (int r = y0 + warp; r < rb1; r += TRD_WARPS) {
             const double *Ar = g.A + (size_t)r * n + i + 1;
-            double s0 = 0.0, s1 = 0.0;
+            // eight independent loads in flight per lane: the trailing matrix streams from HBM/L2
+            double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
             int k = lane;
-            for (; k + 32 < m; k += 64) {
-                s0 = fma(Ar[k], sv[k], s0);
-                s1 = fma(Ar[k + 32], sv[k + 32], s1);
+            for (; k + 7 * 32 < m; k += 8 * 32) {
+                double x[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) x[u] = Ar[k + 32 * u];
+#pragma unroll
+                for (int u = 0; u < 8; u++) acc[u] = fma(x[u], sv[k + 32 * u], acc[u]);
             }
-            if (k < m) s0 = fma(Ar[k], sv[k], s0);
-            const double s = warp_sum(s0 + s1);
+#pragma unroll
+            for (int u = 0; u < 7; u++)
+                if (k + 32 * u < m) acc[u] = fma(Ar[k + 32 * u], sv[k + 32 * u], acc[u]);
+            const double s = warp_sum(((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
             if (lane == 0) {
+                const double vr = sv[r - i - 1];
+                ys[r - rb0] = s;
                 g.y[r] = s;
-                g.V[(size_t)r * LDP + c] = sv[r - i - 1];
+                Vs[(size_t)(r - rb0) * TRD_NB + c] = vr;
+                g.V[(size_t)r * LDP + c] = vr;
             }
         }
         __syncthreads();
@@ -267,15 +281,15 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         const int ncomp = 2 * c + 1;
         for (int t = warp; t < ncomp; t += TRD_WARPS) {
             double s = 0.0;
-            for (int r = r0 + lane; r < r1; r += 32) {
+            for (int r = y0 + lane; r < rb1; r += 32) {
+                const int lr = r - rb0;
                 const double vr = sv[r - i - 1];
-                const double x = t < c ? g.V[(size_t)r * LDP + t]
-                                       : (t < 2 * c ? g.W[(size_t)r * LDP + (t - c)] : g.y[r]);
+                const double x = t < c ? Vs[(size_t)lr * TRD_NB + t] : (t < 2 * c ? Ws[(size_t)lr * TRD_NB + (t - c)] : ys[lr]);
                 s += x * vr;
             }
             s = warp_sum(s);
             const int comp = t < c ? t : (t < 2 * c ? TRD_NB + (t - c) : 2 * TRD_NB);
-            if (lane == 0) g.part[(size_t)comp * G + blockIdx.x] = s;
+            if (lane == 0) g.part[(size_t)comp * G + b] = s;
         }
         if (!grid_barrier(g.bar, g.err)) return;
     }
@@ -759,6 +773,17 @@ __global__ void k_dc_zero_half(DcWork w)
     w.Zn[(size_t)w.rank[M.a + r] * n + colb + c] = 0.0;
 }
 
+// Rows of a large merge's vector update, computed densely into Zt ([kk][b - a],
+// row j = root j), moved to their final positions in Zn.
+__global__ void k_dc_scatter(DcWork w, int mix, const double *__restrict__ Zt)
+{
+    const MergeInfo M = w.mi[mix];
+    const int j = blockIdx.y, k = M.b - M.a;
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= M.kk || col >= k) return;
+    w.Zn[(size_t)w.rank[M.a + j] * w.n + M.a + col] = Zt[(size_t)j * k + col];
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ host side
@@ -779,7 +804,7 @@ struct SyevPtrs {
     long ldva;
     unsigned *bar;
     int *err;
-    double *lam, *Z, *Zn, *U, *Zc;
+    double *lam, *Z, *Zn, *U, *Zc, *Zt;
     int *srt, *kl, *kci, *flg, *dl, *org, *rank, *pos2m;
     double *Ds, *zs, *kd, *kw, *rtau, *zh;
     int2 *grot;
@@ -806,13 +831,14 @@ static size_t carve(uint8_t *base, int n, int npanel, int nlev, int nmerge, Syev
     p.a = (double *)take(sizeof(double) * n);
     p.y = (double *)take(sizeof(double) * n);
     p.part = (double *)take(sizeof(double) * PCOMP * 1024);
-    p.bar = (unsigned *)take(sizeof(unsigned) * 2);
+    p.bar = (unsigned *)take(sizeof(unsigned) * 1024);
     p.err = (int *)take(sizeof(int) * 2);
     p.lam = (double *)take(sizeof(double) * n);
     p.Z = (double *)take(sizeof(double) * NN);
     p.Zn = (double *)take(sizeof(double) * NN);
     p.U = (double *)take(sizeof(double) * NN);
     p.Zc = (double *)take(sizeof(double) * NN);
+    p.Zt = (double *)take(sizeof(double) * NN);
     p.srt = (int *)take(sizeof(int) * n);
     p.kl = (int *)take(sizeof(int) * n);
     p.kci = (int *)take(sizeof(int) * n);
@@ -881,15 +907,20 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
     MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     MODAL_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
     if (!coop) { set_error("eigensolver: the device has no cooperative launch"); return MODAL_ERR_CUDA; }
-    const size_t smem = sizeof(double) * (size_t)std::max(1, n);
-    if (smem > 200 * 1024) { set_error("eigensolver: n = %d exceeds the panel kernel's shared-memory vector", n); return MODAL_ERR_ARG; }
+    // CTAs per panel: one per SM for large trailing matrices, fewer (cheaper
+    // barriers and reductions) once the trailing matrix is small
+    auto grid_of = [&](int rows) { return std::max(1, std::min(std::min(nsm, 1024), ceil_div(rows, 16))); };
+    int Rmax = 1;
+    for (int j0 = 0; j0 < n - 1; j0 += TRD_NB) Rmax = std::max(Rmax, ceil_div(n - j0, grid_of(n - j0)));
+    // v (n) + this CTA's V and W rows (Rmax x NB each) + y and a (Rmax each)
+    const size_t smem = sizeof(double) * ((size_t)n + (size_t)Rmax * (2 * TRD_NB + 2));
+    if (smem > 200 * 1024) { set_error("eigensolver: n = %d exceeds the panel kernel's shared memory", n); return MODAL_ERR_ARG; }
     MODAL_CUDA(cudaFuncSetAttribute(k_trd_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     MODAL_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trd_panel, TRD_THREADS, smem));
     if (per_sm < 1) { set_error("eigensolver: panel kernel does not fit on an SM"); return MODAL_ERR_CUDA; }
-    int G = std::min(nsm, std::max(1, (n + 15) / 16));
-    G = std::min(G, 1024);
     MODAL_CUDA(cudaMemsetAsync(p.err, 0, 2 * sizeof(int), ctx->stream));
+    MODAL_CUDA(cudaMemsetAsync(p.bar, 0, 2 * sizeof(unsigned), ctx->stream));
     MODAL_CUDA(cudaMemsetAsync(p.VA, 0, sizeof(double) * (size_t)n * p.ldva, ctx->stream));
     MODAL_TRY(oz_reset(ctx));
     OzOpts oz;
@@ -900,13 +931,13 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
         const int j0 = pi * TRD_NB;
         const int nbp = std::min(TRD_NB, n - 1 - j0);  // reflectors 0 .. n-2
         MODAL_CUDA(cudaMemsetAsync(p.P, 0, sizeof(double) * (size_t)n * LDP, ctx->stream));
-        MODAL_CUDA(cudaMemsetAsync(p.bar, 0, 2 * sizeof(unsigned), ctx->stream));
         TrdArgs g;
         g.A = A; g.n = n; g.j0 = j0; g.nbp = nbp;
         g.V = p.P;
         g.W = p.P + TRD_NB;
         g.d = p.d; g.e = p.e; g.tau = p.tau; g.a = p.a; g.y = p.y; g.part = p.part; g.bar = p.bar; g.err = p.err;
         void *args[] = {&g};
+        const int G = grid_of(n - j0);
         MODAL_CUDA(cudaLaunchCooperativeKernel((const void *)k_trd_panel, dim3(G), dim3(TRD_THREADS), args, smem, ctx->stream));
         MODAL_TRY(launched(ctx, "trd_panel"));
         k_panel_post<<<ceil_div((long)n * LDP, 256), 256, 0, ctx->stream>>>(n, j0, nbp, p.P, p.Psw, p.VA, p.ldva);
@@ -965,9 +996,34 @@ static modal_status dc_run(modal_ctx *ctx, int n, SyevState &st, SyevPtrs &p)
         MODAL_TRY(launched(ctx, "dc_rank"));
         k_dc_gather<<<dim3(ceil_div(kmax, 128), kmax, nm), 128, 0, ctx->stream>>>(w);
         MODAL_TRY(launched(ctx, "dc_gather"));
-        const long tiles = (long)ceil_div(kmax, DT) * ceil_div(hmax, DT);
-        k_dc_gemm<<<dim3((unsigned)tiles, 1, 2 * nm), 256, 0, ctx->stream>>>(w);
-        MODAL_TRY(launched(ctx, "dc_gemm"));
+        if (kmax >= DC_OZ_MIN) {
+            // large merges: the two half products on the tensor cores (FP64 accuracy),
+            // sized from the merge descriptors
+            std::vector<MergeInfo> hm(nm);
+            MODAL_CUDA(cudaMemcpyAsync(hm.data(), w.mi, sizeof(MergeInfo) * nm, cudaMemcpyDeviceToHost, ctx->stream));
+            MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
+            OzOpts o;
+            o.slices = OZ_SLICES;
+            o.check = false;
+            for (int x = 0; x < nm; x++) {
+                const MergeInfo &M = hm[x];
+                const int k = M.b - M.a, kk = M.kk;
+                if (kk == 0) continue;
+                const int K0 = M.k1 + M.k2, K1 = kk - M.k1;
+                const double *Ub = p.U + (size_t)M.a * n + M.a, *Zb = p.Zc + (size_t)M.a * n;
+                if (K0 > 0)
+                    MODAL_TRY(oz_gemm_ex(ctx, kk, M.m - M.a, K0, 1.0, Ub, n, false, Zb + M.a, n, false, 0.0, p.Zt, k, o));
+                if (K1 > 0)
+                    MODAL_TRY(oz_gemm_ex(ctx, kk, M.b - M.m, K1, 1.0, Ub + M.k1, n, false, Zb + (size_t)M.k1 * n + M.m, n,
+                                         false, 0.0, p.Zt + (M.m - M.a), k, o));
+                k_dc_scatter<<<dim3(ceil_div(k, 128), kk), 128, 0, ctx->stream>>>(w, x, p.Zt);
+                MODAL_TRY(launched(ctx, "dc_scatter"));
+            }
+        } else {
+            const long tiles = (long)ceil_div(kmax, DT) * ceil_div(hmax, DT);
+            k_dc_gemm<<<dim3((unsigned)tiles, 1, 2 * nm), 256, 0, ctx->stream>>>(w);
+            MODAL_TRY(launched(ctx, "dc_gemm"));
+        }
         k_dc_zero_half<<<dim3(ceil_div(hmax, 128), kmax, 2 * nm), 128, 0, ctx->stream>>>(w);
         MODAL_TRY(launched(ctx, "dc_zero_half"));
         k_dc_lam<<<dim3(ceil_div(kmax, 256), nm), 256, 0, ctx->stream>>>(w);

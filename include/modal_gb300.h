@@ -88,7 +88,8 @@ typedef enum {
     MODAL_T_EIG_TRD = 10, /* eigensolver: Householder tridiagonalisation */
     MODAL_T_EIG_DC = 11,  /* eigensolver: divide and conquer on the tridiagonal matrix */
     MODAL_T_EIG_BACK = 12, /* eigensolver: back-transformation of the kept eigenvectors */
-    MODAL_T_COUNT = 13
+    MODAL_T_TC = 13,      /* every FP64-accuracy tensor-core product kernel (k_oz_gemm) */
+    MODAL_T_COUNT = 14
 } modal_timer;
 modal_status modal_ctx_profile(modal_ctx *ctx, int enable);
 modal_status modal_ctx_timer(modal_ctx *ctx, int timer, double *ms, long *count);

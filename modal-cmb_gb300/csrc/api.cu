@@ -165,7 +165,7 @@ void modal_ctx_destroy(modal_ctx *c)
                       &c->modesr, &c->scratch, &c->scratch2, &c->shape_tab, &c->shape_desc, &c->slab_order,
                       &c->split, &c->tr_x, &c->tr_qt, &c->tr_prim, &c->tr_mt, &c->tr_v, &c->tr_out,
                       &c->adj, &c->adj2, &c->adj3, &c->prune, &c->gemm_part, &c->qe, &c->me, &c->tri_pol, &c->gamma_pol,
-                      &c->tr_qte, &c->tr_we, &c->tr_mte, &c->prim, &c->eigw, &c->ozw, &c->ozerr};
+                      &c->tr_qte, &c->tr_we, &c->tr_mte, &c->prim, &c->eigw, &c->ozw, &c->ozerr, &c->ozrun};
     batch_release(c);
     for (DevBuf *b : bufs) release(*b);
     timers_clear(c);
@@ -389,11 +389,12 @@ modal_status modal_init_glint(modal_ctx *c)
         StageTimer t(c, MODAL_T_PL);
         MODAL_TRY(legendre_table_dev(c, c->nmu, lmax_all, c->mu.as<double>(), c->pl.as<double>()));
     }
-    {
+    // the FP64 M table (calculate_orthoMij_T) is made on first use by the FP64
+    // paths (mt_ready); the split form contracts the P_l table on the tensor cores
+    c->have_mt = false;
+    if (c->have_basis_e) {  // calculate_orthoMij_E (orthogonalisation_late.c:131-157)
         StageTimer t(c, MODAL_T_MIJ);
-        MODAL_TRY(mij_dev(c));
-        if (c->have_basis_e)  // calculate_orthoMij_E (orthogonalisation_late.c:131-157)
-            MODAL_TRY(mij_table_dev(c, c->qe.as<double>(), c->lmin_e, c->lmax_e, c->P_e, c->me));
+        MODAL_TRY(mij_table_dev(c, c->qe.as<double>(), c->lmin_e, c->lmax_e, c->P_e, c->me));
     }
     MODAL_TRY(sync(c));
     c->have_glint = true;
@@ -408,6 +409,7 @@ modal_status modal_get_mij(modal_ctx *c, double *out)
     MODAL_CUDA(cudaSetDevice(c->device));
     const int P = c->P, nmu = c->nmu;
     // device [nmu][P*P] -> reference Mij_T[P][P][nmu]
+    MODAL_TRY(mt_ready(c));
     MODAL_TRY(ensure(c->scratch2, sizeof(double) * (size_t)nmu * P * P));
     MODAL_TRY(transpose_dev(c, c->mt.as<double>(), c->scratch2.as<double>(), nmu, P * P));
     MODAL_TRY(d2h(c, out, c->scratch2.ptr, sizeof(double) * (size_t)nmu * P * P));

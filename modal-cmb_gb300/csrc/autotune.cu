@@ -177,6 +177,7 @@ modal_status modal_autotune(modal_ctx *c, const char *cache_path)
 
     // ---- FP64 Gamma kernel: mu steps per shared-memory stage
     if (!c->have_glint) MODAL_TRY(modal_init_glint(c));
+    MODAL_TRY(mt_ready(c));
     const std::string kg = "gamma64 " + arch + " P=" + std::to_string(P) + " nmu=" + std::to_string(c->nmu);
     int gv[1] = {0};
     if (cache_lookup(cache_path, kg, gv, 1)) {

@@ -1,6 +1,7 @@
 // common.cuh -- context state and helpers shared by the CUDA translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
@@ -34,6 +35,7 @@ struct modal_ctx {
     bool have_basis = false, have_modes = false, have_user_gl = false;
     bool have_glint = false, have_gamma = false, have_spec = false, have_ortho = false;
     bool have_beta = false;
+    bool have_mt = false;   // M table of the current quadrature computed (made on first use by the FP64 paths)
     int ortho_branch = 0, ortho_rank = 0;
     double pca_floor = 0.0;  // PCA keeps eigenvalues > pca_floor * e_max (0: the reference's > 0)
     modal::BatchGraph *batch = nullptr;  // captured batched-projection graph (batch.cu)
@@ -104,6 +106,7 @@ struct modal_ctx {
     modal::DevBuf eigw;        // eigensolver workspace (syev.cu)
     modal::DevBuf ozw;         // tensor-core FP64 products: operand slices, exponents, tiles (ozgemm.cu)
     modal::DevBuf ozerr;       // their sticky error word
+    modal::DevBuf ozrun;       // their work-item lists and K-split partial sums
 
     // profiling: event pairs per stage, summed on read
     bool profile = false;
@@ -167,6 +170,8 @@ struct StageTimer {
 modal_status gl_nodes_dev(modal_ctx *ctx, int n, double *d_mu, double *d_w);
 modal_status legendre_table_dev(modal_ctx *ctx, int nmu, int lmax, const double *d_mu, double *d_pl);
 modal_status mij_dev(modal_ctx *ctx);
+// The FP64 M table of the current basis and quadrature, computed on first use.
+modal_status mt_ready(modal_ctx *ctx);
 modal_status mij_table_dev(modal_ctx *ctx, const double *q, int lmin, int lmax, int P, DevBuf &out);
 // Gamma over the quadrature nodes mu0 .. mu0 + nmu - 1 (all of them: mu0 = 0, nmu = ctx->nmu).
 modal_status gamma_fp64_dev(modal_ctx *ctx, int mu0, int nmu);
@@ -243,6 +248,20 @@ struct OzOpts {
     int ksplit = 0;      // K split over work items (0: fill the GPU)
     bool check = true;   // synchronise and report an expired wait now (else: oz_check later)
 };
+// Sliced operand of the tensor-core product: [s][rows_pad][Kpad] FP16 digits and
+// the per-row exponents (rows_pad a multiple of 128, Kpad of 64).
+struct OzOperand {
+    __half *slices;
+    int *ex;
+    int rows, rows_pad;
+};
+// Digits of the rows of op(X) (R x K; trans: element (r, k) = X[k*ld + r]).
+modal_status oz_slice(modal_ctx *ctx, int R, int K, const double *X, long ld, bool trans, int s, int Rpad, int Kpad,
+                      __half *out, int *ex);
+// C (M x N = A.rows x B.rows) = beta C + alpha A B^T over pre-sliced operands;
+// tile_list: the 128 x 128 output tiles to compute (NULL: all, or per o.lower / o.diag_tiles).
+modal_status oz_run(modal_ctx *ctx, const OzOperand &A, const OzOperand &B, int Kpad, int s,
+                    const std::vector<int2> *tile_list, double alpha, double beta, double *C, long ldc, const OzOpts &o);
 modal_status oz_reset(modal_ctx *ctx);  // clear the sticky error word of unchecked calls
 modal_status oz_check(modal_ctx *ctx);  // synchronise; MODAL_ERR_TIMEOUT if any call's wait expired
 modal_status oz_gemm_ex(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, long lda, bool transA,

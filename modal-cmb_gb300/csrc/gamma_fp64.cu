@@ -98,6 +98,15 @@ modal_status mij_dev(modal_ctx *ctx)
     return mij_table_dev(ctx, ctx->q.as<double>(), ctx->lmin, ctx->lmax, ctx->P, ctx->mt);
 }
 
+modal_status mt_ready(modal_ctx *ctx)
+{
+    if (ctx->have_mt) return MODAL_OK;
+    StageTimer t(ctx, MODAL_T_MIJ);
+    MODAL_TRY(mij_dev(ctx));
+    ctx->have_mt = true;
+    return MODAL_OK;
+}
+
 // --------------------------------------------------------------------------
 // mu-contraction, FP64.  One CTA per 32x32 tile of (m,n) with tile(m) <= tile(n);
 // thread (tx,ty) owns n = n0+tx and m = m0+ty+8r, r < 4.  A chunk of KC mu
@@ -171,6 +180,7 @@ __global__ void __launch_bounds__(256) k_gamma_fp64(int N, int P, int nmu, int K
 modal_status gamma_fp64_dev(modal_ctx *ctx, int mu0, int nmu)
 {
     const int N = ctx->N, P = ctx->P;
+    MODAL_TRY(mt_ready(ctx));
     MODAL_TRY(ensure(ctx->gamma, sizeof(double) * (size_t)N * N));
     MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * nmu));
     k_wgt48<<<ceil_div(nmu, 256), 256, 0, ctx->stream>>>(nmu, ctx->w.as<double>() + mu0, ctx->scratch2.as<double>());

@@ -434,32 +434,43 @@ modal_status oz_map(CUtensorMap *m, const void *base, long rows, int Kpad, int b
 // only the 128-row tiles (tm, tn) with tm / diag_tiles == tn / diag_tiles
 // (the diagonal blocks of that many tiles); o.ksplit: K split over that many
 // work items per tile (0: chosen to fill the GPU), partials added in order.
-modal_status oz_gemm_ex(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, long lda, bool transA,
-                        const double *B, long ldb, bool transB, double beta, double *C, long ldc, const OzOpts &o)
+modal_status oz_slice(modal_ctx *ctx, int R, int K, const double *X, long ld, bool trans, int s, int Rpad, int Kpad,
+                      __half *out, int *ex)
 {
+    if (Rpad % OZ_BM || Kpad % 64 || R > Rpad || K > Kpad || s < 2 || s > OZ_MAXS) {
+        set_error("oz_slice: bad layout (R=%d Rpad=%d K=%d Kpad=%d s=%d)", R, Rpad, K, Kpad, s);
+        return MODAL_ERR_ARG;
+    }
+    k_oz_slice<<<Rpad / 32, 256, 0, ctx->stream>>>(R, K, Rpad, Kpad, X, ld, trans ? 1 : 0, s, out, ex);
+    return launched(ctx, "oz_slice");
+}
+
+modal_status oz_run(modal_ctx *ctx, const OzOperand &A, const OzOperand &B, int Kpad, int s,
+                    const std::vector<int2> *tile_list, double alpha, double beta, double *C, long ldc, const OzOpts &o)
+{
+    const int M = A.rows, N = B.rows, Mpad = A.rows_pad, Npad = B.rows_pad;
     if (M <= 0 || N <= 0) return MODAL_OK;
-    const int s = o.slices;
-    if (s < 2 || s > OZ_MAXS) { set_error("oz_gemm: slices %d outside [2, %d]", s, OZ_MAXS); return MODAL_ERR_ARG; }
-    if (K <= 0) {
-        if (beta == 1.0) return MODAL_OK;
-        set_error("oz_gemm: K = %d with beta != 1", K);
+    if (s < 2 || s > OZ_MAXS || Mpad % OZ_BM || Npad % OZ_BM || Kpad % 64 || Kpad <= 0) {
+        set_error("oz_run: bad layout (Mpad=%d Npad=%d Kpad=%d s=%d)", Mpad, Npad, Kpad, s);
         return MODAL_ERR_ARG;
     }
     MODAL_TRY(oz_encoder());
-    const int Mpad = ceil_div(M, OZ_BM) * OZ_BM, Npad = ceil_div(N, OZ_BN) * OZ_BN;
-    const int Kpad = ceil_div(K, 64) * 64;
     const int ntm = Mpad / OZ_BM, ntn = Npad / OZ_BN;
     const int nkb = ceil_div(Kpad, OZ_KB);
     int nsm = 0;
     MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
-    std::vector<int2> base;
-    // tile order: column of tiles outer so that consecutive CTAs share B slices in L2
-    for (int tn = 0; tn < ntn; tn++)
-        for (int tm = 0; tm < ntm; tm++) {
-            if (o.lower && tn > tm) continue;
-            if (o.diag_tiles > 0 && tm / o.diag_tiles != tn / o.diag_tiles) continue;
-            base.push_back(make_int2(tm, tn));
-        }
+    std::vector<int2> own;
+    if (!tile_list) {
+        // tile order: column of tiles outer so that consecutive CTAs share B slices in L2
+        for (int tn = 0; tn < ntn; tn++)
+            for (int tm = 0; tm < ntm; tm++) {
+                if (o.lower && tn > tm) continue;
+                if (o.diag_tiles > 0 && tm / o.diag_tiles != tn / o.diag_tiles) continue;
+                own.push_back(make_int2(tm, tn));
+            }
+    }
+    const std::vector<int2> &base = tile_list ? *tile_list : own;
+    if (base.empty()) return MODAL_OK;
     int ks = o.ksplit;
     if (ks <= 0) ks = (int)std::min<long>(nkb, std::max<long>(1, (long)nsm / std::max<size_t>(1, base.size())));
     ks = std::max(1, std::min(ks, nkb));
@@ -471,28 +482,17 @@ modal_status oz_gemm_ex(modal_ctx *ctx, int M, int N, int K, double alpha, const
         for (const int2 &t : base) tiles.push_back(make_int4(t.x, t.y, z, 0));
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     size_t off = 0;
-    const size_t o_a = off; off += al((size_t)s * Mpad * Kpad * 2);
-    const size_t o_b = off; off += al((size_t)s * Npad * Kpad * 2);
-    const size_t o_ea = off; off += al((size_t)Mpad * 4);
-    const size_t o_eb = off; off += al((size_t)Npad * 4);
     const size_t o_t = off; off += al(tiles.size() * sizeof(int4));
     const size_t o_p = off; off += (ks > 1) ? al((size_t)ks * M * N * 8) : 0;
-    MODAL_TRY(ensure(ctx->ozw, off));
-    uint8_t *b = ctx->ozw.as<uint8_t>();
-    __half *As = reinterpret_cast<__half *>(b + o_a), *Bs = reinterpret_cast<__half *>(b + o_b);
-    int *ea = reinterpret_cast<int *>(b + o_ea), *eb = reinterpret_cast<int *>(b + o_eb);
+    MODAL_TRY(ensure(ctx->ozrun, off));
+    uint8_t *b = ctx->ozrun.as<uint8_t>();
     MODAL_TRY(ensure(ctx->ozerr, 256));
     int *err = ctx->ozerr.as<int>();
     MODAL_CUDA(cudaMemcpyAsync(b + o_t, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
     if (o.check) MODAL_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
-    k_oz_slice<<<Mpad / 32, 256, 0, ctx->stream>>>(M, K, Mpad, Kpad, A, lda, transA ? 1 : 0, s, As, ea);
-    MODAL_TRY(launched(ctx, "oz_slice"));
-    // columns of op(B) = rows of op(B)^T: transB ? B[n*ldb + k] (rows of B) : B[k*ldb + n] (columns of B)
-    k_oz_slice<<<Npad / 32, 256, 0, ctx->stream>>>(N, K, Npad, Kpad, B, ldb, transB ? 0 : 1, s, Bs, eb);
-    MODAL_TRY(launched(ctx, "oz_slice"));
     CUtensorMap ma, mb;
-    MODAL_TRY(oz_map(&ma, As, (long)s * Mpad, Kpad, OZ_BM));
-    MODAL_TRY(oz_map(&mb, Bs, (long)s * Npad, Kpad, OZ_BN));
+    MODAL_TRY(oz_map(&ma, A.slices, (long)s * Mpad, Kpad, OZ_BM));
+    MODAL_TRY(oz_map(&mb, B.slices, (long)s * Npad, Kpad, OZ_BN));
     OzArgs g;
     g.M = M; g.N = N; g.Kpad = Kpad; g.Mpad = Mpad; g.Npad = Npad; g.s = s;
     g.nkb = nkb;
@@ -501,17 +501,49 @@ modal_status oz_gemm_ex(modal_ctx *ctx, int M, int N, int K, double alpha, const
     g.lower = o.lower;
     g.tiles = reinterpret_cast<const int4 *>(b + o_t);
     g.part = ks > 1 ? reinterpret_cast<double *>(b + o_p) : nullptr;
-    g.ea = ea; g.eb = eb; g.alpha = alpha; g.beta = beta; g.C = C; g.ldc = ldc; g.err = err;
+    g.ea = A.ex; g.eb = B.ex; g.alpha = alpha; g.beta = beta; g.C = C; g.ldc = ldc; g.err = err;
     MODAL_CUDA(cudaFuncSetAttribute(k_oz_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZ_SMEM));
     const int grid = std::max(1, std::min(g.ntiles, nsm));
-    k_oz_gemm<<<grid, 192, OZ_SMEM, ctx->stream>>>(ma, mb, g);
-    MODAL_TRY(launched(ctx, "oz_gemm"));
+    {
+        StageTimer t(ctx, MODAL_T_TC);
+        k_oz_gemm<<<grid, 192, OZ_SMEM, ctx->stream>>>(ma, mb, g);
+        MODAL_TRY(launched(ctx, "oz_gemm"));
+    }
     if (ks > 1) {
         k_oz_reduce<<<ceil_div((long)M * N, 256), 256, 0, ctx->stream>>>(M, N, ks, g.part, alpha, beta, C, ldc, o.lower);
         MODAL_TRY(launched(ctx, "oz_reduce"));
     }
     // unchecked calls leave the (sticky) error word for oz_check
     return o.check ? oz_check(ctx) : MODAL_OK;
+}
+
+modal_status oz_gemm_ex(modal_ctx *ctx, int M, int N, int K, double alpha, const double *A, long lda, bool transA,
+                        const double *B, long ldb, bool transB, double beta, double *C, long ldc, const OzOpts &o)
+{
+    if (M <= 0 || N <= 0) return MODAL_OK;
+    const int s = o.slices;
+    if (s < 2 || s > OZ_MAXS) { set_error("oz_gemm: slices %d outside [2, %d]", s, OZ_MAXS); return MODAL_ERR_ARG; }
+    if (K <= 0) {
+        if (beta == 1.0) return MODAL_OK;
+        set_error("oz_gemm: K = %d with beta != 1", K);
+        return MODAL_ERR_ARG;
+    }
+    const int Mpad = ceil_div(M, OZ_BM) * OZ_BM, Npad = ceil_div(N, OZ_BN) * OZ_BN;
+    const int Kpad = ceil_div(K, 64) * 64;
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    size_t off = 0;
+    const size_t o_a = off; off += al((size_t)s * Mpad * Kpad * 2);
+    const size_t o_b = off; off += al((size_t)s * Npad * Kpad * 2);
+    const size_t o_ea = off; off += al((size_t)Mpad * 4);
+    const size_t o_eb = off; off += al((size_t)Npad * 4);
+    MODAL_TRY(ensure(ctx->ozw, off));
+    uint8_t *b = ctx->ozw.as<uint8_t>();
+    OzOperand oa{reinterpret_cast<__half *>(b + o_a), reinterpret_cast<int *>(b + o_ea), M, Mpad};
+    OzOperand ob{reinterpret_cast<__half *>(b + o_b), reinterpret_cast<int *>(b + o_eb), N, Npad};
+    MODAL_TRY(oz_slice(ctx, M, K, A, lda, transA, s, Mpad, Kpad, oa.slices, oa.ex));
+    // columns of op(B) = rows of op(B)^T: transB ? B[n*ldb + k] (rows of B) : B[k*ldb + n] (columns of B)
+    MODAL_TRY(oz_slice(ctx, N, K, B, ldb, !transB, s, Npad, Kpad, ob.slices, ob.ex));
+    return oz_run(ctx, oa, ob, Kpad, s, nullptr, alpha, beta, C, ldc, o);
 }
 
 modal_status oz_reset(modal_ctx *ctx)

@@ -160,6 +160,7 @@ modal_status modal_gamma_pol(modal_ctx *c, double *gamma_tte, double *gamma_tee,
     if (!c->have_pol) { set_error("modal_gamma_pol: set the polarised modes first"); return MODAL_ERR_STATE; }
     MODAL_CUDA(cudaSetDevice(c->device));
     if (!c->have_glint) MODAL_TRY(modal_init_glint(c));
+    MODAL_TRY(mt_ready(c));
     const int N = c->N, PT = c->P, PE = c->P_e, nmu = c->nmu;
     const size_t NN = (size_t)N * N;
     MODAL_TRY(ensure(c->gamma_pol, sizeof(double) * 3 * NN));

@@ -35,10 +35,10 @@ import numpy as np  # noqa: E402
 METRIC = "Gamma+ortho s and shape projections/s, split-prec vs FP64, GB300, rel err<=1e-6"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64 (nominal; no measured FP64 peak is available)
-# From the ncu capture of k_gamma_lift at cfg2 (profiles/gamma_lift_cfg2.md):
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch, and tensor-pipe activity.
-TRAFFIC_LIFT_CFG2 = 1.356191e9 + 46.257152e6
-NCU_TENSOR_ACTIVE_CFG2 = 50.6
+# DRAM bytes (read + write) of the tridiagonalisation's panel kernels in one
+# eigen-decomposition at l <= 2000, P = 30 (N = 4960), from an ncu capture of
+# those kernels, not from this run (None until captured).
+NCU_PANEL_TRAFFIC_CFG2 = None
 
 
 def parse():
@@ -208,7 +208,8 @@ def run_ours(a, ws, rank, local):
         clocks = clk.stop() if clk else None
         barrier()
         launches = ctx.launches - launches0
-        tm = {k: ctx.timer(k) for k in ("gl", "pl", "mij", "gamma", "lift", "ortho", "project", "alpha")}
+        tm = {k: ctx.timer(k) for k in ("gl", "pl", "mij", "gamma", "lift", "tc", "ortho", "eig_trd", "eig_panel",
+                                        "eig_dc", "eig_back", "project", "alpha")}
         return np.array(times), wall, launches, tm, clocks
 
     times, wall, launches, tm, clocks = run(prec, a.steps, a.warmup)
@@ -253,15 +254,20 @@ def run_ours(a, ws, rank, local):
         # alpha with a PCA eigenvalue floor above the split form's Gamma error:
         # the same FP64 orthogonalisation of each Gamma, keeping eigenvalues > floor * e_max
         fl = {}
+        probes = np.random.default_rng(7).standard_normal((4, N))
         for floor in (1e-6, 1e-4):
             ctx.set_pca_floor(floor)
-            _, _, _, r64 = ctx.orthogonalise(G64, download=False)
+            _, lam64, _, r64 = ctx.orthogonalise(G64)
             af64, _ = ctx.alpha(S_cmp, b64)
-            _, _, _, rs = ctx.orthogonalise(Gs, download=False)
+            _, lams, _, rs = ctx.orthogonalise(Gs)
             afs, _ = ctx.alpha(S_cmp, bs)
+            # the kept-subspace operator lambda^T lambda (orthoinv) on random probes
+            p64, ps = lam64.T @ (lam64 @ probes.T), lams.T @ (lams @ probes.T)
             fl["%g" % floor] = {"kept_fp64": r64, "kept_split": rs,
                                 "alpha_fro": float(np.linalg.norm(afs - af64) / np.linalg.norm(af64)),
-                                "alpha_gamma_norm": float(np.max(gnorm(afs - af64) / gnorm(af64)))}
+                                "alpha_gamma_norm": float(np.max(gnorm(afs - af64) / gnorm(af64))),
+                                "orthoinv_probe_fro": float(np.linalg.norm(ps - p64) / np.linalg.norm(p64))}
+            del lam64, lams
         ctx.set_pca_floor(0.0)
         extra["rel_err_vs_fp64"]["alpha_with_pca_floor"] = fl
 
@@ -287,61 +293,82 @@ def run_ours(a, ws, rank, local):
             torch.cuda.synchronize()
             p_ms.append(e0.elapsed_time(e1))
         p256 = float(np.median(p_ms))
-        fp64_256 = extra.get("fp64_projection_ms", proj_ms) * 256.0 / S
+        # the FP64 form of the same 256 shapes, timed once (device time on the context stream)
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b256_64 = ctx.project(sh256, mg.PREC_FP64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fp64_256 = e0.elapsed_time(e1)
+        beta256_err = float(np.max(np.linalg.norm(b256 - b256_64, axis=1) / np.linalg.norm(b256_64, axis=1)))
         go64 = extra.get("fp64_gamma_ortho_ms", go_ms)
         gos = extra.get("split_gamma_ortho_ms", go_ms)
         extra["projection_256_shapes"] = {
             "path": "modal_project_batch (captured CUDA graph, %d captures)" % ctx.captures,
             "split_ms": p256, "split_projections_per_s": 256.0 / (p256 * 1e-3),
-            "fp64_ms_scaled_from_%d_shapes" % S: fp64_256,
+            "fp64_ms": fp64_256, "split_beta_max_rel_err_vs_fp64": beta256_err,
             "split_vs_fp64_gamma_ortho_plus_256_projections": (go64 + fp64_256) / (gos + p256)}
 
-    # roofline of the dominant kernel of this library on the path: the mu-contraction.
-    # achieved = algorithmic flop of Gamma (18 N(N+1)/2 n_mu, counted once per pair)
-    # / that kernel's mean device time in the timed steps (CUDA events on its stream).
+    # roofline of the dominant kernel of the timed step: the tridiagonalisation's
+    # panel kernel (the FP64 matrix-vector product over the trailing matrix of
+    # every column).  achieved = algorithmic bytes of one eigen-decomposition,
+    # 8 * sum_{m=1}^{N-1} m^2 (the trailing matrix read once per column), / the
+    # panel kernels' device time per eigen-decomposition (CUDA events).
     pk, pk_kind = peaks()
     flops = 18.0 * N * (N + 1) / 2.0 * nmu
-    if prec == mg.PREC_FP64:
-        g_ms, g_n = tm["gamma"]
-        t_ms = g_ms / max(1, g_n)
-        achieved = flops / (t_ms * 1e-3) / 1e12
-        roof = {"bound": "fp64", "achieved": achieved, "peak": FP64_NOMINAL_TFLOPS, "unit": "TFLOP/s",
-                "frac": achieved / FP64_NOMINAL_TFLOPS, "traffic": None,
-                "kernel": "k_gamma_fp64", "kernel_ms": t_ms, "peak_kind": "nominal FP64 (no measured FP64 peak)",
-                "algorithmic": "18 N(N+1)/2 n_mu flop per launch"}
-    else:
-        l_ms, l_n = tm["lift"]
-        t_ms = l_ms / max(1, l_n)
-        achieved = flops / (t_ms * 1e-3) / 1e12
+    hbm = pk.get("hbm_gbs", 6800.0)
+    p_ms, p_n = tm["eig_panel"]
+    o_ms, o_n = tm["ortho"]
+    roof = None
+    if p_n > 0 and o_n > 0:
+        t_ms = p_ms / o_n  # panel kernels per orthogonalisation
+        alg_bytes = 8.0 * (N - 1) * N * (2 * N - 1) / 6.0
+        achieved = alg_bytes / (t_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": NCU_PANEL_TRAFFIC_CFG2 if a.config == "cfg2" else None,
+                "traffic_source": "ncu capture of the panel kernels at this config, not this run",
+                "kernel": "k_trd_panel (155 launches per eigen-decomposition)", "kernel_ms": t_ms,
+                "peak_kind": pk_kind + " HBM copy bandwidth",
+                "algorithmic": "8 sum_{m<N} m^2 bytes per eigen-decomposition (trailing matrix read per column)",
+                "note": "the product also runs at the FP64 rate: 2 sum m^2 flop = %.1f TFLOP/s of the nominal %.2f"
+                        % (2.0 * alg_bytes / 8.0 / (t_ms * 1e-3) / 1e12, FP64_NOMINAL_TFLOPS)}
+    # the mu-contraction on the tensor cores (split form): algorithmic and executed rates
+    l_ms, l_n = tm["lift"]
+    mu_contraction = None
+    if prec == mg.PREC_SPLIT and l_n > 0:
+        t_ms = l_ms / l_n
         U = P * (P + 1) // 2
-        rows = 0
         UV = U * (U + 1) // 2
         v_of = np.repeat(np.arange(U), np.arange(U, 0, -1))
-        for j in range((UV + 255) // 256):
-            rows += min(256, UV - j * 256) * (v_of[min(UV, (j + 1) * 256) - 1] // 128 + 1)
+        ntiles = 0
+        for j in range((UV + 127) // 128):
+            ntiles += min(v_of[min(UV, (j + 1) * 128) - 1] // 128 + 1, (U + 127) // 128)
         kpad = -(-nmu // 64) * 64
-        executed = 2.0 * 3 * rows * 128 * kpad  # three FP16 products, tiles actually computed
-        peak = pk.get("bf16_tflops", 1933.1)
-        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                "traffic": TRAFFIC_LIFT_CFG2 if a.config == "cfg2" else None,
-                "kernel": "k_gamma_lift", "kernel_ms": t_ms, "peak_kind": pk_kind + " bf16 burst (FP16 dense rate is equal)",
-                "algorithmic": "18 N(N+1)/2 n_mu flop per launch",
-                "executed_tensor_tflops": executed / (t_ms * 1e-3) / 1e12,
-                "executed_frac": executed / (t_ms * 1e-3) / 1e12 / peak,
-                "ncu_tensor_pipe_active_pct": NCU_TENSOR_ACTIVE_CFG2 if a.config == "cfg2" else None}
+        executed = 2.0 * 28 * 128 * 128 * kpad * ntiles  # 7 slices: 28 digit products per tile
+        peak = pk.get("bf16_tflops", 1900.0)
+        mu_contraction = {"kernel": "k_oz_gemm (mu-contraction, 7 exact 7-bit slices)", "kernel_ms": t_ms,
+                          "algorithmic_tflops": flops / (t_ms * 1e-3) / 1e12,
+                          "executed_tensor_tflops": executed / (t_ms * 1e-3) / 1e12,
+                          "executed_frac": executed / (t_ms * 1e-3) / 1e12 / peak, "peak": peak,
+                          "peak_kind": pk_kind + " bf16 burst (FP16 dense rate is equal)",
+                          "algorithmic": "18 N(N+1)/2 n_mu flop per launch"}
 
     # end to end through the C ABI with host buffers
     e2e = run_e2e(ctx, mg, q, tr, cl, shapes, prec, a.steps)
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
-        cpu = cpu_baseline(a.config, lmax, P, q, tr, cl, shapes, samples=1)
+        cpu = cpu_baseline(a.config, lmax, P, q, tr, cl, shapes, gamma=G64)
     ctx.close()
     extras = run_extras(mg, local) if rank == 0 and a.config == "cfg2" else None
     next_rows = run_next_rows(mg, local, not a.no_cpu_baseline) if rank == 0 and a.config == "cfg2" else None
     line = {
         "metric": METRIC, "value": go_ms * 1e-3, "unit": "s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": step_ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == mg.PREC_FP64 else "f16x3 split (hi/lo pieces, 3 products), f32 tile acc, f64 sum",
+        "dtype": "f64" if prec == mg.PREC_FP64 else ("f64 orthogonalisation; Gamma on f16 tensor cores with exact 7-bit "
+                                                     "integer slices (f32 tensor-memory sums exact, double-f32 across "
+                                                     "node blocks), f64 gather"),
         "data": "synthetic (seeded shapes; synthetic C_l; shifted Legendre basis)",
         "config": {"workload": f"{a.config}: l=2..{lmax}, P={P}, N={N}, n_mu={nmu}, S={S} shapes",
                    "l2": "flushed (256 MB write between steps)", "parallelism": f"replicas x{ws}",
@@ -352,6 +379,7 @@ def run_ours(a, ws, rank, local):
         "next_rows": next_rows,
         "stage_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in tm.items()},
         "roofline": roof,
+        "mu_contraction": mu_contraction,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": int(launches),
@@ -543,13 +571,18 @@ def run_e2e(ctx, mg, q, tr, cl, shapes, prec, steps):
 
 # -------------------------------------------------------- CPU reference arm
 
-def cpu_baseline(config, lmax, P, q, tr, cl, shapes, samples=1):
-    """Reference CPU path on the host cores, on bounded samples extrapolated to
-    the full workload: Gamma (P_l table + l-contraction in full, calculate_orthol
-    over a sample of pairs), orthogonalisation (the reference always runs the
-    full eigen-decomposition, ortho_late_mpi.c:775, then Cholesky; timed at a
-    sample size and scaled as N^3) and the projection (calculate_mode_3D over a
-    sample of tetrapyd points per thread)."""
+_GAMMA_CACHE = {}
+
+
+def cpu_baseline(config, lmax, P, q, tr, cl, shapes, gamma=None):
+    """Reference CPU path on the host cores: Gamma (P_l table + l-contraction in
+    full, calculate_orthol over a sample of pairs, extrapolated per pair), the
+    orthogonalisation of the actual normalised Gamma at full size (the
+    reference's gsl_eigen_symmv + PCA outputs, ortho_late_mpi.c:759-805, with
+    LAPACK through numpy standing in for GSL), and the projection
+    (calculate_mode_3D over a sample of tetrapyd points per thread).  gamma:
+    the FP64 Gamma when the caller has it; otherwise it is computed once per
+    process by the CPU restatement (setup, not timed)."""
     import oracle
     cores = os.cpu_count() or 1
     ref = None
@@ -564,7 +597,7 @@ def cpu_baseline(config, lmax, P, q, tr, cl, shapes, samples=1):
     N = len(tr)
     nmu = 3 * lmax // 2 + 1
     total_pairs = N * (N + 1) // 2
-    npairs = min(total_pairs, 20000)
+    npairs = min(total_pairs, 400000)
     if ref is not None:
         # the reference's own init_orthol_glint + calculate_orthoMij_T and calculate_orthol loop
         ref.setup(2, lmax, q, tr, cl)
@@ -575,6 +608,7 @@ def cpu_baseline(config, lmax, P, q, tr, cl, shapes, samples=1):
         t0 = time.perf_counter()
         ref.gamma(nranks=cores, npairs=npairs)
         t_pairs = time.perf_counter() - t0
+        x = w = M = None
     else:
         t0 = time.perf_counter()
         x, w = orc.gl_nodes(nmu)
@@ -585,15 +619,18 @@ def cpu_baseline(config, lmax, P, q, tr, cl, shapes, samples=1):
         orc.gamma_sample(M, w, tr, npairs, nthreads=cores)
         t_pairs = time.perf_counter() - t0
     t_gamma = t_init + t_pairs * total_pairs / npairs
-    # orthogonalisation: eigen (numpy/LAPACK standing in for gsl_eigen_symmv) + Cholesky restatement
-    ns = min(N, 1024)
-    rng = np.random.default_rng(0)
-    A = rng.standard_normal((ns, ns))
-    Gs = A @ A.T + ns * np.eye(ns)
+    # orthogonalisation of the actual normalised Gamma, full size
+    if gamma is None:
+        key = (lmax, P, N)
+        if key not in _GAMMA_CACHE:
+            if M is None:
+                x, w = orc.gl_nodes(nmu)
+                M = orc.mij(orc.legendre_table(x, lmax), 2, lmax, q)
+            _GAMMA_CACHE[key] = orc.gamma(M, w, tr, nthreads=cores)
+        gamma = _GAMMA_CACHE[key]
     t0 = time.perf_counter()
-    np.linalg.eigh(Gs)
-    orc.ortho_cholesky(Gs)
-    t_ortho = (time.perf_counter() - t0) * (N / ns) ** 3
+    inv, lam, r = oracle.ortho_pca(gamma)
+    t_ortho = time.perf_counter() - t0
     # projection sample
     npts_total = orc.tetrapyd_count(2, lmax)
     per_thread = 2000 if N > 1000 else 20000
@@ -605,8 +642,9 @@ def cpu_baseline(config, lmax, P, q, tr, cl, shapes, samples=1):
         orc.project(2, lmax, q, tr, cl, sh, nthreads=cores, max_points=per_thread)
     t_proj = (time.perf_counter() - t0) * npts_total / (per_thread * cores)
     return {"value": t_gamma + t_ortho, "unit": "s", "cores": cores, "kind": kind,
-            "sample": (f"Gamma: l-contraction in full + {npairs} of {total_pairs} pairs; ortho: eigh+Cholesky at "
-                       f"N={ns} scaled by (N/{ns})^3; projection: {per_thread} points/thread of {npts_total}"),
+            "sample": (f"Gamma: l-contraction in full + {npairs} of {total_pairs} pairs, per-pair extrapolation; "
+                       f"ortho: eigen-decomposition and PCA outputs of the actual normalised Gamma at N={N} "
+                       f"(LAPACK via numpy for GSL), in full; projection: {per_thread} points/thread of {npts_total}"),
             "gamma_s": t_gamma, "ortho_s": t_ortho, "projections_per_s": 1.0 / t_proj}
 
 

@@ -89,7 +89,8 @@ typedef enum {
     MODAL_T_EIG_DC = 11,  /* eigensolver: divide and conquer on the tridiagonal matrix */
     MODAL_T_EIG_BACK = 12, /* eigensolver: back-transformation of the kept eigenvectors */
     MODAL_T_TC = 13,      /* every FP64-accuracy tensor-core product kernel (k_oz_gemm) */
-    MODAL_T_COUNT = 14
+    MODAL_T_EIG_PANEL = 14, /* eigensolver: the tridiagonalisation's panel kernels alone */
+    MODAL_T_COUNT = 15
 } modal_timer;
 modal_status modal_ctx_profile(modal_ctx *ctx, int enable);
 modal_status modal_ctx_timer(modal_ctx *ctx, int timer, double *ms, long *count);

@@ -938,8 +938,12 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
         g.d = p.d; g.e = p.e; g.tau = p.tau; g.a = p.a; g.y = p.y; g.part = p.part; g.bar = p.bar; g.err = p.err;
         void *args[] = {&g};
         const int G = grid_of(n - j0);
-        MODAL_CUDA(cudaLaunchCooperativeKernel((const void *)k_trd_panel, dim3(G), dim3(TRD_THREADS), args, smem, ctx->stream));
-        MODAL_TRY(launched(ctx, "trd_panel"));
+        {
+            StageTimer tp(ctx, MODAL_T_EIG_PANEL);
+            MODAL_CUDA(cudaLaunchCooperativeKernel((const void *)k_trd_panel, dim3(G), dim3(TRD_THREADS), args, smem,
+                                                   ctx->stream));
+            MODAL_TRY(launched(ctx, "trd_panel"));
+        }
         k_panel_post<<<ceil_div((long)n * LDP, 256), 256, 0, ctx->stream>>>(n, j0, nbp, p.P, p.Psw, p.VA, p.ldva);
         MODAL_TRY(launched(ctx, "panel_post"));
         const int s = j0 + nbp, rest = n - s;

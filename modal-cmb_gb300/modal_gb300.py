@@ -40,7 +40,8 @@ EXPORTS = [
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9,
-          "eig_trd": 10, "eig_dc": 11, "eig_back": 12, "tc": 13}
+          "eig_trd": 10, "eig_dc": 11, "eig_back": 12, "tc": 13,
+          "eig_panel": 14}
 
 
 class ModalError(RuntimeError):

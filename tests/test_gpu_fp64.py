@@ -183,6 +183,27 @@ def test_cholesky_blocked_large_spd(mg, orc):
     assert np.max(np.abs(lam @ o - np.eye(N))) <= 1e-11
 
 
+
+@pytest.mark.parametrize("lmax,P", [(2000, 30), (2500, 40)])
+def test_gamma_fp64_benchmark_sizes_vs_oracle_pairs(mg, orc, lmax, P):
+    """The FP64 Gamma at the benchmark sizes (l <= 2000, P = 30, N = 4960; l <=
+    2500, P = 40, N = 11480) against the oracle's restatement of
+    calculate_orthol (orthogonalisation_late.c:239-336) on the same nodes, for
+    2000 random (m, n) pairs: within 1e-12 of max |Gamma|."""
+    q, tr, cl = mg.workload(lmax, P)
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.init_glint()
+        G = c.gamma(mg.PREC_FP64)
+        x, w = c.get_gl()
+    M = orc.mij(orc.legendre_table(x, lmax), 2, lmax, q)
+    rng = np.random.default_rng(lmax)
+    pairs = rng.integers(0, len(tr), (2000, 2))
+    ref = np.array([orc.orthol_pair(M, w, tr, int(m), int(n)) for m, n in pairs])
+    got = G[pairs[:, 0], pairs[:, 1]]
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(G))
+
 def test_pca_branch_forced_and_on_failure(mg):
     import oracle
     rng = np.random.default_rng(12)

@@ -1,7 +1,9 @@
-"""Split-precision forms against FP64 on the GPU: the tensor-core Gamma (FP16
-hi/lo pieces), its node-range partials, and the compensated FP32 projection.
-Tolerance: relative Frobenius and relative max error <= 1e-6 (the target for
-the split form); emulation predicts ~5e-8."""
+"""Split-precision forms against FP64 on the GPU: the tensor-core Gamma (both
+contractions on tcgen05 with exact 7-bit integer slices), its node-range
+partials, and the compensated FP32 projection.  Tolerances: the split Gamma
+within 1e-12 of the FP64 Gamma (relative Frobenius and max; measured 1.6e-13 at
+l <= 2000, P = 30); the FP32 projection within 1e-6; alpha and the kept-subspace
+operator lambda^T lambda at PCA floors 1e-6 and 1e-4 within 1e-6."""
 import numpy as np
 import pytest
 from conftest import rel_fro, rel_max
@@ -58,10 +60,10 @@ def test_split_gamma_after_basis_and_range_changes(mg):
             c.init_glint()
             G64 = c.gamma(mg.PREC_FP64)
             Gs = c.gamma(mg.PREC_SPLIT)
-            assert rel_max(Gs, G64) <= 1e-6, lmax
+            assert rel_max(Gs, G64) <= 1e-12, lmax
         nmu = 3 * 200 // 2 + 1
         Sp = c.gamma_partial(mg.PREC_SPLIT, 0, 64) + c.gamma_partial(mg.PREC_SPLIT, 64, nmu)
-        assert rel_max(Sp, G64) <= 1e-6
+        assert rel_max(Sp, G64) <= 1e-12
 
 
 def test_gamma_partials_over_mu_shards(mg):
@@ -83,29 +85,76 @@ def test_gamma_partials_over_mu_shards(mg):
         with pytest.raises(mg.ModalError):  # the device Gamma is a partial now
             c.orthogonalise(None)
     assert rel_max(S64, G64) <= 1e-13
-    assert rel_fro(Ssp, G64) <= 1e-6 and rel_max(Ssp, G64) <= 1e-6
+    assert rel_fro(Ssp, G64) <= 1e-12 and rel_max(Ssp, G64) <= 1e-12
 
 
 @pytest.mark.parametrize("lmin,lmax,P", [(2, 40, 1), (2, 60, 4), (2, 500, 10), (3, 600, 17), (2, 700, 20)])
 def test_split_gamma_vs_fp64(mg, lmin, lmax, P):
     G64, Gs, Gs2 = _both(mg, lmin, lmax, P)
     assert np.all(np.isfinite(Gs))
-    assert rel_fro(Gs, G64) <= 1e-6
-    assert rel_max(Gs, G64) <= 1e-6
+    assert rel_fro(Gs, G64) <= 1e-12
+    assert rel_max(Gs, G64) <= 1e-12
     assert np.array_equal(Gs, Gs.T)
     assert np.array_equal(Gs, Gs2)  # deterministic
 
 
 def test_split_gamma_unsorted_duplicate_modes(mg):
     G64, Gs, _ = _both(mg, 2, 300, 6, triples=[[5, 1, 0], [0, 0, 0], [2, 2, 2], [5, 1, 0], [1, 3, 5]])
-    assert rel_max(Gs, G64) <= 1e-6
+    assert rel_max(Gs, G64) <= 1e-12
 
 
-def test_split_gamma_cfg2(mg):
-    """Full benchmark size: l <= 2000, P = 30, N = 4960, n_mu = 3001."""
-    G64, Gs, _ = _both(mg, 2, 2000, 30)
-    assert rel_fro(Gs, G64) <= 1e-6
-    assert rel_max(Gs, G64) <= 1e-6
+def test_split_gamma_cfg2_alpha_basis_with_floor(mg):
+    """Full benchmark size, l <= 2000, P = 30 (N = 4960, n_mu = 3001): the split
+    Gamma within 1e-12 of FP64; then each Gamma through the same FP64
+    orthogonalisation with a PCA floor (1e-6, 1e-4 of e_max): the same kept rank,
+    alpha = lambda^T lambda beta within 1e-6, and the kept-subspace operator
+    lambda^T lambda (the reference's orthoinv, eigenmodetoday_mpi.c:148-162)
+    within 1e-6 on random probes.  The reference's floor-free rule keeps
+    eigenvalues down to ~1e-13 e_max and is ill-posed at this size (two FP64
+    solvers differ by ~1e-5 there), hence the floors."""
+    lmax, P = 2000, 30
+    q, tr, cl = mg.workload(lmax, P)
+    rng = np.random.default_rng(7)
+    probes = rng.standard_normal((4, len(tr)))
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        c.init_glint()
+        G64 = c.gamma(mg.PREC_FP64)
+        Gs = c.gamma(mg.PREC_SPLIT)
+        assert rel_fro(Gs, G64) <= 1e-12 and rel_max(Gs, G64) <= 1e-12
+        beta = c.project(mg.separable_shapes(lmax, 4, seed=3), mg.PREC_FP64)
+        for floor in (1e-6, 1e-4):
+            c.set_pca_floor(floor)
+            out = []
+            for G in (G64, Gs):
+                _, lam, branch, rank = c.orthogonalise(G)
+                a, _ = c.alpha(4, beta)
+                out.append((rank, a, (lam.T @ (lam @ probes.T)).T))
+            (r64, a64, p64), (rs, as_, ps) = out
+            assert rs == r64, floor
+            assert rel_fro(as_, a64) <= 1e-6, floor
+            assert rel_fro(ps, p64) <= 1e-6, floor
+        c.set_pca_floor(0.0)
+
+
+def test_split_projection_bumps_cfg3(mg):
+    """cfg3's non-separable shapes at full size (l <= 2000, P = 30): 16 Gaussian
+    bumps, sigma from 0.05 to 0.3, in FP32 against FP64, <= 1e-6 each."""
+    lmax, P = 2000, 30
+    q, tr, cl = mg.workload(lmax, P)
+    shapes = mg.bump_shapes(14, seed=33)
+    shapes += [{"kind": mg.SHAPE_BUMP, "c": np.array([0.34, 0.33, 0.33]), "sigma": 0.05},
+               {"kind": mg.SHAPE_BUMP, "c": np.array([0.5, 0.3, 0.2]), "sigma": 0.05}]
+    with mg.Context(0) as c:
+        c.set_basis(2, lmax, q)
+        c.set_modes(tr)
+        c.set_spectrum(cl)
+        b64 = c.project(shapes, mg.PREC_FP64)
+        bs = c.project(shapes, mg.PREC_SPLIT)
+    for s in range(len(shapes)):
+        assert rel_fro(bs[s], b64[s]) <= 1e-6, (s, shapes[s]["sigma"], rel_fro(bs[s], b64[s]))
 
 
 @pytest.mark.parametrize("lmin,lmax,P,S", [(2, 60, 4, 3), (2, 500, 10, 9), (5, 300, 33, 5), (2, 800, 40, 6)])
@@ -133,7 +182,7 @@ def test_split_projection_vs_fp64(mg, lmin, lmax, P, S):
 
 def test_split_cfg5_largest_config(mg):
     """The largest configuration, l <= 2500, P = 40 (N = 11480, n_mu = 3751):
-    split Gamma within 1e-6 of FP64 (relative Frobenius and max), symmetric and
+    split Gamma within 1e-12 of FP64 (relative Frobenius and max), symmetric and
     reproducible; two shapes projected in FP32 within the P = 40 bound (2e-6)
     of FP64."""
     lmax, P = 2500, 40
@@ -150,7 +199,7 @@ def test_split_cfg5_largest_config(mg):
         b64 = c.project(shapes, mg.PREC_FP64)
         bs = c.project(shapes, mg.PREC_SPLIT)
     assert G64.shape == (11480, 11480)
-    assert rel_fro(Gs, G64) <= 1e-6 and rel_max(Gs, G64) <= 1e-6
+    assert rel_fro(Gs, G64) <= 1e-12 and rel_max(Gs, G64) <= 1e-12
     assert np.array_equal(Gs, Gs.T) and np.array_equal(Gs, Gs2)
     for s in range(2):
         assert rel_fro(bs[s], b64[s]) <= 2e-6, (s, rel_fro(bs[s], b64[s]))

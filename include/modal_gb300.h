@@ -447,9 +447,9 @@ modal_status modal_lambda_min(modal_ctx *ctx, double *lambda_min, double *eigvec
 /* ------------------------------------------------- allocation-free Gamma */
 
 /* FP64 Gamma for callers that cannot allocate device memory: code running
- * inside an engine or CUDA-graph executor that owns every device byte and
- * forbids cudaMalloc/cudaFree (which synchronise the device and fragment
- * its arena), or a plugin that is handed pre-allocated buffers.  No
+ * inside an engine that owns every device byte and forbids cudaMalloc/cudaFree
+ * (which synchronise the device and fragment its arena), or a plugin that is
+ * handed pre-allocated buffers.  No
  * counterpart in the reference (it allocates with malloc on the host).
  *
  * All buffers are DEVICE pointers owned by the caller: d_q[L][P] basis
@@ -465,7 +465,9 @@ modal_status modal_lambda_min(modal_ctx *ctx, double *lambda_min, double *eigvec
  * lmax <= 600 with P <= 6, fit) are rejected with MODAL_ERR_ARG and a
  * message giving the size needed; no device memory is ever allocated.  The
  * first call on a device looks up the array's device address and should
- * come before any stream capture.  All calls share the array: calls that
+ * come before any stream capture; that address is kept for the life of the
+ * process, so do not reset the device while the library is loaded.  Every
+ * call reads a status word back and waits for `stream` before returning.  All calls share the array: calls that
  * overlap on the GPU (different streams or threads) race, so serialise them.
  * Out-of-range triples give MODAL_ERR_ARG. */
 #define MODAL_NOALLOC_SCRATCH_BYTES (8u << 20)

@@ -81,7 +81,8 @@ struct modal_ctx {
     modal::DevBuf tr_prim;     // [Nprim][3]
     modal::DevBuf tr_mt;       // [xsize][nmu][Pp][P]
     modal::DevBuf tr_v;        // [lmax+1] weights
-    modal::DevBuf tr_out;      // [N][Nprim] (polarised: [3][N][Nprim])
+    modal::DevBuf tr_out;      // [XG][N][Nprim] partial sums per radial-sample group (polarised: group g of
+                               // form f at (3g + f) N Nprim); only the first slice holds the result after the reduction
     bool tr_pol = false;       // E side of the transfer functions installed
     modal::DevBuf tr_qte;      // [xsize][Pp][lmax+1] E transfer functions
     modal::DevBuf tr_we;       // [2][lmax+1] E weights (q~_E factor, q~_T leakage factor)

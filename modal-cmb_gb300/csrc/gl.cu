@@ -84,17 +84,28 @@ __global__ void k_pl_factors(int lmax, double *pw)
     if (l <= lmax) pw[l] = pow(2.0 * l + 1.0, 2.0 / 3.0);
 }
 
-// One thread per node and one warp per block, so that the n_mu independent
-// recurrences spread over as many SMs as possible: the recurrence is serial in
-// l and GB300's FP64 rate per SM is low, so the number of SMs in use, not the
-// bytes written, sets the time.  The arithmetic is gsl_sf_legendre_Pl's
-// upward recurrence exactly, (x (2l-1) P_{l-1} - (l-1) P_{l-2}) / l: folding
-// the division into precomputed factors moves the table by ~1e-12 at l = 500
-// (the coefficient roundings accumulate coherently along l), which would
-// show in Gamma's 1e-12 parity with the reference.
-__global__ void __launch_bounds__(32) k_legendre_table(int nmu, int lmax, const double *__restrict__ mu,
-                                                       const double *__restrict__ pw, double *__restrict__ pl)
+// One thread per node, so that the n_mu independent recurrences spread over as
+// many warps as possible: the recurrence is serial in l and GB300's FP64 rate
+// per SM is low, so the length of the FP64 dependency chain, not the bytes
+// written, sets the time (~1.45 ms for 3001 nodes to l = 2000: 33 GB/s of
+// table).  The arithmetic is gsl_sf_legendre_Pl's upward recurrence exactly,
+// (x (2l-1) P_{l-1} - (l-1) P_{l-2}) / l, with the integer factors read as
+// doubles from shared memory (the same values, so the same bits; it saves
+// three integer-to-FP64 conversions per step, 10%).  Folding the division into
+// precomputed reciprocals is faster but moves the table by ~1e-12 at l = 500
+// (the roundings accumulate coherently along l), which would show in Gamma's
+// 1e-12 parity with the reference.
+constexpr int PL_WPB = 4;  // warps per block
+__global__ void __launch_bounds__(32 * PL_WPB) k_legendre_table(int nmu, int lmax, const double *__restrict__ mu,
+                                                                const double *__restrict__ pw, double *__restrict__ pl)
 {
+    extern __shared__ double tab[];  // [lmax+1][3]: 2l - 1, l - 1, l
+    for (int l = threadIdx.x; l <= lmax; l += blockDim.x) {
+        tab[3 * l] = (double)(2 * l - 1);
+        tab[3 * l + 1] = (double)(l - 1);
+        tab[3 * l + 2] = (double)l;
+    }
+    __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nmu) return;
     const double x = mu[k];
@@ -103,7 +114,7 @@ __global__ void __launch_bounds__(32) k_legendre_table(int nmu, int lmax, const 
     if (lmax >= 1) pl[(size_t)nmu + k] = pw[1] * x;
     double pm2 = 1.0, pm1 = x;
     for (int l = 2; l <= lmax; l++) {
-        const double pr = (x * (2 * l - 1) * pm1 - (l - 1) * pm2) / l;
+        const double pr = (x * tab[3 * l] * pm1 - tab[3 * l + 1] * pm2) / tab[3 * l + 2];
         pm2 = pm1;
         pm1 = pr;
         double p = pr;
@@ -120,7 +131,10 @@ modal_status legendre_table_dev(modal_ctx *ctx, int nmu, int lmax, const double 
     double *pw = ctx->scratch2.as<double>();
     k_pl_factors<<<ceil_div(lmax + 1, 256), 256, 0, ctx->stream>>>(lmax, pw);
     MODAL_TRY(launched(ctx, "pl_factors"));
-    k_legendre_table<<<ceil_div(nmu, 32), 32, 0, ctx->stream>>>(nmu, lmax, d_mu, pw, d_pl);
+    const size_t smem = sizeof(double) * 3 * (size_t)(lmax + 1);
+    if (smem > 200 * 1024) { set_error("legendre table: lmax = %d too large", lmax); return MODAL_ERR_ARG; }
+    MODAL_CUDA(cudaFuncSetAttribute(k_legendre_table, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_legendre_table<<<ceil_div(nmu, 32 * PL_WPB), 32 * PL_WPB, smem, ctx->stream>>>(nmu, lmax, d_mu, pw, d_pl);
     return launched(ctx, "legendre_table");
 }
 

@@ -1,11 +1,11 @@
 // noalloc.cu -- FP64 Gamma that allocates no device memory.
 //
 // Who needs this: code that runs where device allocation is not allowed or
-// not possible -- inside a CUDA-graph-driven or arena-managed engine that
-// owns all device memory and forbids cudaMalloc/cudaFree (they synchronise
-// the device and fragment the arena), plugins loaded into a host process
-// that hands them pre-allocated buffers, and tight loops where an allocation
-// per call would stall.  Such callers pass device buffers for the inputs and
+// not possible -- inside an arena-managed engine that owns all device memory
+// and forbids cudaMalloc/cudaFree (they synchronise the device and fragment
+// the arena), plugins loaded into a host process that hands them
+// pre-allocated buffers, and tight loops where an allocation per call would
+// stall.  Such callers pass device buffers for the inputs and
 // the output; every intermediate (quadrature, P_l table, l-contraction)
 // lives in one fixed array compiled into this library.
 //
@@ -16,7 +16,10 @@
 // on each device (with that device current) the entry point asks the runtime
 // for the real address with cudaGetSymbolAddress and remembers it; later
 // calls on that device reuse it.  That first call should therefore come
-// before any stream capture.
+// before any stream capture.  The address is kept for the life of the
+// process, so the device must not be reset (cudaDeviceReset) while the
+// library is loaded.  Every call reads a status word back and waits for its
+// stream before returning.
 //
 // Every call shares the one array and overwrites it; the kernels fully
 // rewrite every region they read, so nothing needs clearing between calls.
@@ -99,6 +102,8 @@ extern "C" modal_status modal_gamma_fp64_noalloc(int lmin, int lmax, int P, cons
     }
     if (own_nodes) nmu = 3 * lmax / 2 + 1;  // orthogonalisation_late.c:37
     if (nmu < 1) { set_error("modal_gamma_fp64_noalloc: nmu=%d", nmu); return MODAL_ERR_ARG; }
+    // the P_l table kernel keeps 3 (lmax + 1) doubles in shared memory (<= 48 KB)
+    if (lmax > 2000) { set_error("modal_gamma_fp64_noalloc: lmax=%d above 2000", lmax); return MODAL_ERR_ARG; }
     const int npair = P * (P + 1) / 2;
     // scratch layout: status, triples[3N], wg[nmu], pw[lmax+1], pairs[npair], mu[nmu], w[nmu],
     //                 pl[(lmax+1) nmu], mt[nmu P P]
@@ -151,7 +156,9 @@ extern "C" modal_status modal_gamma_fp64_noalloc(int lmin, int lmax, int P, cons
         w = w_s;
     }
     k_pl_factors<<<ceil_div(lmax + 1, 256), 256, 0, s>>>(lmax, pw);
-    k_legendre_table<<<ceil_div(nmu, 32), 32, 0, s>>>(nmu, lmax, mu, pw, pl);
+    // the table kernel keeps its integer factors in 3 (lmax + 1) doubles of shared
+    // memory (at most 24 KB for the problems the scratch array admits)
+    k_legendre_table<<<ceil_div(nmu, 32), 32, sizeof(double) * 3 * (size_t)(lmax + 1), s>>>(nmu, lmax, mu, pw, pl);
     k_noalloc_pairs<<<1, 1, 0, s>>>(P, pairs, status);
     k_noalloc_triples<<<ceil_div(3L * N, 256), 256, 0, s>>>(N, P, d_triples, triples, status);
     dim3 gm(ceil_div(nmu, NA_MIJ_BK), ceil_div(npair, NA_MIJ_BU));

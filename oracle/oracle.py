@@ -22,7 +22,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libmodaloracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libmodalref.so")
-REFERENCE_DIR = "/root/reference"
+# the reference checkout (only for compiling it in place; absent on GPU machines)
+REFERENCE_DIR = os.environ.get("MODAL_REFERENCE_DIR", "/root/reference")
 
 
 def _shape_args(shape):

@@ -10,9 +10,11 @@
 //    in shared memory; the CTAs meet at a grid barrier twice per column: (a) finish the previous column's w vector and update the
 //    next column with the panel's rank-2c correction, reduce its norm; (b)
 //    form the reflector and the product y = A v over the trailing matrix (the
-//    FP64 matrix-vector product that bounds this stage).  After a panel,
-//    A22 -= V W^T + W V^T on the lower triangle as an FP64-accurate
-//    tensor-core product (ozgemm.cu), mirrored to the upper one.
+//    matrix-vector product that bounds this stage, summed in double-float
+//    FP32 arithmetic over a (head, tail) copy of the trailing matrix).  After
+//    a panel, A22 -= V W^T + W V^T on the lower triangle as an FP64-accurate
+//    tensor-core product (ozgemm.cu), and the trailing block's double-float
+//    copy is refreshed from it.
 // 2. Divide and conquer on T (Cuppen; Dongarra-Sorensen deflation; Gu-Eisenstat
 //    eigenvectors).  The tree is split down to single rows; every level's
 //    merges run batched: sort and deflate (one CTA per merge), secular roots
@@ -104,7 +106,9 @@ __device__ bool grid_barrier(unsigned *bar, int *err)
 // ------------------------------------------------------------------ stage 1
 
 struct TrdArgs {
-    double *A;
+    double *A;          // FP64, lower triangle current (the column updates read it)
+    const float2 *Ahl;  // the trailing matrix, both triangles, as double-float (head, tail) pairs
+    float2 *ahl;        // [n] the updated column as double-float pairs
     int n, j0, nbp;
     double *V, *W;  // panel: rows of LDP doubles, V in columns [0, NB), W in [NB, 2 NB); zero outside the reflectors
     double *d, *e, *tau;
@@ -128,6 +132,13 @@ __device__ __forceinline__ double grid_total(const double *part, int comp, int l
 // and keeps their V, W, y and updated-column entries in shared memory; only
 // reductions over all rows and the head row of each reflector go through
 // global memory.  Shared memory: v (n doubles) | V rows | W rows (R x NB each) | y | a.
+// x = head + tail with |x - head - tail| <= 2^-48 |x|
+__device__ __forceinline__ float2 df_split(double x)
+{
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - (double)h));
+}
+
 __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
 {
     extern __shared__ double sm[];
@@ -140,7 +151,8 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
     const int G = gridDim.x, b = blockIdx.x;
     const int R = (n - g.j0 + G - 1) / G;
     const int rb0 = min(n, g.j0 + b * R), rb1 = min(n, rb0 + R);
-    double *sv = sm, *Vs = sv + n, *Ws = Vs + (size_t)R * TRD_NB, *ys = Ws + (size_t)R * TRD_NB, *as = ys + R;
+    float *svh = reinterpret_cast<float *>(sm), *svl = svh + n;  // the column a as head, tail (v = scale a)
+    double *Vs = sm + n, *Ws = Vs + (size_t)R * TRD_NB, *ys = Ws + (size_t)R * TRD_NB, *as = ys + R;
     for (int e = tid; e < 2 * R * TRD_NB; e += blockDim.x) Vs[e] = 0.0;
     __syncthreads();
 
@@ -202,6 +214,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                     for (int t = 0; t < c; t++) x -= Vr[t] * s_wi[t] + Wr[t] * s_vi[t];
                     as[lr] = x;
                     g.a[r] = x;
+                    g.ahl[r] = df_split(x);
                     if (r >= i + 2) nrm += x * x;
                 }
             }
@@ -211,6 +224,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 const double x = g.A[(size_t)r * n + i];
                 as[r - rb0] = x;
                 g.a[r] = x;
+                g.ahl[r] = df_split(x);
                 if (r >= i + 2) nrm += x * x;
             }
         }
@@ -248,31 +262,77 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         __syncthreads();
         const double scale = s_scal[2];
         const int m = n - i - 1;  // trailing size
-        for (int k = tid; k < m; k += blockDim.x) sv[k] = (k == 0) ? 1.0 : g.a[i + 1 + k] * scale;
+        // v = (1, scale a[i+2..n)): the gemv uses a as double-float pairs and applies scale at the end
+        for (int k = tid; k < m; k += blockDim.x) {
+            const float2 h = (k == 0) ? make_float2(0.f, 0.f) : g.ahl[i + 1 + k];
+            svh[k] = h.x;
+            svl[k] = h.y;
+        }
         __syncthreads();
         const int y0 = max(rb0, i + 1);
-        // warp per row: y[r] = sum_k A[r][i+1+k] v[k]
+        // warp per row: y[r] = A[r][i+1] + scale sum_{k>=1} A[r][i+1+k] a[i+1+k], the sum in
+        // double-float FP32 arithmetic (products split exactly by FMA, heads added by TwoSum):
+        // about 2^-47 relative to sum |A a|, at the FP32 rate instead of GB300's FP64 rate
         for (int r = y0 + warp; r < rb1; r += TRD_WARPS) {
-            const double *Ar = g.A + (size_t)r * n + i + 1;
-            // eight independent loads in flight per lane: the trailing matrix streams from HBM/L2
-            double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-            int k = lane;
-            for (; k + 7 * 32 < m; k += 8 * 32) {
-                double x[8];
+            const float2 *Ar = g.Ahl + (size_t)r * n + i + 1;
+            // elements k = kb.. as 16-byte pairs (four loads of 512 B per warp in flight);
+            // an unaligned element k = 1 and an odd last element go to lane 0
+            const int kb = (((size_t)r * n + i + 2) & 1) ? 2 : 1;
+            const int npair = (m - kb) / 2;
+            const float4 *A4 = reinterpret_cast<const float4 *>(Ar + kb);
+            const float *vbh = svh + kb, *vbl = svl + kb;  // scalar shared-memory reads (kb may be odd)
+            float sh[8], sl[8];
 #pragma unroll
-                for (int u = 0; u < 8; u++) x[u] = Ar[k + 32 * u];
+            for (int u = 0; u < 8; u++) { sh[u] = 0.f; sl[u] = 0.f; }
+            auto acc = [&](float ah, float al, float vh, float vl, float &h, float &l) {
+                const float p = ah * vh;
+                float e = fmaf(ah, vh, -p);
+                e = fmaf(ah, vl, e);
+                e = fmaf(al, vh, e);
+                const float t = h + p, bp = t - h;
+                l += ((h - (t - bp)) + (p - bp)) + e;
+                h = t;
+            };
+            int j = lane;
+            for (; j + 3 * 32 < npair; j += 4 * 32) {
+                float4 x[4];
 #pragma unroll
-                for (int u = 0; u < 8; u++) acc[u] = fma(x[u], sv[k + 32 * u], acc[u]);
+                for (int u = 0; u < 4; u++) x[u] = A4[j + 32 * u];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int e = 2 * (j + 32 * u);
+                    acc(x[u].x, x[u].y, vbh[e], vbl[e], sh[2 * u], sl[2 * u]);
+                    acc(x[u].z, x[u].w, vbh[e + 1], vbl[e + 1], sh[2 * u + 1], sl[2 * u + 1]);
+                }
             }
-#pragma unroll
-            for (int u = 0; u < 7; u++)
-                if (k + 32 * u < m) acc[u] = fma(Ar[k + 32 * u], sv[k + 32 * u], acc[u]);
-            const double s = warp_sum(((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7])));
+            for (; j < npair; j += 32) {
+                const float4 x = A4[j];
+                acc(x.x, x.y, vbh[2 * j], vbl[2 * j], sh[0], sl[0]);
+                acc(x.z, x.w, vbh[2 * j + 1], vbl[2 * j + 1], sh[1], sl[1]);
+            }
             if (lane == 0) {
-                const double vr = sv[r - i - 1];
-                ys[r - rb0] = s;
+                if (kb == 2 && m > 1) {
+                    const float2 x = Ar[1];
+                    acc(x.x, x.y, svh[1], svl[1], sh[2], sl[2]);
+                }
+                if (kb + 2 * npair < m) {
+                    const int k = kb + 2 * npair;
+                    const float2 x = Ar[k];
+                    acc(x.x, x.y, svh[k], svl[k], sh[3], sl[3]);
+                }
+            }
+            double part = 0.0;
+#pragma unroll
+            for (int u = 0; u < 8; u++) part += (double)sh[u] + (double)sl[u];
+            const double ssum = warp_sum(part);
+            if (lane == 0) {
+                const float2 a0 = Ar[0];
+                const double s = fma(scale, ssum, (double)a0.x + (double)a0.y);
+                const int lr = r - rb0;
+                const double vr = (r == i + 1) ? 1.0 : as[lr] * scale;
+                ys[lr] = s;
                 g.y[r] = s;
-                Vs[(size_t)(r - rb0) * TRD_NB + c] = vr;
+                Vs[(size_t)lr * TRD_NB + c] = vr;
                 g.V[(size_t)r * LDP + c] = vr;
             }
         }
@@ -283,7 +343,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             double s = 0.0;
             for (int r = y0 + lane; r < rb1; r += 32) {
                 const int lr = r - rb0;
-                const double vr = sv[r - i - 1];
+                const double vr = (r == i + 1) ? 1.0 : as[lr] * scale;
                 const double x = t < c ? Vs[(size_t)lr * TRD_NB + t] : (t < 2 * c ? Ws[(size_t)lr * TRD_NB + (t - c)] : ys[lr]);
                 s += x * vr;
             }
@@ -295,23 +355,31 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
     }
 }
 
-// Upper triangle of the trailing block [s, n) x [s, n) := its lower triangle.
-__global__ void k_mirror_lower(double *A, int n, int s)
+// The trailing block [s, n) x [s, n) as double-float pairs, both triangles,
+// from the FP64 lower triangle: one CTA per lower 32 x 32 tile writes the
+// tile and its transpose (the diagonal tile reflects within itself).
+__global__ void k_trail_hilo(const double *__restrict__ A, int n, int s, float2 *__restrict__ Ahl)
 {
     __shared__ double tile[32][33];
-    const int tr = blockIdx.y, tc = blockIdx.x;  // tile row, tile column (upper: tc >= tr)
-    if (tc < tr) return;
+    const int tr = blockIdx.y, tc = blockIdx.x;
+    if (tc > tr) return;
     const int r0 = s + tr * 32, c0 = s + tc * 32;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
-    // read the transposed source tile: rows c0.., columns r0..
     for (int k = ty; k < 32; k += 8) {
-        const int rr = c0 + k, cc = r0 + tx;
-        tile[k][tx] = (rr < n && cc < n) ? A[(size_t)rr * n + cc] : 0.0;
+        const int rr = r0 + k, cc = c0 + tx;
+        tile[k][tx] = (rr < n && cc < n && cc <= rr) ? A[(size_t)rr * n + cc] : 0.0;
     }
     __syncthreads();
     for (int k = ty; k < 32; k += 8) {
-        const int rr = r0 + k, cc = c0 + tx;
-        if (rr < n && cc < n && cc > rr) A[(size_t)rr * n + cc] = tile[tx][k];
+        const int rr = r0 + k, cc = c0 + tx;  // (rr, cc) in this tile
+        if (rr < n && cc < n) {
+            const double v = (tc < tr || tx <= k) ? tile[k][tx] : tile[tx][k];
+            Ahl[(size_t)rr * n + cc] = df_split(v);
+        }
+        if (tc < tr) {
+            const int rt = c0 + k, ct = r0 + tx;  // (rt, ct) in the transposed tile
+            if (rt < n && ct < n) Ahl[(size_t)rt * n + ct] = df_split(tile[tx][k]);
+        }
     }
 }
 
@@ -801,6 +869,7 @@ static void build_tree(int a, int b, int lev, std::vector<std::vector<int3>> &ou
 // Carve the eigensolver's workspace out of ctx->eigw for size n.
 struct SyevPtrs {
     double *P, *Psw, *VA, *GB, *TB, *d, *e, *tau, *a, *y, *part;
+    float2 *Ahl, *ahl;
     long ldva;
     unsigned *bar;
     int *err;
@@ -821,6 +890,8 @@ static size_t carve(uint8_t *base, int n, int npanel, int nlev, int nmerge, Syev
     const long nvpad = (long)std::max(1, ceil_div(std::max(1, n - 1), NBB)) * NBB;
     p.ldva = nvpad;
     p.P = (double *)take(sizeof(double) * (size_t)n * LDP);
+    p.Ahl = (float2 *)take(sizeof(float2) * NN);
+    p.ahl = (float2 *)take(sizeof(float2) * n);
     p.Psw = (double *)take(sizeof(double) * (size_t)n * LDP);
     p.VA = (double *)take(sizeof(double) * (size_t)n * nvpad);          // every reflector, column j = v_j
     p.GB = (double *)take(sizeof(double) * (size_t)nvpad * nvpad);      // diagonal NBB blocks of VA^T VA
@@ -922,6 +993,11 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
     MODAL_CUDA(cudaMemsetAsync(p.err, 0, 2 * sizeof(int), ctx->stream));
     MODAL_CUDA(cudaMemsetAsync(p.bar, 0, 2 * sizeof(unsigned), ctx->stream));
     MODAL_CUDA(cudaMemsetAsync(p.VA, 0, sizeof(double) * (size_t)n * p.ldva, ctx->stream));
+    {
+        const int nt = ceil_div(n, 32);
+        k_trail_hilo<<<dim3(nt, nt), 256, 0, ctx->stream>>>(A, n, 0, p.Ahl);
+        MODAL_TRY(launched(ctx, "trail_hilo"));
+    }
     MODAL_TRY(oz_reset(ctx));
     OzOpts oz;
     oz.slices = OZ_SLICES;
@@ -932,7 +1008,7 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
         const int nbp = std::min(TRD_NB, n - 1 - j0);  // reflectors 0 .. n-2
         MODAL_CUDA(cudaMemsetAsync(p.P, 0, sizeof(double) * (size_t)n * LDP, ctx->stream));
         TrdArgs g;
-        g.A = A; g.n = n; g.j0 = j0; g.nbp = nbp;
+        g.A = A; g.Ahl = p.Ahl; g.ahl = p.ahl; g.n = n; g.j0 = j0; g.nbp = nbp;
         g.V = p.P;
         g.W = p.P + TRD_NB;
         g.d = p.d; g.e = p.e; g.tau = p.tau; g.a = p.a; g.y = p.y; g.part = p.part; g.bar = p.bar; g.err = p.err;
@@ -953,8 +1029,8 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
             MODAL_TRY(oz_gemm_ex(ctx, rest, rest, LDP, -1.0, p.P + (size_t)s * LDP, LDP, false, p.Psw + (size_t)s * LDP,
                                  LDP, true, 1.0, A22, n, oz));
             const int nt = ceil_div(rest, 32);
-            k_mirror_lower<<<dim3(nt, nt), 256, 0, ctx->stream>>>(A, n, s);
-            MODAL_TRY(launched(ctx, "mirror_lower"));
+            k_trail_hilo<<<dim3(nt, nt), 256, 0, ctx->stream>>>(A, n, s, p.Ahl);
+            MODAL_TRY(launched(ctx, "trail_hilo"));
         }
     }
     k_copy_last_diag<<<1, 32, 0, ctx->stream>>>(A, n, p.d);

@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--config", default="cfg2")
     ap.add_argument("--prec", choices=["auto", "fp64", "split"], default="auto")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # only the warm-up and timed steps, one short line (for profiler launch lists)
+    ap.add_argument("--step-only", action="store_true")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     return a
@@ -217,6 +219,12 @@ def run_ours(a, ws, rank, local):
     proj_ms = float(np.median(times[:, 1]))
     step_ms = float(np.median(times.sum(axis=1)))
     go_ms, proj_ms, step_ms = max_over_ranks([go_ms, proj_ms, step_ms], ws, f"cuda:{local}")
+    stages = {k: {"ms": v[0] / a.steps, "launches": v[1] / a.steps} for k, v in tm.items()}
+    if a.step_only:
+        ctx.close()
+        return {"metric": METRIC, "value": go_ms * 1e-3, "unit": "s", "mode": "step-only", "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": step_ms, "config": {"workload": a.config},
+                "gpu_launches": int(launches), "stage_ms_per_step": stages}
 
     # the other precision, for the split-vs-FP64 ratio and the error against FP64
     extra = {}
@@ -377,7 +385,7 @@ def run_ours(a, ws, rank, local):
         "tuning": tuning,
         "extras": extras,
         "next_rows": next_rows,
-        "stage_ms_per_step": {k: v[0] / max(1, v[1]) for k, v in tm.items()},
+        "stage_ms_per_step": stages,
         "roofline": roof,
         "mu_contraction": mu_contraction,
         "cpu_baseline": cpu,

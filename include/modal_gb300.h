@@ -250,6 +250,17 @@ modal_status modal_set_ortho(modal_ctx *ctx, const double *orthol, const double 
  * reproducible.  Takes effect at the next modal_orthogonalise. */
 modal_status modal_set_pca_floor(modal_ctx *ctx, double floor);
 
+/* Kernel of the FP32 (MODAL_PREC_SPLIT) projection: 1 runs the point-by-basis
+ * contraction of each slab on the tcgen05 tensor cores (three exact BF16
+ * pieces per operand, six products, FP32 tensor-memory sums per 32-point
+ * chunk, Kahan across chunks) where P <= 32; 0 (default), or P > 32, runs the
+ * CUDA-core FP32 slab kernel.  Both evaluate every shape at every point on the
+ * CUDA cores, which is most of the work, so the tensor-core form is not the
+ * faster one on GB300; modal_autotune times both.  modal_get_proj_kernel
+ * reports which one the current basis uses.  No reference counterpart. */
+modal_status modal_set_proj_kernel(modal_ctx *ctx, int tensor_cores);
+modal_status modal_get_proj_kernel(const modal_ctx *ctx, int *tensor_cores);
+
 /* Eigen-decomposition of the symmetric n x n matrix a (host, row-major; only
  * read): every eigenvalue in ascending order in w[n], and, when v is not NULL,
  * the eigenvectors as rows of v[n][n] (row j belongs to w[j]).  FP64 on the
@@ -286,8 +297,9 @@ modal_status modal_project_batch(modal_ctx *ctx, int S, const modal_shape *shape
 long modal_ctx_captures(const modal_ctx *ctx);
 
 /* Launch-configuration tuner.  Times the candidate configurations of the
- * FP32 projection kernel (shapes per CTA; grid or persistent 1-2 CTAs per SM)
- * and of the FP64 Gamma kernel (mu steps per shared-memory stage) on this
+ * FP32 projection (the tensor-core kernel where P <= 32; the CUDA-core kernel
+ * with shapes per CTA and grid or persistent 1-2 CTAs per SM) and of the FP64
+ * Gamma kernel (mu steps per shared-memory stage) on this
  * context's problem, keeps the fastest, and appends them to the text file
  * cache_path (NULL: no file) keyed by GPU architecture and problem size; a
  * later call that finds its keys there applies them without timing.  Needs

@@ -530,6 +530,23 @@ modal_status modal_set_pca_floor(modal_ctx *c, double floor)
     return MODAL_OK;
 }
 
+modal_status modal_set_proj_kernel(modal_ctx *c, int tensor_cores)
+{
+    if (!c || (tensor_cores != 0 && tensor_cores != 1)) {
+        set_error("modal_set_proj_kernel: 0 (CUDA cores) or 1 (tensor cores)");
+        return MODAL_ERR_ARG;
+    }
+    c->proj_tc = tensor_cores;
+    return MODAL_OK;
+}
+
+modal_status modal_get_proj_kernel(const modal_ctx *c, int *tensor_cores)
+{
+    if (!c || !tensor_cores) { set_error("modal_get_proj_kernel: NULL argument"); return MODAL_ERR_ARG; }
+    *tensor_cores = (c->proj_tc != 0 && c->P <= 32) ? 1 : 0;
+    return MODAL_OK;
+}
+
 modal_status modal_set_spectrum(modal_ctx *c, const double *cl)
 {
     MODAL_TRY(need(c, c && c->have_basis, "modal_set_spectrum: set the basis first"));
@@ -556,7 +573,8 @@ modal_status modal_project(modal_ctx *c, int S, const modal_shape *shapes, modal
     c->have_beta = true;
     c->beta_S = S;
     if (beta) MODAL_TRY(d2h(c, beta, c->beta.ptr, sizeof(double) * (size_t)S * c->N));
-    return sync(c);
+    MODAL_TRY(sync(c));
+    return oz_check(c);  // a bounded wait of the tensor-core slab kernel that expired
 }
 
 modal_status modal_alpha(modal_ctx *c, int S, const double *beta, double *alpha, double *modesR)

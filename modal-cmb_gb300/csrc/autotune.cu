@@ -147,32 +147,40 @@ modal_status modal_autotune(modal_ctx *c, const char *cache_path)
     const std::string arch = arch_tag(c->device);
     const int P = c->P;
 
-    // ---- projection slab kernel: (shapes per CTA, persistent CTAs per SM)
-    const std::string kp = "proj " + arch + " lmax=" + std::to_string(c->lmax) + " P=" + std::to_string(P);
-    int pv[2] = {0, 0};
-    if (cache_lookup(cache_path, kp, pv, 2)) {
+    // ---- projection slab kernel: tensor-core kernel (P <= 32), or the CUDA-core
+    // kernel with (shapes per CTA, persistent CTAs per SM)
+    const std::string kp = "proj2 " + arch + " lmax=" + std::to_string(c->lmax) + " P=" + std::to_string(P);
+    int pv[3] = {0, 0, 0};
+    if (cache_lookup(cache_path, kp, pv, 3)) {
         c->proj_sg = pv[0];
         c->proj_cpb = pv[1];
+        c->proj_tc = pv[2];
     } else {
         std::vector<double> tab;
         std::vector<modal_shape> sh;
         tune_shapes(c->lmax, tab, sh);
-        std::vector<int> sgs = (P <= 32) ? std::vector<int>{8, 4} : std::vector<int>{4};
+        struct Cand { int sg, cpb, tc; };
+        std::vector<Cand> cands;
+        if (P <= 32) cands.push_back({0, 0, 1});
+        for (int sg : (P <= 32) ? std::vector<int>{8, 4} : std::vector<int>{4})
+            for (int cpb : {0, 1, 2}) cands.push_back({sg, cpb, 0});
         float best = 1e30f;
-        int bsg = sgs[0], bcpb = 0;
-        for (int sg : sgs)
-            for (int cpb : {0, 1, 2}) {
-                c->proj_sg = sg;
-                c->proj_cpb = cpb;
-                float ms = 0.f;
-                MODAL_TRY(time_projection(c, sh, &ms));
-                if (ms < best) { best = ms; bsg = sg; bcpb = cpb; }
-            }
-        c->proj_sg = bsg;
-        c->proj_cpb = bcpb;
-        pv[0] = bsg;
-        pv[1] = bcpb;
-        cache_append(cache_path, kp, pv, 2, best);
+        Cand b = cands[0];
+        for (const Cand &cd : cands) {
+            c->proj_sg = cd.sg;
+            c->proj_cpb = cd.cpb;
+            c->proj_tc = cd.tc;
+            float ms = 0.f;
+            MODAL_TRY(time_projection(c, sh, &ms));
+            if (ms < best) { best = ms; b = cd; }
+        }
+        c->proj_sg = b.sg;
+        c->proj_cpb = b.cpb;
+        c->proj_tc = b.tc;
+        pv[0] = b.sg;
+        pv[1] = b.cpb;
+        pv[2] = b.tc;
+        cache_append(cache_path, kp, pv, 3, best);
     }
 
     // ---- FP64 Gamma kernel: mu steps per shared-memory stage

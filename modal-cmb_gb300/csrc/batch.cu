@@ -21,7 +21,7 @@ namespace modal {
 
 struct BatchGraph {
     // layout key
-    int S = 0, prec = -1, lmin = -1, lmax = -1, P = -1, N = -1, sg = -1, cpb = -1;
+    int S = 0, prec = -1, lmin = -1, lmax = -1, P = -1, N = -1, sg = -1, cpb = -1, tc = -1;
     std::vector<int> kinds, nterms;
     std::vector<const void *> ptrs;
     // graph and pinned staging
@@ -61,7 +61,7 @@ static std::vector<const void *> batch_ptrs(const modal_ctx *c)
 static bool batch_matches(const BatchGraph &g, const modal_ctx *c, int S, const modal_shape *shapes, modal_prec prec)
 {
     if (!g.exec || g.S != S || g.prec != (int)prec || g.lmin != c->lmin || g.lmax != c->lmax || g.P != c->P ||
-        g.N != c->N || g.sg != c->proj_sg || g.cpb != c->proj_cpb)
+        g.N != c->N || g.sg != c->proj_sg || g.cpb != c->proj_cpb || g.tc != c->proj_tc)
         return false;
     for (int s = 0; s < S; s++)
         if (g.kinds[s] != shapes[s].kind || (shapes[s].kind == MODAL_SHAPE_SEPARABLE && g.nterms[s] != shapes[s].nterms))
@@ -129,6 +129,7 @@ static modal_status batch_capture(modal_ctx *c, int S, const modal_shape *shapes
     g.N = c->N;
     g.sg = c->proj_sg;
     g.cpb = c->proj_cpb;
+    g.tc = c->proj_tc;
     g.kinds.resize(S);
     g.nterms.resize(S);
     for (int s = 0; s < S; s++) {
@@ -182,6 +183,7 @@ modal_status modal_project_batch(modal_ctx *c, int S, const modal_shape *shapes,
     }
     c->launches += g.kernels;
     MODAL_CUDA(cudaStreamSynchronize(c->stream));
+    MODAL_TRY(oz_check(c));  // a bounded wait of the tensor-core slab kernel that expired
     std::memcpy(beta, g.h_beta, sizeof(double) * (size_t)S * c->N);
     c->have_beta = true;  // beta also stays on the device for modal_alpha
     c->beta_S = S;

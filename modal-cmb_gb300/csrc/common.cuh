@@ -42,6 +42,7 @@ struct modal_ctx {
     long captures = 0;                   // graphs captured so far
     // tuned launch configurations (0: built-in defaults; set by modal_autotune)
     int proj_sg = 0, proj_cpb = 0, gamma_kc = 0;
+    int proj_tc = 0;  // 1: FP32 projection on the tensor cores where P <= 32 (0: CUDA-core kernel)
     int beta_S = 0;
 
     // device state
@@ -220,6 +221,10 @@ struct ProjPlan {
     long tabf_total = 0;  // floats of the FP32 separable tables
     RadialArgs ra;        // radial shapes (3D transfer Gamma only)
     int max_nterms = 0;
+    bool tc = false;        // tensor-core slab kernel (FP32 form, P <= 32)
+    int Mpad = 0;           // compact k entries per row of its BF16 q pieces
+    size_t o_bq = 0, o_perm = 0;
+    std::vector<int> perm;  // shape order of its work items (by kind and term count)
 };
 // plan: validate, size every buffer, upload the slab schedule (may allocate);
 // stage: copy shape tables/descriptors to the device; record: enqueue the

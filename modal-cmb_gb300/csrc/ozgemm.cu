@@ -559,7 +559,7 @@ modal_status oz_check(modal_ctx *ctx)
     int herr = 0;
     MODAL_CUDA(cudaMemcpyAsync(&herr, ctx->ozerr.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     MODAL_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (herr) { set_error("oz_gemm: a bounded wait in the tensor-core kernel expired (role %d)", herr); return MODAL_ERR_TIMEOUT; }
+    if (herr) { set_error("a bounded wait in a tensor-core kernel expired (role %d: 1-4 Ozaki GEMM, 21-22 slab projection)", herr); return MODAL_ERR_TIMEOUT; }
     return MODAL_OK;
 }
 

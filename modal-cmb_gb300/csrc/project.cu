@@ -18,7 +18,9 @@
 // F_i goes to a [S][L][P*P] buffer; a second pass forms B and beta.
 #include <algorithm>
 #include <vector>
+#include <cuda_bf16.h>
 #include "common.cuh"
+#include "tc_ptx.cuh"
 
 namespace modal {
 
@@ -714,6 +716,389 @@ __global__ void __launch_bounds__(256, 2) k_project_slab_f32(int lmin, int lmax,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core form of the FP32 slab projection (P <= 32).
+//
+// The two contractions of slab i,
+//   H_s[j][c] = sum_k f_s(i,j,k) q_c(k)        over the points of row j,
+//   F_s[b][c] += sum_j q_b(j) H_s[j][c]        over the rows,
+// are split between the tensor cores and the CUDA cores.  The first (about 85%
+// of the arithmetic) runs as tcgen05 MMAs with M = 128 rows (4 shapes x 32
+// rows of one parity), N = 32 basis columns and K = 16 per step; the second
+// stays on CUDA cores, once per block of 32 rows, as in k_project_slab_f32.
+//
+// Operands.  Row j of slab i holds k = j + (i & 1) + 2m, so every k of a row
+// has the parity of i + j; a block of 32 rows j = jb, jb + 2, ... shares it.
+// In compact coordinates m = k >> 1 row j starts one step after row j - 2: the
+// block is a band, walked in chunks of 32 m (64 bytes of BF16 per row), with
+// zeros outside each row's band.  Each value f = W(i,j,k) S_s(i,j,k) (FP32,
+// evaluated by the thread that owns the row) is split exactly into three BF16
+// pieces f1 + f2 + f3 (8 significant bits each; BF16 keeps the FP32 exponent
+// range, so nothing is scaled), and q_c(k) likewise from FP64.  The six
+// products fa qb with a + b <= 4 (pieces numbered from 1) carry each product to
+// about 2^-24 relative, the precision of the FP32 product of the CUDA-core
+// kernel; products of BF16 pieces are exact in FP32.
+//
+// Accumulation.  Each chunk's 12 MMAs (2 K-steps x 6 products) write a fresh
+// FP32 accumulator in tensor memory (two, alternating), which the row's thread
+// reads back (tcgen05.ld) and adds into its H row as a Kahan pair, as the
+// CUDA-core kernel does per 32-point block.
+//
+// Roles: warps 0-3 own tensor-memory lanes 0-127 (thread = lane = A row): they
+// evaluate the A rows, stage the B tile, drain the accumulator and run the
+// fold.  Warp 4 allocates tensor memory and one of its threads issues the MMAs.
+// Hand-off per buffer: `ready` (128 arrivals) and `done` (tcgen05.commit).
+// Every wait is bounded; a timeout sets *err and ends the kernel.
+// ---------------------------------------------------------------------------
+constexpr int PT_SG = 4, PT_JR = 32;
+constexpr int PT_A_PIECE = 128 * 64, PT_B_PIECE = 32 * 64;
+constexpr int PT_BUF = 3 * PT_A_PIECE + 3 * PT_B_PIECE;  // 30 KB per buffer
+constexpr int PT_HS_LD = 36;                             // floats per staged H row (16-byte aligned, conflict-free)
+constexpr int PT_OFF_QS = 2 * PT_BUF;                    // q_b(j) of the block's rows, [32][32] floats
+constexpr int PT_OFF_F = PT_OFF_QS + 32 * 32 * 4;        // F Kahan pairs, [hi|lo][32][128] floats
+constexpr int PT_OFF_BAR = PT_OFF_F + 2 * 32 * 128 * 4;
+constexpr int PT_SMEM = PT_OFF_BAR + 128 + 1024;         // barriers and flags, 1 KB alignment slack
+constexpr uint32_t PT_TMEM_COLS = 64;
+constexpr long long PT_WAIT = 2000000000LL;              // clock64 cycles, about 1 s
+// kind::f16 instruction descriptor with A = B = BF16, D = F32, both K-major
+constexpr uint32_t PT_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(32 >> 3) << 17) |
+                              ((uint32_t)(128 >> 4) << 24);
+static_assert(PT_BUF % 1024 == 0 && PT_OFF_QS % 1024 == 0, "swizzled tiles need 1 KB alignment");
+static_assert(128 * PT_HS_LD * 4 <= 2 * PT_BUF, "H staging aliases the operand buffers");
+
+// v0 -> low half, v1 -> high half: v = w1 + w2 + w3 exactly (three BF16 pieces).
+__device__ __forceinline__ void bf16_split3(float v0, float v1, uint32_t &w1, uint32_t &w2, uint32_t &w3)
+{
+    const __nv_bfloat162 p1 = __floats2bfloat162_rn(v0, v1);
+    const float r0 = v0 - __low2float(p1), r1 = v1 - __high2float(p1);
+    const __nv_bfloat162 p2 = __floats2bfloat162_rn(r0, r1);
+    const __nv_bfloat162 p3 = __floats2bfloat162_rn(r0 - __low2float(p2), r1 - __high2float(p2));
+    w1 = *reinterpret_cast<const uint32_t *>(&p1);
+    w2 = *reinterpret_cast<const uint32_t *>(&p2);
+    w3 = *reinterpret_cast<const uint32_t *>(&p3);
+}
+
+// Barrier 1 over the 128 threads of warps 0-3; returns the OR of `v` over them.
+__device__ __forceinline__ bool pt_bar_or(bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
+
+// q_c(k) as three BF16 pieces, K-major per (k parity, piece):
+// Bq[((par * 3 + piece) * 32 + c) * Mpad + m] = piece of q_c(2m + par), zero for
+// k outside [lmin, lmax] and for c >= P.  The pieces are taken from FP64.
+__global__ void k_bq_pieces(int lmin, int lmax, int P, int Mpad, const double *__restrict__ q,
+                            __nv_bfloat16 *__restrict__ Bq)
+{
+    const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= 64L * Mpad) return;
+    const int m = (int)(e % Mpad), c = (int)((e / Mpad) % 32), par = (int)(e / (32L * Mpad));
+    const int k = 2 * m + par;
+    double v = (k >= lmin && k <= lmax && c < P) ? q[(size_t)(k - lmin) * P + c] : 0.0;
+    const size_t plane = (size_t)32 * Mpad, at = (size_t)c * Mpad + m;
+    for (int pc = 0; pc < 3; pc++) {
+        const __nv_bfloat16 h = __double2bfloat16(v);
+        Bq[((size_t)par * 3 + pc) * plane + at] = h;
+        v -= (double)__bfloat162float(h);
+    }
+}
+
+// Work item w = (slab rank w / G, group of 4 shapes w % G) from *counter; the
+// shapes of group g are shapes[perm[4g .. 4g+3]] (sorted by kind and term count
+// so a warp's four shapes take the same path).  Fbuf as k_project_slab_f32.
+__global__ void __maxnreg__(200) k_project_slab_tc(int lmin, int lmax, int P, int S, int G, int nitems,
+                                                            int *__restrict__ counter,
+                                                            const int *__restrict__ slab_order,
+                                                            const int *__restrict__ perm,
+                                                            const float *__restrict__ qf,
+                                                            const __nv_bfloat16 *__restrict__ Bq, int Mpad,
+                                                            const FShape *__restrict__ shapes,
+                                                            const float *__restrict__ tabf,
+                                                            const float *__restrict__ Wt,
+                                                            const long long *__restrict__ sbase,
+                                                            float *__restrict__ Fbuf, int *__restrict__ err)
+{
+    using namespace tc;
+    extern __shared__ uint8_t pt_raw[];
+    uint8_t *sm = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(pt_raw) + 1023) & ~(uintptr_t)1023);
+    float *Qs = reinterpret_cast<float *>(sm + PT_OFF_QS);
+    float *Fs = reinterpret_cast<float *>(sm + PT_OFF_F);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sm + PT_OFF_BAR);
+    uint64_t *ready = bars, *done = bars + 2;
+    volatile int *cmd = reinterpret_cast<volatile int *>(bars + 4);  // per buffer: 1 = chunk, 0 = exit
+    volatile int *abort_flag = cmd + 2;
+    volatile int *item_slot = cmd + 3;
+    volatile uint32_t *tmem_slot = reinterpret_cast<volatile uint32_t *>(cmd + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < 2; b++) {
+            mbar_init(smem_u32(&ready[b]), 128);
+            mbar_init(smem_u32(&done[b]), 1);
+        }
+        cmd[0] = cmd[1] = 0;
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 4) {
+        tmem_alloc(smem_u32((const void *)tmem_slot), PT_TMEM_COLS);
+        tc_fence_before();
+    }
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 4) {
+        if (lane == 0) {
+            long u = 0;
+            for (;; u++) {
+                const int b = (int)(u & 1);
+                if (!mbar_wait(smem_u32(&ready[b]), (uint32_t)((u >> 1) & 1), abort_flag, PT_WAIT)) {
+                    if (!*abort_flag) { *abort_flag = 1; atomicCAS(err, 0, 21); }
+                    break;
+                }
+                tc_fence_after();
+                if (cmd[b] == 0) break;
+                const uint32_t a0 = smem_u32(sm + b * PT_BUF), b0 = a0 + 3 * PT_A_PIECE;
+                const uint32_t d = tmem + (uint32_t)(32 * b);
+                // A piece a with B piece b, a + b <= 2 (from 0), smallest products first
+                const int pa[6] = {2, 1, 0, 1, 0, 0}, pb[6] = {0, 1, 2, 0, 1, 0};
+#pragma unroll
+                for (int ks = 0; ks < 2; ks++)
+#pragma unroll
+                    for (int p = 0; p < 6; p++)
+                        umma_f16(d, desc_sw64(a0 + pa[p] * PT_A_PIECE + ks * 32),
+                                 desc_sw64(b0 + pb[p] * PT_B_PIECE + ks * 32), PT_IDESC, (ks | p) ? 1u : 0u);
+                umma_commit(smem_u32(&done[b]));
+            }
+            // after an abort, let the last issued chunk finish before tensor memory is freed
+            if (u > 0) {
+                const long l = u - 1;
+                const long long t0 = clock64();
+                while (!mbar_try(smem_u32(&done[l & 1]), (uint32_t)((l >> 1) & 1)) && clock64() - t0 < PT_WAIT) {
+                }
+            }
+        }
+    } else {
+        const int gt = threadIdx.x;  // A row = tensor-memory lane
+        const uint32_t tl = (uint32_t)(32 * warp) << 16;
+        const int sl = lane & 3, jr = 8 * warp + (lane >> 2);  // row gt = (shape sl, block row jr)
+        const int PP = P * P, L = lmax - lmin + 1, H = (lmax + 2) / 2, swz = (gt >> 1) & 3;
+        float *Fhi = Fs, *Flo = Fs + 32 * 128;
+        float *Hs = reinterpret_cast<float *>(sm);  // aliases the operand buffers between blocks
+        long u = 0;
+        bool stop = false;
+        for (;;) {
+            stop = pt_bar_or(stop);
+            if (stop) break;
+            if (gt == 0) *item_slot = atomicAdd(counter, 1);
+            pt_bar_or(false);
+            const int w = *item_slot;
+            if (w >= nitems) break;
+            const int slab = slab_order[w / G], g = w % G, i = lmin + slab;
+            const int ps = g * PT_SG + sl;
+            const bool sv = ps < S;
+            FShape sh = {1, 0, 0, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, 0.f};
+            if (sv) sh = shapes[perm[ps]];
+            for (int e = 0; e < 32; e++) Fhi[e * 128 + gt] = Flo[e * 128 + gt] = 0.f;
+            for (int par = 0; par < 2 && !stop; par++) {
+                const int kp = (i + par) & 1;
+                for (int jb = i + ((par - i) & 1); jb <= lmax && !stop; jb += 2 * PT_JR) {
+                    // the block's band in compact k: first row's start to last row's end
+                    const int mlo = (jb + (i & 1) - kp) >> 1;
+                    int jl = min(jb + 2 * (PT_JR - 1), lmax);
+                    if ((jl - jb) & 1) jl--;
+                    int kle = min(i + jl, lmax);
+                    if ((kle - kp) & 1) kle--;
+                    const int mhi = (kle - kp) >> 1;
+                    if (mhi < mlo) continue;
+                    // this thread's row
+                    const int j = jb + 2 * jr;
+                    int mf = 1, ml = 0;
+                    long long wb = 0;
+                    if (sv && j <= lmax) {
+                        const int kf = j + (i & 1);
+                        int kl = min(i + j, lmax);
+                        if ((kl - kp) & 1) kl--;
+                        if (kl >= kf) {
+                            mf = (kf - kp) >> 1;
+                            ml = (kl - kp) >> 1;
+                            wb = sbase[slab] + tet_row_offset(i, j, lmax) - mf;
+                        }
+                    }
+                    const bool fast = sh.kind == MODAL_SHAPE_SEPARABLE && sh.nterms <= PJ_TCOEF;
+                    float4 cf[PJ_TCOEF];
+#pragma unroll
+                    for (int t = 0; t < PJ_TCOEF; t++) {
+                        float3 c3 = make_float3(0.f, 0.f, 0.f);
+                        if (fast && ml >= mf && t < sh.nterms) c3 = sep_row_coef(sh, tabf, H, t, i, j);
+                        cf[t] = make_float4(c3.x * (1.f / 6.f), c3.y * (1.f / 6.f), c3.z * (1.f / 6.f), 0.f);
+                    }
+                    float Hh[32], Hl[32];
+#pragma unroll
+                    for (int c = 0; c < 32; c++) Hh[c] = Hl[c] = 0.f;
+                    const int q0 = mlo >> 5, q1 = mhi >> 5;
+                    for (int q = q0; q <= q1; q++, u++) {
+                        const int b = (int)(u & 1);
+                        uint8_t *buf = sm + b * PT_BUF;
+#pragma unroll 1
+                        for (int e8 = 0; e8 < 4; e8++) {
+                            const int m0 = 32 * q + 8 * e8;
+                            float v[8];
+#pragma unroll
+                            for (int x = 0; x < 8; x++) {
+                                const int m = m0 + x;
+                                float val = 0.f;
+                                if (m >= mf && m <= ml) {
+                                    const int k = 2 * m + kp;
+                                    float s;
+                                    if (fast) {
+                                        s = 0.f;
+#pragma unroll
+                                        for (int t = 0; t < PJ_TCOEF; t++) {
+                                            if (t < sh.nterms) {
+                                                const float4 T = tab4(sh, tabf, H, t, k);
+                                                s = fmaf(cf[t].x, T.z, fmaf(cf[t].y, T.y, fmaf(cf[t].z, T.x, s)));
+                                            }
+                                        }
+                                    } else {
+                                        s = shape_f(sh, tabf, H, i, j, k);
+                                    }
+                                    val = __ldg(Wt + wb + m) * s;
+                                }
+                                v[x] = val;
+                            }
+                            uint32_t w1[4], w2[4], w3[4];
+#pragma unroll
+                            for (int y = 0; y < 4; y++) bf16_split3(v[2 * y], v[2 * y + 1], w1[y], w2[y], w3[y]);
+                            const int off = gt * 64 + ((e8 ^ swz) << 4);
+                            *reinterpret_cast<uint4 *>(buf + off) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+                            *reinterpret_cast<uint4 *>(buf + PT_A_PIECE + off) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+                            *reinterpret_cast<uint4 *>(buf + 2 * PT_A_PIECE + off) = make_uint4(w3[0], w3[1], w3[2], w3[3]);
+                        }
+                        {   // B tile: piece r, row c = gt >> 2, 16-byte chunk e = gt & 3
+                            const int c = gt >> 2, e = gt & 3;
+#pragma unroll
+                            for (int r = 0; r < 3; r++) {
+                                const uint4 bv = __ldg(reinterpret_cast<const uint4 *>(
+                                    Bq + ((size_t)(kp * 3 + r) * 32 + c) * Mpad + 32 * q + 8 * e));
+                                *reinterpret_cast<uint4 *>(buf + 3 * PT_A_PIECE + r * PT_B_PIECE + c * 64 +
+                                                           ((e ^ ((c >> 1) & 3)) << 4)) = bv;
+                            }
+                        }
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        tc_fence_before();
+                        if (gt == 0) cmd[b] = 1;
+                        mbar_arrive(smem_u32(&ready[b]));
+                        // drain the chunk before this one (the last one after the loop)
+                        if (q > q0 || q == q1) {
+                            const long first = (q > q0) ? u - 1 : u, last = (q == q1) ? u : u - 1;
+                            for (long ud = first; ud <= last; ud++) {
+                                const int bd = (int)(ud & 1);
+                                bool ok = mbar_wait(smem_u32(&done[bd]), (uint32_t)((ud >> 1) & 1), abort_flag, PT_WAIT);
+                                ok = __all_sync(0xffffffffu, ok);
+                                if (!ok) {
+                                    if (!*abort_flag) { *abort_flag = 1; atomicCAS(err, 0, 22); }
+                                    stop = true;
+                                    break;
+                                }
+                                tc_fence_after();
+                                uint32_t r[32];
+                                tmem_ld32(tmem + tl + (uint32_t)(32 * bd), r);
+                                tmem_wait_ld();
+#pragma unroll
+                                for (int c = 0; c < 32; c++) kahan_add(Hh[c], Hl[c], __uint_as_float(r[c]));
+                            }
+                            tc_fence_before();
+                        }
+                        if (stop) break;
+                    }
+                    if (pt_bar_or(stop)) { stop = true; break; }
+                    // fold: F_s[b][c] += sum_jr q_b(jb + 2 jr) H[(s, jr)][c]; the operand
+                    // buffers are idle (every chunk of the block has been drained)
+#pragma unroll
+                    for (int c4 = 0; c4 < 8; c4++)
+                        *reinterpret_cast<float4 *>(Hs + gt * PT_HS_LD + 4 * c4) =
+                            make_float4(Hh[4 * c4] + Hl[4 * c4], Hh[4 * c4 + 1] + Hl[4 * c4 + 1],
+                                        Hh[4 * c4 + 2] + Hl[4 * c4 + 2], Hh[4 * c4 + 3] + Hl[4 * c4 + 3]);
+                    {
+                        const int jq = gt >> 2, b0 = 8 * (gt & 3), jj = jb + 2 * jq;
+#pragma unroll
+                        for (int x = 0; x < 8; x++) {
+                            const int bb = b0 + x;
+                            Qs[jq * 32 + bb] = (jj <= lmax && bb < P) ? qf[(size_t)(jj - lmin) * P + bb] : 0.f;
+                        }
+                    }
+                    pt_bar_or(false);
+#pragma unroll 1
+                    for (int r = 0; r < 2; r++) {
+                        const int tau = gt + 128 * r, s3 = tau >> 6, bt = (tau >> 3) & 7, ct = tau & 7;
+                        float acc[4][4];
+#pragma unroll
+                        for (int x = 0; x < 4; x++)
+#pragma unroll
+                            for (int y = 0; y < 4; y++) acc[x][y] = 0.f;
+#pragma unroll 8
+                        for (int q2 = 0; q2 < PT_JR; q2++) {
+                            const float4 qv = *reinterpret_cast<const float4 *>(Qs + q2 * 32 + 4 * bt);
+                            const int mrow = 32 * (q2 >> 3) + 4 * (q2 & 7) + s3;
+                            const float4 hv = *reinterpret_cast<const float4 *>(Hs + mrow * PT_HS_LD + 4 * ct);
+                            const float qa[4] = {qv.x, qv.y, qv.z, qv.w}, ha[4] = {hv.x, hv.y, hv.z, hv.w};
+#pragma unroll
+                            for (int x = 0; x < 4; x++)
+#pragma unroll
+                                for (int y = 0; y < 4; y++) acc[x][y] = fmaf(qa[x], ha[y], acc[x][y]);
+                        }
+#pragma unroll
+                        for (int x = 0; x < 4; x++)
+#pragma unroll
+                            for (int y = 0; y < 4; y++) {
+                                const int e = (r * 16 + 4 * x + y) * 128 + gt;
+                                kahan_add(Fhi[e], Flo[e], acc[x][y]);
+                            }
+                    }
+                    pt_bar_or(false);  // Hs and Qs are read before the next block writes the buffers
+                }
+            }
+            if (stop) continue;  // the loop head agrees on stopping
+#pragma unroll 1
+            for (int r = 0; r < 2; r++) {
+                const int tau = gt + 128 * r, s3 = tau >> 6, bt = (tau >> 3) & 7, ct = tau & 7;
+                const int p3 = g * PT_SG + s3;
+                if (p3 >= S) continue;
+                float *dst = Fbuf + ((size_t)perm[p3] * L + slab) * PP;
+#pragma unroll
+                for (int x = 0; x < 4; x++)
+#pragma unroll
+                    for (int y = 0; y < 4; y++) {
+                        const int bb = 4 * bt + x, c = 4 * ct + y;
+                        const int e = (r * 16 + 4 * x + y) * 128 + gt;
+                        if (bb < P && c < P) dst[bb * P + c] = Fhi[e] + Flo[e];
+                    }
+            }
+        }
+        // tell the MMA thread to stop (after every issued chunk has been drained)
+        if (!stop) {
+            const int b = (int)(u & 1);
+            if (gt == 0) cmd[b] = 0;
+            mbar_arrive(smem_u32(&ready[b]));
+        }
+    }
+    __syncthreads();
+    if (warp == 4) {
+        tc_fence_after();
+        tmem_dealloc(tmem, PT_TMEM_COLS);
+    }
+}
+
 // B[s][a][bc] = sum_slab q[slab][a] F[s][slab][bc], FP32 with Kahan compensation.
 __global__ void k_project_B_f32(int L, int P, int S, const float *__restrict__ qf, const float *__restrict__ Fbuf,
                                 double *__restrict__ B)
@@ -835,6 +1220,7 @@ modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_p
     MODAL_TRY(ensure(ctx->beta, sizeof(double) * (size_t)S * N));
     if (prec == MODAL_PREC_SPLIT) {
         proj_config(ctx, P, &pl.SG, &pl.CPL, &pl.cpb);
+        pl.tc = (P <= 32 && ctx->proj_tc != 0);
         auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
         size_t o = 0;
         pl.o_q = o; o += al(sizeof(float) * (size_t)L * P);
@@ -849,12 +1235,30 @@ modal_status proj_plan(modal_ctx *ctx, int S, const modal_shape *shapes, modal_p
         pl.npts = npts;
         pl.o_sb = o; o += al(sizeof(long long) * (size_t)(L + 1));
         pl.o_w = o; o += al(sizeof(float) * (size_t)npts);
+        if (pl.tc) {
+            pl.Mpad = (lmax / 2 + 1 + 31) / 32 * 32;
+            pl.o_bq = o; o += al(sizeof(__nv_bfloat16) * 2 * 3 * 32 * (size_t)pl.Mpad);
+            pl.o_perm = o; o += al(sizeof(int) * (size_t)S);
+        }
         MODAL_TRY(ensure(ctx->scratch, o));
         const size_t nb4 = (size_t)(P + 3) / 4;
         pl.smem = sizeof(float) * 32 * (size_t)pl.SG * nb4 * nb4;  // F Kahan pairs, element-major over 4 x 4 tiles
         int dev = ctx->device, nsm = 0;
         MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
         pl.nsm = nsm;
+        if (pl.tc) {
+            // work items of 4 shapes of one kind and term count where possible
+            pl.perm.resize(S);
+            for (int s = 0; s < S; s++) pl.perm[s] = s;
+            std::stable_sort(pl.perm.begin(), pl.perm.end(), [&](int a, int b) {
+                const DShape &x = pl.desc[a], &y = pl.desc[b];
+                return x.kind != y.kind ? x.kind < y.kind : x.nterms < y.nterms;
+            });
+            MODAL_CUDA(cudaMemcpyAsync(ctx->scratch.as<uint8_t>() + pl.o_perm, pl.perm.data(), sizeof(int) * S,
+                                       cudaMemcpyHostToDevice, ctx->stream));
+            MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, PT_SMEM));
+            MODAL_TRY(oz_reset(ctx));
+        }
         if (pl.SG == 8) MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_f32<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
         else if (pl.CPL == 1) MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_f32<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
         else MODAL_CUDA(cudaFuncSetAttribute(k_project_slab_f32<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
@@ -928,22 +1332,35 @@ modal_status proj_record(modal_ctx *ctx, const ProjPlan &pl)
         MODAL_TRY(launched(ctx, "slab_base"));
         k_weight_table<<<dim3(L, ceil_div(L, 8)), 256, 0, ctx->stream>>>(lmin, lmax, vlf, sbase, Wt);
         MODAL_TRY(launched(ctx, "weight_table"));
-        const int G = ceil_div(S, pl.SG), nitems = L * G;
-        dim3 grid(L, G);
-        int *cnt = nullptr;
-        if (pl.cpb > 0) {
+        if (pl.tc) {
+            __nv_bfloat16 *Bq = reinterpret_cast<__nv_bfloat16 *>(b + pl.o_bq);
+            k_bq_pieces<<<ceil_div(64L * pl.Mpad, 256), 256, 0, ctx->stream>>>(lmin, lmax, P, pl.Mpad, ctx->q.as<double>(), Bq);
+            MODAL_TRY(launched(ctx, "bq_pieces"));
+            const int Gt = ceil_div(S, PT_SG), nit = L * Gt;
             MODAL_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), ctx->stream));
-            grid = dim3(std::min(nitems, pl.nsm * pl.cpb), 1);
-            cnt = counter;
+            k_project_slab_tc<<<std::min(nit, 2 * pl.nsm), 160, PT_SMEM, ctx->stream>>>(
+                lmin, lmax, P, S, Gt, nit, counter, ctx->slab_order.as<int>(), reinterpret_cast<const int *>(b + pl.o_perm),
+                qf, Bq, pl.Mpad, fs, tabf, Wt, sbase, Fbuf, ctx->ozerr.as<int>());
+            MODAL_TRY(launched(ctx, "project_slab_tc"));
         }
-        auto run = [&](auto kern) -> modal_status {
-            kern<<<grid, 256, pl.smem, ctx->stream>>>(lmin, lmax, P, S, G, nitems, cnt, ctx->slab_order.as<int>(), qf,
-                                                     vlf, fs, tabf, Wt, sbase, Fbuf);
-            return launched(ctx, "project_slab_f32");
-        };
-        if (pl.SG == 8) MODAL_TRY(run(k_project_slab_f32<8, 1>));
-        else if (pl.CPL == 1) MODAL_TRY(run(k_project_slab_f32<4, 1>));
-        else MODAL_TRY(run(k_project_slab_f32<4, 2>));
+        if (!pl.tc) {
+            const int G = ceil_div(S, pl.SG), nitems = L * G;
+            dim3 grid(L, G);
+            int *cnt = nullptr;
+            if (pl.cpb > 0) {
+                MODAL_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), ctx->stream));
+                grid = dim3(std::min(nitems, pl.nsm * pl.cpb), 1);
+                cnt = counter;
+            }
+            auto run = [&](auto kern) -> modal_status {
+                kern<<<grid, 256, pl.smem, ctx->stream>>>(lmin, lmax, P, S, G, nitems, cnt, ctx->slab_order.as<int>(), qf,
+                                                         vlf, fs, tabf, Wt, sbase, Fbuf);
+                return launched(ctx, "project_slab_f32");
+            };
+            if (pl.SG == 8) MODAL_TRY(run(k_project_slab_f32<8, 1>));
+            else if (pl.CPL == 1) MODAL_TRY(run(k_project_slab_f32<4, 1>));
+            else MODAL_TRY(run(k_project_slab_f32<4, 2>));
+        }
         k_project_B_f32<<<ceil_div((long)S * P * PP, 256), 256, 0, ctx->stream>>>(L, P, S, qf, Fbuf, B);
         MODAL_TRY(launched(ctx, "project_B_f32"));
         k_project_beta<<<ceil_div((long)S * N, 256), 256, 0, ctx->stream>>>(N, P, S, ctx->triples.as<int>(), B,

@@ -294,6 +294,17 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 h = t;
             };
             int j = lane;
+            for (; j + 7 * 32 < npair; j += 8 * 32) {
+                float4 x[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) x[u] = A4[j + 32 * u];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int e = 2 * (j + 32 * u);
+                    acc(x[u].x, x[u].y, vbh[e], vbl[e], sh[2 * (u & 3)], sl[2 * (u & 3)]);
+                    acc(x[u].z, x[u].w, vbh[e + 1], vbl[e + 1], sh[2 * (u & 3) + 1], sl[2 * (u & 3) + 1]);
+                }
+            }
             for (; j + 3 * 32 < npair; j += 4 * 32) {
                 float4 x[4];
 #pragma unroll

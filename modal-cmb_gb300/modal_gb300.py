@@ -36,7 +36,7 @@ EXPORTS = [
     "modal_set_pca_floor", "modal_project_batch", "modal_ctx_captures", "modal_autotune", "modal_get_tuning",
     "modal_set_basis_e", "modal_set_modes_pol", "modal_gamma_pol", "modal_set_transfer_pol",
     "modal_gamma_transfer_pol", "modal_prim_points", "modal_prim_ortho", "modal_prim_eigen", "modal_set_ortho",
-    "modal_eigh", "modal_gemm_f64",
+    "modal_eigh", "modal_gemm_f64", "modal_set_proj_kernel", "modal_get_proj_kernel",
 ]
 
 TIMERS = {"gl": 0, "pl": 1, "mij": 2, "gamma": 3, "ortho": 4, "project": 5, "alpha": 6, "lift": 7, "adjoint": 8, "prune": 9,
@@ -115,6 +115,8 @@ def lib():
             "modal_basis_prune": (i, [vp, i, vp, i, vp, vp, vp]),
             "modal_lambda_min": (i, [vp, ctypes.POINTER(d), vp, vp]),
             "modal_set_pca_floor": (i, [vp, d]),
+            "modal_set_proj_kernel": (i, [vp, i]),
+            "modal_get_proj_kernel": (i, [vp, vp]),
             "modal_eigh": (i, [vp, i, vp, vp, vp]),
             "modal_gemm_f64": (i, [vp, i, i, i, d, vp, i, vp, i, d, vp, i]),
             "modal_project_batch": (i, [vp, i, vp, i, vp]),
@@ -350,6 +352,16 @@ class Context:
     def set_pca_floor(self, floor):
         _check(lib().modal_set_pca_floor(self.h, float(floor)))
 
+    def set_proj_kernel(self, tensor_cores):
+        """FP32 projection kernel: True = tcgen05 tensor cores (P <= 32), False = CUDA cores."""
+        _check(lib().modal_set_proj_kernel(self.h, 1 if tensor_cores else 0))
+
+    def proj_kernel(self):
+        """True when the FP32 projection of the current basis runs on the tensor cores."""
+        v = ctypes.c_int()
+        _check(lib().modal_get_proj_kernel(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
     def gemm_f64(self, A, B, transA=False, transB=False, alpha=1.0, beta=0.0, C=None, slices=8):
         """alpha op(A) op(B) + beta C in FP64 accuracy on the tensor cores
         (modal_gemm_f64: exact 7-bit integer slices of the operands)."""
@@ -405,7 +417,7 @@ class Context:
     def tuning(self):
         a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _check(lib().modal_get_tuning(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-        return {"proj_sg": a.value, "proj_cpb": b.value, "gamma_kc": c.value}
+        return {"proj_sg": a.value, "proj_cpb": b.value, "gamma_kc": c.value, "proj_tc": int(self.proj_kernel())}
 
     def set_transfer(self, xvec, qtilde, prim):
         xvec = _f64(xvec)

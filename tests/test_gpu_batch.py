@@ -2,6 +2,7 @@
 import os
 
 import numpy as np
+from conftest import rel_fro
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -74,31 +75,45 @@ def test_batch_recaptures_on_layout_or_buffer_change(mg):
 
 
 def test_autotune_applies_and_caches(mg, tmp_path):
+    """The tuner picks between the tensor-core kernel and the CUDA-core FP32
+    kernel's launch configurations, caches its choice and reads it back.  A
+    CUDA-core configuration changes the schedule, not the arithmetic (same bits
+    for every one); the two kernels agree within the FP32 tolerance."""
     lmax = 200
     path = os.fspath(tmp_path / "tune.txt")
     with _ctx(mg, lmax, 8) as c:
         shapes = _mixed(mg, lmax, 7, 12)
-        before = c.project(shapes, 1)
+        assert not c.proj_kernel()  # the CUDA-core kernel by default
+        before_cc = c.project(shapes, 1)
+        c.set_proj_kernel(True)
+        assert c.proj_kernel()
+        before_tc = c.project(shapes, 1)
+        c.set_proj_kernel(False)
+        b64 = c.project(shapes, 0)
+        for s in range(len(shapes)):
+            assert rel_fro(before_tc[s], b64[s]) <= 1e-6 and rel_fro(before_cc[s], b64[s]) <= 1e-6
         t = c.autotune(path)
-        assert t["proj_sg"] in (4, 8) and t["proj_cpb"] in (0, 1, 2) and t["gamma_kc"] in (4, 8, 16, 32)
-        # a configuration changes the schedule, not the arithmetic
-        assert np.array_equal(c.project(shapes, 1), before)
+        assert t["proj_tc"] in (0, 1) and t["gamma_kc"] in (4, 8, 16, 32)
+        if not t["proj_tc"]:
+            assert t["proj_sg"] in (4, 8) and t["proj_cpb"] in (0, 1, 2)
+        assert np.array_equal(c.project(shapes, 1), before_tc if t["proj_tc"] else before_cc)
         g1 = c.gamma(mg.PREC_FP64)
     lines = open(path).read().splitlines()
-    assert len(lines) == 2 and lines[0].startswith("proj sm_") and lines[1].startswith("gamma64 sm_")
+    assert len(lines) == 2 and lines[0].startswith("proj2 sm_") and lines[1].startswith("gamma64 sm_")
     with _ctx(mg, lmax, 8) as c2:
         assert c2.autotune(path) == t  # read back, not re-timed
         assert len(open(path).read().splitlines()) == 2
         c2.init_glint()
         assert np.array_equal(c2.gamma(mg.PREC_FP64), g1)
-    # every candidate, forced through the cache file, gives the same beta
-    key = lines[0].split("  #")[0].rsplit(" ", 2)[0]
-    for n, (sg, cpb) in enumerate([(4, 0), (8, 1), (4, 2), (8, 0)]):
+    # every candidate, forced through the cache file, gives its kernel's beta
+    key = lines[0].split("  #")[0].rsplit(" ", 3)[0]
+    for n, (sg, cpb, tcv) in enumerate([(4, 0, 0), (8, 1, 0), (4, 2, 0), (8, 0, 0), (0, 0, 1)]):
         p2 = os.fspath(tmp_path / f"t{n}.txt")
         with open(p2, "w") as f:
-            f.write(f"{key} {sg} {cpb}\n{lines[1]}\n")
+            f.write(f"{key} {sg} {cpb} {tcv}\n{lines[1]}\n")
         with _ctx(mg, lmax, 8) as c3:
             got = c3.autotune(p2)
-            assert (got["proj_sg"], got["proj_cpb"]) == (sg, cpb)
-            assert np.array_equal(c3.project(shapes, 1), before)
-            assert np.array_equal(c3.project_batch(shapes, 1), before)
+            assert (got["proj_sg"], got["proj_cpb"], got["proj_tc"]) == (sg, cpb, tcv)
+            ref = before_tc if tcv else before_cc
+            assert np.array_equal(c3.project(shapes, 1), ref)
+            assert np.array_equal(c3.project_batch(shapes, 1), ref)

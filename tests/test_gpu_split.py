@@ -203,3 +203,52 @@ def test_split_cfg5_largest_config(mg):
     assert np.array_equal(Gs, Gs.T) and np.array_equal(Gs, Gs2)
     for s in range(2):
         assert rel_fro(bs[s], b64[s]) <= 2e-6, (s, rel_fro(bs[s], b64[s]))
+
+
+@pytest.mark.parametrize("lmin,lmax,P,S", [(2, 40, 1, 1), (2, 61, 5, 7), (3, 257, 12, 9), (2, 600, 32, 6)])
+def test_split_projection_tensor_cores(mg, lmin, lmax, P, S):
+    """The tensor-core slab kernel (P <= 32, switched on) against FP64
+    (<= 1e-6 relative per shape) and against the CUDA-core FP32 kernel; groups
+    of four shapes that mix kinds and term counts (up to 12 terms, past the
+    4-term row-coefficient path), an S that is not a multiple of 4, odd and even
+    l_min, one-function bases; repeated calls and the captured batch give the
+    same bits."""
+    cl = mg.synthetic_cl(lmax)
+    q = mg.weighted_q(mg.legendre_q(lmin, lmax, P), cl, lmin)
+    shapes = (mg.separable_shapes(lmax, (S + 1) // 2, seed=41, tmin=1, tmax=12 if S > 5 else 3)
+              + mg.bump_shapes(S // 2, seed=42))
+    with mg.Context(0) as c:
+        c.set_basis(lmin, lmax, q)
+        c.set_modes(mg.mode_triples(P))
+        c.set_spectrum(cl)
+        assert not c.proj_kernel()  # the CUDA-core kernel by default
+        c.set_proj_kernel(True)
+        assert c.proj_kernel()
+        b64 = c.project(shapes, mg.PREC_FP64)
+        bt = c.project(shapes, mg.PREC_SPLIT)
+        bt2 = c.project(shapes, mg.PREC_SPLIT)
+        bb = c.project_batch(shapes, mg.PREC_SPLIT)
+        c.set_proj_kernel(False)
+        bc = c.project(shapes, mg.PREC_SPLIT)
+    assert np.array_equal(bt, bt2) and np.array_equal(bt, bb)
+    for s in range(S):
+        assert rel_fro(bt[s], b64[s]) <= 1e-6, (s, rel_fro(bt[s], b64[s]))
+        assert rel_fro(bt[s], bc[s]) <= 2e-6, (s, rel_fro(bt[s], bc[s]))
+
+
+def test_split_projection_kernel_choice(mg):
+    """The CUDA-core kernel by default; switched on, P <= 32 projects on the
+    tensor cores and P > 32 stays on the CUDA-core kernel."""
+    for P, want in ((32, True), (33, False)):
+        lmax = 120
+        q, tr, cl = mg.workload(lmax, P)
+        with mg.Context(0) as c:
+            c.set_basis(2, lmax, q)
+            c.set_modes(tr)
+            c.set_spectrum(cl)
+            assert not c.proj_kernel()
+            c.set_proj_kernel(True)
+            assert c.proj_kernel() == want
+            c.set_proj_kernel(False)
+            assert not c.proj_kernel()
+            assert mg.lib().modal_set_proj_kernel(c.h, 2) != 0  # only 0 or 1

@@ -36,9 +36,10 @@ METRIC = "Gamma+ortho s and shape projections/s, split-prec vs FP64, GB300, rel 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64 (nominal; no measured FP64 peak is available)
 # DRAM bytes (read + write) of the tridiagonalisation's panel kernels in one
-# eigen-decomposition at l <= 2000, P = 30 (N = 4960), from an ncu capture of
-# those kernels, not from this run (None until captured).
-NCU_PANEL_TRAFFIC_CFG2 = None
+# eigen-decomposition at l <= 2000, P = 30 (N = 4960): an ncu capture of the 155
+# panel launches of one eigen-decomposition (dram__bytes_read.sum 2.0724e11 +
+# dram__bytes_write.sum 5.70e8), not measured by this run.
+NCU_PANEL_TRAFFIC_CFG2 = 2.0724e11 + 5.70e8
 
 
 def parse():
@@ -311,13 +312,35 @@ def run_ours(a, ws, rank, local):
         torch.cuda.synchronize()
         fp64_256 = e0.elapsed_time(e1)
         beta256_err = float(np.max(np.linalg.norm(b256 - b256_64, axis=1) / np.linalg.norm(b256_64, axis=1)))
+        # the same batch with the slab contraction on the tensor cores (P <= 32)
+        tc256 = None
+        if P <= 32:
+            tuned_tc = ctx.proj_kernel()
+            ctx.set_proj_kernel(True)
+            btc = ctx.project_batch(sh256, mg.PREC_SPLIT)
+            t_tc = []
+            for _ in range(2):
+                flush.zero_()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                ctx.project_batch(sh256, mg.PREC_SPLIT)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                t_tc.append(e0.elapsed_time(e1))
+            ctx.set_proj_kernel(tuned_tc)
+            tc256 = {"ms": float(min(t_tc)), "beta_max_rel_err_vs_fp64": float(np.max(
+                np.linalg.norm(btc - b256_64, axis=1) / np.linalg.norm(b256_64, axis=1))),
+                     "kernel": "k_project_slab_tc (tcgen05, BF16 three-piece operands)"}
         go64 = extra.get("fp64_gamma_ortho_ms", go_ms)
         gos = extra.get("split_gamma_ortho_ms", go_ms)
         extra["projection_256_shapes"] = {
             "path": "modal_project_batch (captured CUDA graph, %d captures)" % ctx.captures,
             "split_ms": p256, "split_projections_per_s": 256.0 / (p256 * 1e-3),
             "fp64_ms": fp64_256, "split_beta_max_rel_err_vs_fp64": beta256_err,
-            "split_vs_fp64_gamma_ortho_plus_256_projections": (go64 + fp64_256) / (gos + p256)}
+            "split_vs_fp64_gamma_ortho_plus_256_projections": (go64 + fp64_256) / (gos + p256),
+            "kernel": "k_project_slab_tc" if ctx.proj_kernel() else "k_project_slab_f32 (CUDA cores)",
+            "tensor_core_form": tc256}
 
     # roofline of the dominant kernel of the timed step: the tridiagonalisation's
     # panel kernel (the FP64 matrix-vector product over the trailing matrix of
@@ -337,7 +360,7 @@ def run_ours(a, ws, rank, local):
         roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": NCU_PANEL_TRAFFIC_CFG2 if a.config == "cfg2" else None,
                 "traffic_source": "ncu capture of the panel kernels at this config, not this run",
-                "kernel": "k_trd_panel (155 launches per eigen-decomposition)", "kernel_ms": t_ms,
+                "kernel": "k_trd_panel (%d launches per eigen-decomposition)" % round(p_n / o_n), "kernel_ms": t_ms,
                 "peak_kind": pk_kind + " HBM copy bandwidth",
                 "algorithmic": "8 sum_{m<N} m^2 bytes per eigen-decomposition (trailing matrix read per column)",
                 "note": "the product also runs at the FP64 rate: 2 sum m^2 flop = %.1f TFLOP/s of the nominal %.2f"

@@ -61,34 +61,37 @@ constexpr long long OZ_WAIT = 1ll << 31;  // ~1 s of clock64 per wait
 constexpr uint32_t OZ_IDESC = idesc_f16(OZ_BM, OZ_BN);
 
 // ------------------------------------------------------------------ slicing
-// Slices of the rows of op(X), R x K: element (r, k) = trans ? X[k*ld + r] : X[r*ld + k].
-// out: [s][Rpad][Kpad] FP16 digits; ex[r]: the row's exponent.  Rows >= R and
-// columns >= K are zero.  One CTA (32 x 8 threads) per 32 rows.
-__global__ void __launch_bounds__(256) k_oz_slice(int R, int K, int Rpad, int Kpad, const double *__restrict__ X,
-                                                  long ld, int trans, int s, __half *__restrict__ out,
-                                                  int *__restrict__ ex)
+// Rows of op(X), R x K: element (r, k) = trans ? X[k*ld + r] : X[r*ld + k].
+// Tiles of 32 rows x 32 columns through shared memory (coalesced either way).
+__device__ __forceinline__ void oz_load_tile(double (*tile)[33], const double *__restrict__ X, long ld, int trans,
+                                             int R, int K, int r0, int k0)
+{
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    if (!trans) {
+        for (int rr = ty; rr < 32; rr += 8) {
+            const int r = r0 + rr, k = k0 + tx;
+            tile[rr][tx] = (r < R && k < K) ? X[(size_t)r * ld + k] : 0.0;
+        }
+    } else {
+        for (int kk = ty; kk < 32; kk += 8) {
+            const int r = r0 + tx, k = k0 + kk;
+            tile[tx][kk] = (r < R && k < K) ? X[(size_t)k * ld + r] : 0.0;
+        }
+    }
+}
+
+// Row exponents, over K chunks in parallel: ex[r] = max over the row of
+// ilogb(|x|) + 1 (atomicMax over the chunks; ex starts at a value below every
+// exponent, and an all-zero row keeps it).  grid (Rpad / 32, K chunks).
+__global__ void __launch_bounds__(256) k_oz_rowexp(int R, int K, int kchunk, const double *__restrict__ X, long ld,
+                                                   int trans, int *__restrict__ ex)
 {
     __shared__ double tile[32][33];
-    __shared__ double smx[8][32];
-    __shared__ int sexp[32];
-    const int r0 = blockIdx.x * 32;
+    const int r0 = blockIdx.x * 32, kb = blockIdx.y * kchunk, ke = min(K, kb + kchunk);
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    auto load = [&](int k0) {
-        if (!trans) {
-            for (int rr = ty; rr < 32; rr += 8) {
-                const int r = r0 + rr, k = k0 + tx;
-                tile[rr][tx] = (r < R && k < K) ? X[(size_t)r * ld + k] : 0.0;
-            }
-        } else {
-            for (int kk = ty; kk < 32; kk += 8) {
-                const int r = r0 + tx, k = k0 + kk;
-                tile[tx][kk] = (r < R && k < K) ? X[(size_t)k * ld + r] : 0.0;
-            }
-        }
-    };
     double mx[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int k0 = 0; k0 < K; k0 += 32) {
-        load(k0);
+    for (int k0 = kb; k0 < ke; k0 += 32) {
+        oz_load_tile(tile, X, ld, trans, R, ke, r0, k0);
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < 4; j++) mx[j] = fmax(mx[j], fabs(tile[ty + 8 * j][tx]));
@@ -99,23 +102,35 @@ __global__ void __launch_bounds__(256) k_oz_slice(int R, int K, int Rpad, int Kp
         double v = mx[j];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (tx == 0) smx[0][ty + 8 * j] = v;
+        const int r = r0 + ty + 8 * j;
+        if (tx == 0 && r < R && v > 0.0 && isfinite(v)) atomicMax(ex + r, ilogb(v) + 1);
     }
-    __syncthreads();
+}
+
+// Slices of the rows of op(X) from their exponents: out: [s][Rpad][Kpad] FP16
+// digits.  Rows >= R and columns >= K are zero; a row whose exponent is still
+// the starting value (all zero) gets exponent 0.  grid (Rpad / 32, K chunks).
+__global__ void __launch_bounds__(256) k_oz_slice(int R, int K, int Rpad, int Kpad, int kchunk,
+                                                  const double *__restrict__ X, long ld, int trans, int s,
+                                                  __half *__restrict__ out, int *__restrict__ ex)
+{
+    __shared__ double tile[32][33];
+    __shared__ int sexp[32];
+    const int r0 = blockIdx.x * 32, kb = blockIdx.y * kchunk, ke = min(Kpad, kb + kchunk);
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     if (threadIdx.x < 32) {
-        const double m = smx[0][threadIdx.x];
-        const int e = (m > 0.0 && isfinite(m)) ? ilogb(m) + 1 : 0;
-        sexp[threadIdx.x] = e;
-        if (r0 + (int)threadIdx.x < Rpad) ex[r0 + threadIdx.x] = e;
+        const int r = r0 + threadIdx.x;
+        const int e = ex[r];
+        sexp[threadIdx.x] = (e < -100000) ? 0 : e;
     }
     __syncthreads();
+    if (blockIdx.y == 0 && threadIdx.x < 32) ex[r0 + threadIdx.x] = sexp[threadIdx.x];
     const size_t plane = (size_t)Rpad * Kpad;
-    for (int k0 = 0; k0 < Kpad; k0 += 32) {
-        if (k0 < K) load(k0);
+    for (int k0 = kb; k0 < ke; k0 += 32) {
+        if (k0 < K) oz_load_tile(tile, X, ld, trans, R, K, r0, k0);
         __syncthreads();
         for (int rr = ty; rr < 32; rr += 8) {
             const int r = r0 + rr, k = k0 + tx;
-            if (r >= Rpad) continue;
             // F = x 2^{6 - e + 7(s-1)} rounded to an integer, |F| < 2^55; its balanced
             // base-128 digits, least significant first, are exact integer operations
             const double y = (k0 < K) ? ldexp(tile[rr][tx], 6 - sexp[rr] + 7 * (s - 1)) : 0.0;
@@ -441,7 +456,17 @@ modal_status oz_slice(modal_ctx *ctx, int R, int K, const double *X, long ld, bo
         set_error("oz_slice: bad layout (R=%d Rpad=%d K=%d Kpad=%d s=%d)", R, Rpad, K, Kpad, s);
         return MODAL_ERR_ARG;
     }
-    k_oz_slice<<<Rpad / 32, 256, 0, ctx->stream>>>(R, K, Rpad, Kpad, X, ld, trans ? 1 : 0, s, out, ex);
+    // K split into chunks (multiples of 32) so that the grid has about two CTAs per SM
+    int nsm = 0;
+    MODAL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int rb = Rpad / 32, want = std::max(1, ceil_div(2 * nsm, rb));
+    const int kchunk = std::max(32, ceil_div(ceil_div(Kpad, want), 32) * 32);
+    const int nkc = ceil_div(Kpad, kchunk);
+    MODAL_CUDA(cudaMemsetAsync(ex, 0x80, sizeof(int) * (size_t)Rpad, ctx->stream));  // below every exponent
+    k_oz_rowexp<<<dim3(rb, ceil_div(std::max(K, 1), kchunk)), 256, 0, ctx->stream>>>(R, K, kchunk, X, ld, trans ? 1 : 0,
+                                                                                     ex);
+    MODAL_TRY(launched(ctx, "oz_rowexp"));
+    k_oz_slice<<<dim3(rb, nkc), 256, 0, ctx->stream>>>(R, K, Rpad, Kpad, kchunk, X, ld, trans ? 1 : 0, s, out, ex);
     return launched(ctx, "oz_slice");
 }
 

@@ -39,6 +39,7 @@ namespace modal {
 namespace {
 
 constexpr int TRD_NB = 32;                 // panel width
+constexpr int DC_DEFL_SMEM = 216 * 1024;    // shared memory of the deflation's serial loop (bytes)
 constexpr int TRD_THREADS = 512;           // 16 warps per CTA
 constexpr int TRD_WARPS = TRD_THREADS / 32;
 constexpr int LDP = 2 * TRD_NB;            // panel row: V (TRD_NB columns) then W
@@ -73,23 +74,38 @@ __device__ __forceinline__ double warp_max(double v)
 // Grid barrier for a cooperative launch (all CTAs co-resident), one per phase:
 // bar[0] counts arrivals, bar[1] is the generation.  Measured faster here
 // than per-CTA flag words that every CTA polls (152 x 152 pollers on a few L2
-// lines).  Bounded: a wait that runs out of its clock64 budget sets *err, and
-// every CTA returns false once *err is set.
+// lines).  Memory ordering by release/acquire atomics at GPU scope instead of
+// full fences: each CTA's arrival is an acq_rel add (its writes, ordered before
+// it by __syncthreads, are released; the last arrival acquires every earlier
+// one), the last arrival releases the generation, the others acquire it.
+// Bounded: a wait that runs out of its clock64 budget sets *err, and every CTA
+// returns false once *err is set.
+__device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned *p, unsigned v)
+{
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ bool grid_barrier(unsigned *bar, int *err)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *gen = bar + 1;
-        const unsigned g = *gen;
-        __threadfence();
-        const unsigned arrived = atomicAdd(bar, 1u);
+        const unsigned g = ld_acquire_gpu(bar + 1);
+        const unsigned arrived = atom_add_acq_rel_gpu(bar, 1u);
         if (arrived == gridDim.x - 1) {
             atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
+            atom_add_acq_rel_gpu(bar + 1, 1u);
         } else {
             const long long t0 = clock64();
-            while (*gen == g) {
+            while (ld_acquire_gpu(bar + 1) == g) {
                 if (*(volatile int *)err) break;
                 if (clock64() - t0 > BAR_CYCLES) {
                     atomicExch(err, 1);
@@ -97,7 +113,6 @@ __device__ bool grid_barrier(unsigned *bar, int *err)
                 }
             }
         }
-        __threadfence();
     }
     __syncthreads();
     return *(volatile int *)err == 0;
@@ -156,6 +171,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
     for (int e = tid; e < 2 * R * TRD_NB; e += blockDim.x) Vs[e] = 0.0;
     __syncthreads();
 
+    double apre = 0.0;  // this thread's first row of the next column of A, loaded one phase early
     for (int c = 0; c <= g.nbp; c++) {
         const int i = g.j0 + c;  // column reduced now; head row of reflector c - 1
         const int x0 = max(rb0, i);
@@ -210,7 +226,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 Wr[cp] = wr;
                 g.W[(size_t)r * LDP + cp] = wr;
                 if (c < g.nbp) {
-                    double x = g.A[(size_t)r * n + i];
+                    double x = (r == x0 + tid) ? apre : g.A[(size_t)r * n + i];
                     for (int t = 0; t < c; t++) x -= Vr[t] * s_wi[t] + Wr[t] * s_vi[t];
                     as[lr] = x;
                     g.a[r] = x;
@@ -239,6 +255,10 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         if (!grid_barrier(g.bar, g.err)) return;
 
         // ---------------- phase Y: reflector of column i, y = A v on the trailing matrix
+        {   // the next column's A entries of this thread's row (A does not change during the panel)
+            const int rn = max(rb0, i + 1) + tid;
+            if (c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
+        }
         if (warp == 0) {
             const double sig = grid_total(g.part, 2 * TRD_NB + 1, lane);
             if (lane == 0) {
@@ -486,8 +506,63 @@ struct DcWork {
 };
 
 // Sort, deflate and compact one merge (one CTA per merge).
-__global__ void __launch_bounds__(256) k_dc_deflate(DcWork w)
+// The serial part of the deflation (Dongarra-Sorensen: small z components,
+// then Givens rotations of close pairs) on D, z and the support flags of one
+// merge, from shared memory when they fit (fl: FT = unsigned char) or global
+// memory (FT = int); the kept list is written to kl, its flags to kf.
+template <typename FT>
+__device__ void dc_deflate_serial(DcWork &w, MergeInfo &M, int a, int k, double rho, double zm, double tol, double *D,
+                                  double *z, FT *fl, FT *kf)
 {
+    int kk = 0, nd = 0, ng = 0, k1 = 0, k2 = 0;
+    if (rho * zm <= tol) {
+        for (int s = 0; s < k; s++) w.dl[a + nd++] = a + s;
+    } else {
+        int pj = -1;
+        for (int nj = 0; nj < k; nj++) {
+            if (rho * fabs(z[nj]) <= tol) { w.dl[a + nd++] = a + nj; continue; }
+            if (pj < 0) { pj = nj; continue; }
+            double s = z[pj], c = z[nj];
+            const double tau = hypot(c, s);
+            const double t = D[nj] - D[pj];
+            c /= tau;
+            s = -s / tau;
+            if (fabs(t * c * s) <= tol) {
+                fl[nj] |= fl[pj];  // the rotated vector has support on both halves
+                z[nj] = tau;
+                z[pj] = 0.0;
+                w.grot[a + ng] = make_int2(a + pj, a + nj);
+                w.gcs[a + ng] = make_double2(c, s);
+                ng++;
+                const double t2 = D[pj] * c * c + D[nj] * s * s;
+                D[nj] = D[pj] * s * s + D[nj] * c * c;
+                D[pj] = t2;
+                w.dl[a + nd++] = a + pj;
+                pj = nj;
+            } else {
+                // a kept entry's flag is final (later rotations only change the newer entry)
+                k1 += (fl[pj] == 1);
+                k2 += (fl[pj] == 3);
+                kf[kk] = fl[pj];
+                w.kl[a + kk++] = a + pj;
+                pj = nj;
+            }
+        }
+        if (pj >= 0) {
+            k1 += (fl[pj] == 1);
+            k2 += (fl[pj] == 3);
+            kf[kk] = fl[pj];
+            w.kl[a + kk++] = a + pj;
+        }
+    }
+    M.kk = kk; M.k1 = k1; M.k2 = k2; M.nd = nd; M.ng = ng; M.rho = rho;
+}
+
+// One CTA per merge.  Shared memory (when the merge fits, DC_DEFL_SMEM): D, z
+// [k] doubles, support flags and kept flags [k] bytes.
+__global__ void __launch_bounds__(256) k_dc_deflate(DcWork w, int use_smem)
+{
+    extern __shared__ double dsm[];
     MergeInfo &M = w.mi[blockIdx.x];
     const int a = M.a, m = M.m, b = M.b, k = b - a, n = w.n;
     const int tid = threadIdx.x;
@@ -495,6 +570,8 @@ __global__ void __launch_bounds__(256) k_dc_deflate(DcWork w)
     const double rho = 2.0 * fabs(em);
     const double sg = em >= 0.0 ? 1.0 : -1.0;
     const double rs = 0.70710678118654752440;
+    double *Dsh = dsm, *zsh = dsm + k;
+    unsigned char *fsh = reinterpret_cast<unsigned char *>(dsm + 2 * k), *kfsh = fsh + k;
     // merge the two ascending halves (stable: ties take the first half first)
     for (int t = tid; t < k; t += blockDim.x) {
         const int src = a + t;
@@ -509,73 +586,55 @@ __global__ void __launch_bounds__(256) k_dc_deflate(DcWork w)
             while (lo < hi) { const int md = (lo + hi) >> 1; if (w.lam[md] <= v) lo = md + 1; else hi = md; }
             rk = (src - m) + (lo - a);
         }
+        const double zv = (src < m ? w.Z[(size_t)src * n + (m - 1)] : sg * w.Z[(size_t)src * n + m]) * rs;
         w.srt[a + rk] = src;
-        w.flg[a + rk] = src < m ? 1 : 2;
-        w.Ds[a + rk] = v;
-        w.zs[a + rk] = (src < m ? w.Z[(size_t)src * n + (m - 1)] : sg * w.Z[(size_t)src * n + m]) * rs;
+        if (use_smem) {
+            Dsh[rk] = v;
+            zsh[rk] = zv;
+            fsh[rk] = src < m ? 1 : 2;
+        } else {
+            w.flg[a + rk] = src < m ? 1 : 2;
+            w.Ds[a + rk] = v;
+            w.zs[a + rk] = zv;
+        }
     }
     __syncthreads();
+    const double *Dr = use_smem ? Dsh : w.Ds + a, *zr = use_smem ? zsh : w.zs + a;
     __shared__ double s_mx[2][8];
     double dm = 0.0, zm = 0.0;
     for (int t = tid; t < k; t += blockDim.x) {
-        dm = fmax(dm, fabs(w.Ds[a + t]));
-        zm = fmax(zm, fabs(w.zs[a + t]));
+        dm = fmax(dm, fabs(Dr[t]));
+        zm = fmax(zm, fabs(zr[t]));
     }
     dm = warp_max(dm);
     zm = warp_max(zm);
     if ((tid & 31) == 0) { s_mx[0][tid >> 5] = dm; s_mx[1][tid >> 5] = zm; }
     __syncthreads();
-    if (tid != 0) return;
-    for (int t = 1; t < (int)(blockDim.x >> 5); t++) { dm = fmax(dm, s_mx[0][t]); zm = fmax(zm, s_mx[1][t]); }
-    const double tol = 8.0 * EPS * fmax(dm, zm);
-    int kk = 0, nd = 0, ng = 0;
-    double *D = w.Ds + a, *z = w.zs + a;
-    if (rho * zm <= tol) {
-        for (int s = 0; s < k; s++) w.dl[a + nd++] = a + s;
-    } else {
-        int pj = -1;
-        for (int nj = 0; nj < k; nj++) {
-            if (rho * fabs(z[nj]) <= tol) { w.dl[a + nd++] = a + nj; continue; }
-            if (pj < 0) { pj = nj; continue; }
-            double s = z[pj], c = z[nj];
-            const double tau = hypot(c, s);
-            const double t = D[nj] - D[pj];
-            c /= tau;
-            s = -s / tau;
-            if (fabs(t * c * s) <= tol) {
-                w.flg[a + nj] |= w.flg[a + pj];  // the rotated vector has support on both halves
-                z[nj] = tau;
-                z[pj] = 0.0;
-                w.grot[a + ng] = make_int2(a + pj, a + nj);
-                w.gcs[a + ng] = make_double2(c, s);
-                ng++;
-                const double t2 = D[pj] * c * c + D[nj] * s * s;
-                D[nj] = D[pj] * s * s + D[nj] * c * c;
-                D[pj] = t2;
-                w.dl[a + nd++] = a + pj;
-                pj = nj;
-            } else {
-                w.kl[a + kk++] = a + pj;
-                pj = nj;
-            }
+    if (tid == 0) {
+        for (int t = 1; t < (int)(blockDim.x >> 5); t++) { dm = fmax(dm, s_mx[0][t]); zm = fmax(zm, s_mx[1][t]); }
+        const double tol = 8.0 * EPS * fmax(dm, zm);
+        if (use_smem)
+            dc_deflate_serial<unsigned char>(w, M, a, k, rho, zm, tol, Dsh, zsh, fsh, kfsh);
+        else
+            dc_deflate_serial<int>(w, M, a, k, rho, zm, tol, w.Ds + a, w.zs + a, w.flg + a, w.kci + a);
+    }
+    __syncthreads();
+    const int kk = M.kk, k1 = M.k1, k2 = M.k2;
+    if (use_smem)  // the rotated D, z and flags back for the later kernels
+        for (int t = tid; t < k; t += blockDim.x) {
+            w.Ds[a + t] = Dsh[t];
+            w.zs[a + t] = zsh[t];
+            w.flg[a + t] = fsh[t];
         }
-        if (pj >= 0) w.kl[a + kk++] = a + pj;
-    }
+    if (tid != 0) return;
     // compact kept values; grouped columns: first-half support, both halves, second half
-    int k1 = 0, k2 = 0;
-    for (int j = 0; j < kk; j++) {
-        const int f = w.flg[w.kl[a + j]];
-        k1 += (f == 1);
-        k2 += (f == 3);
-    }
     int cg[4] = {0, 0, k1 + k2, k1};
     for (int j = 0; j < kk; j++) {
         const int sl = w.kl[a + j];
-        w.kd[a + j] = w.Ds[sl];
-        w.kw[a + j] = w.zs[sl];
-        w.kci[a + j] = cg[w.flg[sl]]++;
+        w.kd[a + j] = use_smem ? Dsh[sl - a] : w.Ds[sl];
+        w.kw[a + j] = use_smem ? zsh[sl - a] : w.zs[sl];
+        w.kci[a + j] = cg[use_smem ? kfsh[j] : w.kci[a + j]]++;
     }
-    M.kk = kk; M.k1 = k1; M.k2 = k2; M.nd = nd; M.ng = ng; M.rho = rho;
 }
 
 // Apply the deflation rotations of each merge to its eigenvector rows (one
@@ -1061,6 +1120,7 @@ static modal_status dc_run(modal_ctx *ctx, int n, SyevState &st, SyevPtrs &p)
     MODAL_TRY(launched(ctx, "dc_eye"));
     double *Z = p.Z, *Zn = p.Zn;
     const int nlev = (int)st.levels.size();
+    MODAL_CUDA(cudaFuncSetAttribute(k_dc_deflate, cudaFuncAttributeMaxDynamicSharedMemorySize, DC_DEFL_SMEM));
     for (int l = 0; l < nlev; l++) {
         const int nm = (int)st.levels[l].size();
         int kmax = 0, hmax = 0;
@@ -1072,7 +1132,10 @@ static modal_status dc_run(modal_ctx *ctx, int n, SyevState &st, SyevPtrs &p)
         w.mi = p.mi + st.level_off[l];
         w.pos2m = p.pos2m + (size_t)l * n;
         w.err = p.err;
-        k_dc_deflate<<<nm, 256, 0, ctx->stream>>>(w);
+        // D, z and flags of the level's largest merge in shared memory when they fit
+        const size_t dsmem = (size_t)kmax * (2 * sizeof(double) + 2);
+        const int use_smem = dsmem <= (size_t)DC_DEFL_SMEM;
+        k_dc_deflate<<<nm, 256, use_smem ? dsmem : 0, ctx->stream>>>(w, use_smem);
         MODAL_TRY(launched(ctx, "dc_deflate"));
         k_dc_rotate<<<dim3(ceil_div(kmax, 128), nm), 128, 0, ctx->stream>>>(w);
         MODAL_TRY(launched(ctx, "dc_rotate"));

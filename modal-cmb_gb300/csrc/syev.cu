@@ -42,6 +42,7 @@ constexpr int TRD_NB = 32;                 // panel width
 constexpr int DC_DEFL_SMEM = 216 * 1024;    // shared memory of the deflation's serial loop (bytes)
 constexpr int TRD_THREADS = 512;           // 16 warps per CTA
 constexpr int TRD_WARPS = TRD_THREADS / 32;
+constexpr int TRD_PRE = 4;                 // rows per warp whose next-column A entry is prefetched
 constexpr int LDP = 2 * TRD_NB;            // panel row: V (TRD_NB columns) then W
 constexpr int PCOMP = 2 * TRD_NB + 2;      // partial components: p[NB], q[NB], y.v, |x|^2
 constexpr int NBB = 256;                   // reflectors per block of the back-transformation
@@ -161,6 +162,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
     __shared__ double s_vi[TRD_NB], s_wi[TRD_NB];
     __shared__ double s_red[TRD_WARPS];
     __shared__ double s_scal[4];
+    __shared__ double s_pp[8][2 * TRD_NB + 1];  // partial dot products per row group
 
     const int n = g.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int G = gridDim.x, b = blockIdx.x;
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
     for (int e = tid; e < 2 * R * TRD_NB; e += blockDim.x) Vs[e] = 0.0;
     __syncthreads();
 
-    double apre = 0.0;  // this thread's first row of the next column of A, loaded one phase early
+    double apre = 0.0;  // lane k: the next column's A entry of the warp's k-th row (k < TRD_PRE)
     for (int c = 0; c <= g.nbp; c++) {
         const int i = g.j0 + c;  // column reduced now; head row of reflector c - 1
         const int x0 = max(rb0, i);
@@ -217,21 +219,34 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             }
             __syncthreads();
             const double yvc = s_scal[0], whead = s_scal[1];
-            for (int r = x0 + tid; r < rb1; r += blockDim.x) {
+            // warp per row: the row's w entry and its updated column entry, each a
+            // sum over the panel's c columns by the lanes
+            int kk = 0;
+            for (int r = x0 + warp; r < rb1; r += TRD_WARPS, kk++) {
                 const int lr = r - rb0;
                 double *Vr = Vs + (size_t)lr * TRD_NB, *Wr = Ws + (size_t)lr * TRD_NB;
-                double s = ys[lr];
-                for (int t = 0; t < cp; t++) s -= Vr[t] * q[t] + Wr[t] * p[t];
-                const double wr = (r == i) ? whead : taup * s - 0.5 * taup * taup * yvc * Vr[cp];
-                Wr[cp] = wr;
-                g.W[(size_t)r * LDP + cp] = wr;
+                double pa = 0.0;
+                if (lane < cp) pa = Vr[lane] * q[lane] + Wr[lane] * p[lane];
+                pa = warp_sum(pa);
+                const double wr = (r == i) ? whead : taup * (ys[lr] - pa) - 0.5 * taup * taup * yvc * Vr[cp];
                 if (c < g.nbp) {
-                    double x = (r == x0 + tid) ? apre : g.A[(size_t)r * n + i];
-                    for (int t = 0; t < c; t++) x -= Vr[t] * s_wi[t] + Wr[t] * s_vi[t];
-                    as[lr] = x;
-                    g.a[r] = x;
-                    g.ahl[r] = df_split(x);
-                    if (r >= i + 2) nrm += x * x;
+                    // this column's A entry, loaded one phase early for the warp's first rows
+                    const double xp = __shfl_sync(0xffffffffu, apre, kk < 32 ? kk : 0);
+                    double pb = 0.0;
+                    if (lane < c) pb = Vr[lane] * s_wi[lane] + (lane == cp ? wr : Wr[lane]) * s_vi[lane];
+                    pb = warp_sum(pb);
+                    if (lane == 0) {
+                        const double x = (kk < TRD_PRE ? xp : g.A[(size_t)r * n + i]) - pb;
+                        as[lr] = x;
+                        g.a[r] = x;
+                        g.ahl[r] = df_split(x);
+                        if (r >= i + 2) nrm += x * x;
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    Wr[cp] = wr;
+                    g.W[(size_t)r * LDP + cp] = wr;
                 }
             }
             if (c == g.nbp) break;
@@ -255,9 +270,9 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         if (!grid_barrier(g.bar, g.err)) return;
 
         // ---------------- phase Y: reflector of column i, y = A v on the trailing matrix
-        {   // the next column's A entries of this thread's row (A does not change during the panel)
-            const int rn = max(rb0, i + 1) + tid;
-            if (c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
+        {   // the next column's A entries of the warp's first rows (A does not change during the panel)
+            const int rn = max(rb0, i + 1) + warp + TRD_WARPS * lane;
+            if (lane < TRD_PRE && c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
         }
         if (warp == 0) {
             const double sig = grid_total(g.part, 2 * TRD_NB + 1, lane);
@@ -293,7 +308,9 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         // warp per row: y[r] = A[r][i+1] + scale sum_{k>=1} A[r][i+1+k] a[i+1+k], the sum in
         // double-float FP32 arithmetic (products split exactly by FMA, heads added by TwoSum):
         // about 2^-47 relative to sum |A a|, at the FP32 rate instead of GB300's FP64 rate
-        for (int r = y0 + warp; r < rb1; r += TRD_WARPS) {
+        const int nrw = (rb1 - y0 - warp + TRD_WARPS - 1) / TRD_WARPS;  // this warp's rows
+        for (int rk = 0; rk < nrw; rk++) {
+            const int r = y0 + warp + TRD_WARPS * ((c & 1) ? nrw - 1 - rk : rk);
             const float2 *Ar = g.Ahl + (size_t)r * n + i + 1;
             // elements k = kb.. as 16-byte pairs (four loads of 512 B per warp in flight);
             // an unaligned element k = 1 and an odd last element go to lane 0
@@ -313,33 +330,32 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 l += ((h - (t - bp)) + (p - bp)) + e;
                 h = t;
             };
-            int j = lane;
-            for (; j + 7 * 32 < npair; j += 8 * 32) {
+            // eight 16-byte loads in flight per lane, the last partial block predicated; odd
+            // columns walk the rows backwards, so they start on the data the previous column
+            // read last (still in L2)
+            const int nfull = npair / (8 * 32);
+            auto block = [&](int jb, bool tail) {
+                const int j = jb * (8 * 32) + lane;
                 float4 x[8];
 #pragma unroll
-                for (int u = 0; u < 8; u++) x[u] = A4[j + 32 * u];
+                for (int u = 0; u < 8; u++)
+                    x[u] = (!tail || j + 32 * u < npair) ? A4[j + 32 * u] : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
-                    const int e = 2 * (j + 32 * u);
-                    acc(x[u].x, x[u].y, vbh[e], vbl[e], sh[2 * (u & 3)], sl[2 * (u & 3)]);
-                    acc(x[u].z, x[u].w, vbh[e + 1], vbl[e + 1], sh[2 * (u & 3) + 1], sl[2 * (u & 3) + 1]);
+                    if (!tail || j + 32 * u < npair) {
+                        const int e = 2 * (j + 32 * u);
+                        acc(x[u].x, x[u].y, vbh[e], vbl[e], sh[2 * (u & 3)], sl[2 * (u & 3)]);
+                        acc(x[u].z, x[u].w, vbh[e + 1], vbl[e + 1], sh[2 * (u & 3) + 1], sl[2 * (u & 3) + 1]);
+                    }
                 }
-            }
-            for (; j + 3 * 32 < npair; j += 4 * 32) {
-                float4 x[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) x[u] = A4[j + 32 * u];
-#pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int e = 2 * (j + 32 * u);
-                    acc(x[u].x, x[u].y, vbh[e], vbl[e], sh[2 * u], sl[2 * u]);
-                    acc(x[u].z, x[u].w, vbh[e + 1], vbl[e + 1], sh[2 * u + 1], sl[2 * u + 1]);
-                }
-            }
-            for (; j < npair; j += 32) {
-                const float4 x = A4[j];
-                acc(x.x, x.y, vbh[2 * j], vbl[2 * j], sh[0], sl[0]);
-                acc(x.z, x.w, vbh[2 * j + 1], vbl[2 * j + 1], sh[1], sl[1]);
+            };
+            const bool tail = nfull * (8 * 32) < npair;
+            if (c & 1) {
+                if (tail) block(nfull, true);
+                for (int jb = nfull - 1; jb >= 0; jb--) block(jb, false);
+            } else {
+                for (int jb = 0; jb < nfull; jb++) block(jb, false);
+                if (tail) block(nfull, true);
             }
             if (lane == 0) {
                 if (kb == 2 && m > 1) {
@@ -368,19 +384,38 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             }
         }
         __syncthreads();
-        // partials over this CTA's rows: p_t = V[:,t].v, q_t = W[:,t].v (t < c), y.v
+        // partials over this CTA's rows: p_t = V[:,t].v, q_t = W[:,t].v (t < c), y.v;
+        // all components at once: thread (group gq of 8, component t), the 8 groups'
+        // sums added in order through shared memory
         const int ncomp = 2 * c + 1;
-        for (int t = warp; t < ncomp; t += TRD_WARPS) {
-            double s = 0.0;
-            for (int r = y0 + lane; r < rb1; r += 32) {
+        {
+            const int gq = tid >> 6;
+            double sp[2] = {0.0, 0.0};
+            for (int r = y0 + gq; r < rb1; r += 8) {
                 const int lr = r - rb0;
                 const double vr = (r == i + 1) ? 1.0 : as[lr] * scale;
-                const double x = t < c ? Vs[(size_t)lr * TRD_NB + t] : (t < 2 * c ? Ws[(size_t)lr * TRD_NB + (t - c)] : ys[lr]);
-                s += x * vr;
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const int t = (tid & 63) + 64 * h;
+                    if (t < ncomp) {
+                        const double x = t < c ? Vs[(size_t)lr * TRD_NB + t]
+                                               : (t < 2 * c ? Ws[(size_t)lr * TRD_NB + (t - c)] : ys[lr]);
+                        sp[h] += x * vr;
+                    }
+                }
             }
-            s = warp_sum(s);
-            const int comp = t < c ? t : (t < 2 * c ? TRD_NB + (t - c) : 2 * TRD_NB);
-            if (lane == 0) g.part[(size_t)comp * G + b] = s;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int t = (tid & 63) + 64 * h;
+                if (t < ncomp) s_pp[gq][t] = sp[h];
+            }
+            __syncthreads();
+            if (tid < ncomp) {
+                double sum = 0.0;
+                for (int q8 = 0; q8 < 8; q8++) sum += s_pp[q8][tid];
+                const int comp = tid < c ? tid : (tid < 2 * c ? TRD_NB + (tid - c) : 2 * TRD_NB);
+                g.part[(size_t)comp * G + b] = sum;
+            }
         }
         if (!grid_barrier(g.bar, g.err)) return;
     }

@@ -317,11 +317,12 @@ def test_alpha_vs_oracle(mg, orc, golden):
         assert np.sqrt(abs(d @ G @ d)) <= 1e-8 * np.sqrt(a_ref @ G @ a_ref)
 
 
-@pytest.mark.parametrize("S", [1, 16, 17, 32, 40])
+@pytest.mark.parametrize("S", [1, 16, 17, 32, 40, 130])
 def test_alpha_products_any_shape_count(mg, S):
     """alpha = (beta lambda^T) lambda and modesR = alpha orthol for S shapes: one
-    or two 16-row passes of the skinny products (S <= 32) or the tiled product
-    (S > 32), against numpy on the downloaded orthogonalisation outputs."""
+    or two 16-row passes of the skinny products (S <= 32) or the FP64-accurate
+    tensor-core product (S > 32), against numpy on the downloaded
+    orthogonalisation outputs."""
     rng = np.random.default_rng(40 + S)
     N = 200
     A = rng.standard_normal((N, N))

@@ -368,10 +368,18 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                     acc(x.x, x.y, svh[k], svl[k], sh[3], sl[3]);
                 }
             }
-            double part = 0.0;
+            // the lane's eight (head, tail) sums combined in double-FP32 (TwoSum), so that only
+            // one conversion and the warp sum use the FP64 pipe (one warp instruction per 16
+            // cycles of an SM on GB300)
+            float hh = sh[0], hl = sl[0];
 #pragma unroll
-            for (int u = 0; u < 8; u++) part += (double)sh[u] + (double)sl[u];
-            const double ssum = warp_sum(part);
+            for (int u = 1; u < 8; u++) {
+                const float t = hh + sh[u], bp = t - hh;
+                const float e = ((hh - (t - bp)) + (sh[u] - bp)) + (hl + sl[u]);
+                hh = t + e;
+                hl = e - (hh - t);
+            }
+            const double ssum = warp_sum((double)hh + (double)hl);
             if (lane == 0) {
                 const float2 a0 = Ar[0];
                 const double s = fma(scale, ssum, (double)a0.x + (double)a0.y);

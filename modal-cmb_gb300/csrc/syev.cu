@@ -42,7 +42,7 @@ constexpr int TRD_NB = 32;                 // panel width
 constexpr int DC_DEFL_SMEM = 216 * 1024;    // shared memory of the deflation's serial loop (bytes)
 constexpr int TRD_THREADS = 512;           // 16 warps per CTA
 constexpr int TRD_WARPS = TRD_THREADS / 32;
-constexpr int TRD_PRE = 4;                 // rows per warp whose next-column A entry is prefetched
+constexpr int VLD = TRD_NB + 1;            // shared-memory row stride of V, W (odd: no bank conflicts across rows)
 constexpr int LDP = 2 * TRD_NB;            // panel row: V (TRD_NB columns) then W
 constexpr int PCOMP = 2 * TRD_NB + 2;      // partial components: p[NB], q[NB], y.v, |x|^2
 constexpr int NBB = 256;                   // reflectors per block of the back-transformation
@@ -169,11 +169,11 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
     const int R = (n - g.j0 + G - 1) / G;
     const int rb0 = min(n, g.j0 + b * R), rb1 = min(n, rb0 + R);
     float *svh = reinterpret_cast<float *>(sm), *svl = svh + n;  // the column a as head, tail (v = scale a)
-    double *Vs = sm + n, *Ws = Vs + (size_t)R * TRD_NB, *ys = Ws + (size_t)R * TRD_NB, *as = ys + R;
-    for (int e = tid; e < 2 * R * TRD_NB; e += blockDim.x) Vs[e] = 0.0;
+    double *Vs = sm + n, *Ws = Vs + (size_t)R * VLD, *ys = Ws + (size_t)R * VLD, *as = ys + R;
+    for (int e = tid; e < 2 * R * VLD; e += blockDim.x) Vs[e] = 0.0;
     __syncthreads();
 
-    double apre = 0.0;  // lane k: the next column's A entry of the warp's k-th row (k < TRD_PRE)
+    double apre = 0.0;  // this thread's row of the next column of A, loaded one phase early
     for (int c = 0; c <= g.nbp; c++) {
         const int i = g.j0 + c;  // column reduced now; head row of reflector c - 1
         const int x0 = max(rb0, i);
@@ -219,34 +219,35 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             }
             __syncthreads();
             const double yvc = s_scal[0], whead = s_scal[1];
-            // warp per row: the row's w entry and its updated column entry, each a
-            // sum over the panel's c columns by the lanes
-            int kk = 0;
-            for (int r = x0 + warp; r < rb1; r += TRD_WARPS, kk++) {
+            // thread per row: the row's w entry and its updated column entry, each a sum over
+            // the panel's columns in four independent chains (the FP64 pipe of an SM takes one
+            // warp instruction per 16 cycles on GB300, so the rows share as few warps as
+            // possible and no warp-wide reductions)
+            for (int r = x0 + tid; r < rb1; r += blockDim.x) {
                 const int lr = r - rb0;
-                double *Vr = Vs + (size_t)lr * TRD_NB, *Wr = Ws + (size_t)lr * TRD_NB;
-                double pa = 0.0;
-                if (lane < cp) pa = Vr[lane] * q[lane] + Wr[lane] * p[lane];
-                pa = warp_sum(pa);
-                const double wr = (r == i) ? whead : taup * (ys[lr] - pa) - 0.5 * taup * taup * yvc * Vr[cp];
+                double *Vr = Vs + (size_t)lr * VLD, *Wr = Ws + (size_t)lr * VLD;
+                double a4[4] = {0.0, 0.0, 0.0, 0.0};
+                int t = 0;
+                for (; t + 3 < cp; t += 4)
+#pragma unroll
+                    for (int u = 0; u < 4; u++) a4[u] = fma(Vr[t + u], q[t + u], fma(Wr[t + u], p[t + u], a4[u]));
+                for (; t < cp; t++) a4[0] = fma(Vr[t], q[t], fma(Wr[t], p[t], a4[0]));
+                const double s = ys[lr] - ((a4[0] + a4[1]) + (a4[2] + a4[3]));
+                const double wr = (r == i) ? whead : taup * s - 0.5 * taup * taup * yvc * Vr[cp];
+                Wr[cp] = wr;
+                g.W[(size_t)r * LDP + cp] = wr;
                 if (c < g.nbp) {
-                    // this column's A entry, loaded one phase early for the warp's first rows
-                    const double xp = __shfl_sync(0xffffffffu, apre, kk < 32 ? kk : 0);
-                    double pb = 0.0;
-                    if (lane < c) pb = Vr[lane] * s_wi[lane] + (lane == cp ? wr : Wr[lane]) * s_vi[lane];
-                    pb = warp_sum(pb);
-                    if (lane == 0) {
-                        const double x = (kk < TRD_PRE ? xp : g.A[(size_t)r * n + i]) - pb;
-                        as[lr] = x;
-                        g.a[r] = x;
-                        g.ahl[r] = df_split(x);
-                        if (r >= i + 2) nrm += x * x;
-                    }
-                }
-                __syncwarp();
-                if (lane == 0) {
-                    Wr[cp] = wr;
-                    g.W[(size_t)r * LDP + cp] = wr;
+                    double b4[4] = {0.0, 0.0, 0.0, 0.0};
+                    t = 0;
+                    for (; t + 3 < c; t += 4)
+#pragma unroll
+                        for (int u = 0; u < 4; u++) b4[u] = fma(Vr[t + u], s_wi[t + u], fma(Wr[t + u], s_vi[t + u], b4[u]));
+                    for (; t < c; t++) b4[0] = fma(Vr[t], s_wi[t], fma(Wr[t], s_vi[t], b4[0]));
+                    const double x = ((r == x0 + tid) ? apre : g.A[(size_t)r * n + i]) - ((b4[0] + b4[1]) + (b4[2] + b4[3]));
+                    as[lr] = x;
+                    g.a[r] = x;
+                    g.ahl[r] = df_split(x);
+                    if (r >= i + 2) nrm += x * x;
                 }
             }
             if (c == g.nbp) break;
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 if (r >= i + 2) nrm += x * x;
             }
         }
-        nrm = warp_sum(nrm);
+        if (x0 + 32 * warp < rb1) nrm = warp_sum(nrm);  // only the warps that hold rows
         if (lane == 0) s_red[warp] = nrm;
         __syncthreads();
         if (tid == 0) {
@@ -270,9 +271,9 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         if (!grid_barrier(g.bar, g.err)) return;
 
         // ---------------- phase Y: reflector of column i, y = A v on the trailing matrix
-        {   // the next column's A entries of the warp's first rows (A does not change during the panel)
-            const int rn = max(rb0, i + 1) + warp + TRD_WARPS * lane;
-            if (lane < TRD_PRE && c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
+        {   // the next column's A entry of this thread's row (A does not change during the panel)
+            const int rn = max(rb0, i + 1) + tid;
+            if (c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
         }
         if (warp == 0) {
             const double sig = grid_total(g.part, 2 * TRD_NB + 1, lane);
@@ -387,7 +388,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 const double vr = (r == i + 1) ? 1.0 : as[lr] * scale;
                 ys[lr] = s;
                 g.y[r] = s;
-                Vs[(size_t)lr * TRD_NB + c] = vr;
+                Vs[(size_t)lr * VLD + c] = vr;
                 g.V[(size_t)r * LDP + c] = vr;
             }
         }
@@ -406,8 +407,8 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 for (int h = 0; h < 2; h++) {
                     const int t = (tid & 63) + 64 * h;
                     if (t < ncomp) {
-                        const double x = t < c ? Vs[(size_t)lr * TRD_NB + t]
-                                               : (t < 2 * c ? Ws[(size_t)lr * TRD_NB + (t - c)] : ys[lr]);
+                        const double x = t < c ? Vs[(size_t)lr * VLD + t]
+                                               : (t < 2 * c ? Ws[(size_t)lr * VLD + (t - c)] : ys[lr]);
                         sp[h] += x * vr;
                     }
                 }
@@ -1097,7 +1098,7 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
     int Rmax = 1;
     for (int j0 = 0; j0 < n - 1; j0 += TRD_NB) Rmax = std::max(Rmax, ceil_div(n - j0, grid_of(n - j0)));
     // v (n) + this CTA's V and W rows (Rmax x NB each) + y and a (Rmax each)
-    const size_t smem = sizeof(double) * ((size_t)n + (size_t)Rmax * (2 * TRD_NB + 2));
+    const size_t smem = sizeof(double) * ((size_t)n + (size_t)Rmax * (2 * VLD + 2));
     if (smem > 200 * 1024) { set_error("eigensolver: n = %d exceeds the panel kernel's shared memory", n); return MODAL_ERR_ARG; }
     MODAL_CUDA(cudaFuncSetAttribute(k_trd_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;

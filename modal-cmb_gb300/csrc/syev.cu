@@ -182,6 +182,17 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         if (c > 0) {
             const int cp = c - 1;
             const int ncomp = 2 * cp + 1;
+            // the head row's V, W entries and y, loaded before the reduction so that their
+            // latency overlaps it (written before the last grid barrier)
+            double vi = 0.0, wi = 0.0, yi = 0.0, taup = 0.0;
+            if (warp == 0) {
+                if (lane < c) {
+                    vi = g.V[(size_t)i * LDP + lane];
+                    wi = g.W[(size_t)i * LDP + lane];
+                }
+                yi = g.y[i];
+                taup = g.tau[i - 1];
+            }
             {   // grid sums of the previous phase's partials, 8 threads per component
                 const int ci = tid >> 3, sub = tid & 7;
                 double s = 0.0;
@@ -197,27 +208,26 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 if (ci < ncomp && sub == 0) s_pq[ci] = s;  // p[0..cp), q[0..cp), y.v
             }
             __syncthreads();
-            const double taup = g.tau[i - 1];
             const double *p = s_pq, *q = s_pq + cp;
             if (warp == 0) {
-                const double *Vi = g.V + (size_t)i * LDP, *Wi = g.W + (size_t)i * LDP;
                 double pq = 0.0, hv = 0.0;
                 if (lane < cp) {
                     pq = p[lane] * q[lane];
-                    hv = Vi[lane] * q[lane] + Wi[lane] * p[lane];
+                    hv = vi * q[lane] + wi * p[lane];
                 }
                 pq = warp_sum(pq);
                 hv = warp_sum(hv);
                 const double yvc = s_pq[2 * cp] - 2.0 * pq;  // (corrected y).v
                 // w of row i (head row: v = 1 there), computed by every CTA alike
-                const double whead = taup * (g.y[i] - hv) - 0.5 * taup * taup * yvc;
-                if (lane == 0) { s_scal[0] = yvc; s_scal[1] = whead; }
+                const double whead = taup * (yi - hv) - 0.5 * taup * taup * yvc;
+                if (lane == 0) { s_scal[0] = yvc; s_scal[1] = whead; s_scal[3] = taup; }
                 if (c < g.nbp && lane < c) {
-                    s_vi[lane] = Vi[lane];
-                    s_wi[lane] = (lane == cp) ? whead : Wi[lane];
+                    s_vi[lane] = vi;
+                    s_wi[lane] = (lane == cp) ? whead : wi;
                 }
             }
             __syncthreads();
+            const double taup_all = s_scal[3];
             const double yvc = s_scal[0], whead = s_scal[1];
             // thread per row: the row's w entry and its updated column entry, each a sum over
             // the panel's columns in four independent chains (the FP64 pipe of an SM takes one
@@ -233,7 +243,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                     for (int u = 0; u < 4; u++) a4[u] = fma(Vr[t + u], q[t + u], fma(Wr[t + u], p[t + u], a4[u]));
                 for (; t < cp; t++) a4[0] = fma(Vr[t], q[t], fma(Wr[t], p[t], a4[0]));
                 const double s = ys[lr] - ((a4[0] + a4[1]) + (a4[2] + a4[3]));
-                const double wr = (r == i) ? whead : taup * s - 0.5 * taup * taup * yvc * Vr[cp];
+                const double wr = (r == i) ? whead : taup_all * s - 0.5 * taup_all * taup_all * yvc * Vr[cp];
                 Wr[cp] = wr;
                 g.W[(size_t)r * LDP + cp] = wr;
                 if (c < g.nbp) {
@@ -276,9 +286,9 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             if (c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
         }
         if (warp == 0) {
+            const double alpha = (lane == 0) ? g.a[i + 1] : 0.0;  // issued before the reduction
             const double sig = grid_total(g.part, 2 * TRD_NB + 1, lane);
             if (lane == 0) {
-                const double alpha = g.a[i + 1];
                 double beta, tau, scale;
                 if (sig == 0.0) {
                     beta = alpha; tau = 0.0; scale = 0.0;
@@ -402,7 +412,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             double sp[2] = {0.0, 0.0};
             for (int r = y0 + gq; r < rb1; r += 8) {
                 const int lr = r - rb0;
-                const double vr = (r == i + 1) ? 1.0 : as[lr] * scale;
+                const double vr = Vs[(size_t)lr * VLD + c];  // v of the row, stored with the product
 #pragma unroll
                 for (int h = 0; h < 2; h++) {
                     const int t = (tid & 63) + 64 * h;

@@ -229,35 +229,48 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
             __syncthreads();
             const double taup_all = s_scal[3];
             const double yvc = s_scal[0], whead = s_scal[1];
-            // thread per row: the row's w entry and its updated column entry, each a sum over
-            // the panel's columns in four independent chains (the FP64 pipe of an SM takes one
-            // warp instruction per 16 cycles on GB300, so the rows share as few warps as
-            // possible and no warp-wide reductions)
-            for (int r = x0 + tid; r < rb1; r += blockDim.x) {
-                const int lr = r - rb0;
-                double *Vr = Vs + (size_t)lr * VLD, *Wr = Ws + (size_t)lr * VLD;
-                double a4[4] = {0.0, 0.0, 0.0, 0.0};
-                int t = 0;
-                for (; t + 3 < cp; t += 4)
-#pragma unroll
-                    for (int u = 0; u < 4; u++) a4[u] = fma(Vr[t + u], q[t + u], fma(Wr[t + u], p[t + u], a4[u]));
-                for (; t < cp; t++) a4[0] = fma(Vr[t], q[t], fma(Wr[t], p[t], a4[0]));
-                const double s = ys[lr] - ((a4[0] + a4[1]) + (a4[2] + a4[3]));
-                const double wr = (r == i) ? whead : taup_all * s - 0.5 * taup_all * taup_all * yvc * Vr[cp];
-                Wr[cp] = wr;
-                g.W[(size_t)r * LDP + cp] = wr;
+            // four threads per row: the row's w entry and its updated column entry, each a sum
+            // over the panel's columns, the threads taking every fourth term in two chains and
+            // adding through two shuffles (short FP64 dependency chains on few warps: the FP64
+            // pipe of an SM takes one warp instruction per 16 cycles on GB300)
+            const int nrows = rb1 - x0, sub = tid & 3;
+            for (int rb = 0; rb < nrows; rb += TRD_THREADS / 4) {
+                const int rr = rb + (tid >> 2), r = x0 + rr;
+                const bool ok = rr < nrows;
+                const int lr = ok ? r - rb0 : 0;
+                const double *Vr = Vs + (size_t)lr * VLD, *Wr = Ws + (size_t)lr * VLD;
+                double a0 = 0.0, a1 = 0.0;
+                if (ok)
+                    for (int t = sub; t < cp; t += 8) {
+                        a0 = fma(Vr[t], q[t], fma(Wr[t], p[t], a0));
+                        if (t + 4 < cp) a1 = fma(Vr[t + 4], q[t + 4], fma(Wr[t + 4], p[t + 4], a1));
+                    }
+                double pa = a0 + a1;
+                pa += __shfl_xor_sync(0xffffffffu, pa, 1);
+                pa += __shfl_xor_sync(0xffffffffu, pa, 2);
+                const double wr = ok ? ((r == i) ? whead : taup_all * (ys[lr] - pa) - 0.5 * taup_all * taup_all * yvc * Vr[cp]) : 0.0;
                 if (c < g.nbp) {
-                    double b4[4] = {0.0, 0.0, 0.0, 0.0};
-                    t = 0;
-                    for (; t + 3 < c; t += 4)
-#pragma unroll
-                        for (int u = 0; u < 4; u++) b4[u] = fma(Vr[t + u], s_wi[t + u], fma(Wr[t + u], s_vi[t + u], b4[u]));
-                    for (; t < c; t++) b4[0] = fma(Vr[t], s_wi[t], fma(Wr[t], s_vi[t], b4[0]));
-                    const double x = ((r == x0 + tid) ? apre : g.A[(size_t)r * n + i]) - ((b4[0] + b4[1]) + (b4[2] + b4[3]));
-                    as[lr] = x;
-                    g.a[r] = x;
-                    g.ahl[r] = df_split(x);
-                    if (r >= i + 2) nrm += x * x;
+                    double b0 = 0.0, b1 = 0.0;
+                    if (ok)
+                        for (int t = sub; t < c; t += 8) {
+                            b0 = fma(Vr[t], s_wi[t], fma(t == cp ? wr : Wr[t], s_vi[t], b0));
+                            if (t + 4 < c) b1 = fma(Vr[t + 4], s_wi[t + 4], fma(t + 4 == cp ? wr : Wr[t + 4], s_vi[t + 4], b1));
+                        }
+                    double pb = b0 + b1;
+                    pb += __shfl_xor_sync(0xffffffffu, pb, 1);
+                    pb += __shfl_xor_sync(0xffffffffu, pb, 2);
+                    if (ok && sub == 0) {
+                        const double x = ((rb == 0) ? apre : g.A[(size_t)r * n + i]) - pb;
+                        as[lr] = x;
+                        g.a[r] = x;
+                        g.ahl[r] = df_split(x);
+                        if (r >= i + 2) nrm += x * x;
+                    }
+                }
+                __syncwarp();
+                if (ok && sub == 0) {
+                    Ws[(size_t)lr * VLD + cp] = wr;
+                    g.W[(size_t)r * LDP + cp] = wr;
                 }
             }
             if (c == g.nbp) break;
@@ -270,7 +283,7 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 if (r >= i + 2) nrm += x * x;
             }
         }
-        if (x0 + 32 * warp < rb1) nrm = warp_sum(nrm);  // only the warps that hold rows
+        if (x0 + 8 * warp < rb1) nrm = warp_sum(nrm);  // only the warps that hold rows
         if (lane == 0) s_red[warp] = nrm;
         __syncthreads();
         if (tid == 0) {
@@ -281,9 +294,10 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         if (!grid_barrier(g.bar, g.err)) return;
 
         // ---------------- phase Y: reflector of column i, y = A v on the trailing matrix
-        {   // the next column's A entry of this thread's row (A does not change during the panel)
-            const int rn = max(rb0, i + 1) + tid;
-            if (c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
+        {   // the next column's A entry of this thread's row (A does not change during the panel;
+            // rows of four threads, the first keeps it)
+            const int rn = max(rb0, i + 1) + (tid >> 2);
+            if ((tid & 3) == 0 && c + 1 < g.nbp && rn < rb1) apre = g.A[(size_t)rn * n + i + 1];
         }
         if (warp == 0) {
             const double alpha = (lane == 0) ? g.a[i + 1] : 0.0;  // issued before the reduction

@@ -37,9 +37,9 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64 (nominal; no measured FP64 peak is available)
 # DRAM bytes (read + write) of the tridiagonalisation's panel kernels in one
 # eigen-decomposition at l <= 2000, P = 30 (N = 4960): an ncu capture of the 155
-# panel launches of one eigen-decomposition (dram__bytes_read.sum 2.0724e11 +
-# dram__bytes_write.sum 5.70e8), not measured by this run.
-NCU_PANEL_TRAFFIC_CFG2 = 2.0724e11 + 5.70e8
+# panel launches of one eigen-decomposition (dram__bytes_read.sum 8.4596e10 +
+# dram__bytes_write.sum 4.07e8), not measured by this run.
+NCU_PANEL_TRAFFIC_CFG2 = 8.4596e10 + 4.07e8
 
 
 def parse():

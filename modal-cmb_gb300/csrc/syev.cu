@@ -45,7 +45,8 @@ constexpr int TRD_WARPS = TRD_THREADS / 32;
 constexpr int VLD = TRD_NB + 1;            // shared-memory row stride of V, W (odd: no bank conflicts across rows)
 constexpr int LDP = 2 * TRD_NB;            // panel row: V (TRD_NB columns) then W
 constexpr int PCOMP = 2 * TRD_NB + 2;      // partial components: p[NB], q[NB], y.v, |x|^2
-constexpr int NBB = 256;                   // reflectors per block of the back-transformation
+constexpr int NBB = 256;                   // reflectors per T block built by k_larft
+constexpr int NBW = 512;                   // reflectors per compact-WY block of the back-transformation (two T blocks joined)
 constexpr int OZ_SLICES = 8;               // 7-bit slices of the tensor-core FP64 products
 constexpr int DC_OZ_MIN = 1024;            // merges of at least this size update their vectors on the tensor cores
 constexpr long long BAR_CYCLES = 1ll << 32;  // ~2 s of clock64 per barrier wait
@@ -523,6 +524,21 @@ __global__ void __launch_bounds__(256) k_larft(int nv, const double *__restrict_
         if (threadIdx.x == 0) Tb[(size_t)c * NBB + c] = tc;
         __syncthreads();
     }
+}
+
+// The T factors of the blocks of NBW reflectors from the two NBB blocks each
+// holds: T = [[T1, T12], [0, T2]] (T12 = -T1 (V1^T V2) T2 is added by two
+// products afterwards); grid (NBW * NBW / 256, blocks).
+__global__ void k_tw_assemble(int nv, const double *__restrict__ TB, double *__restrict__ TW)
+{
+    const int k = blockIdx.y, j0 = k * NBW, w = min(NBW, nv - j0);
+    const int e = blockIdx.x * blockDim.x + threadIdx.x, row = e / NBW, col = e % NBW;
+    if (e >= NBW * NBW) return;
+    double v = 0.0;
+    if (row < NBB && col < NBB) v = TB[(size_t)(2 * k) * NBB * NBB + (size_t)row * NBB + col];
+    else if (row >= NBB && col >= NBB && w > NBB)
+        v = TB[(size_t)(2 * k + 1) * NBB * NBB + (size_t)(row - NBB) * NBB + (col - NBB)];
+    TW[(size_t)k * NBW * NBW + e] = v;
 }
 
 // ------------------------------------------------------------------ stage 2
@@ -1006,7 +1022,7 @@ static void build_tree(int a, int b, int lev, std::vector<std::vector<int3>> &ou
 
 // Carve the eigensolver's workspace out of ctx->eigw for size n.
 struct SyevPtrs {
-    double *P, *Psw, *VA, *GB, *TB, *d, *e, *tau, *a, *y, *part;
+    double *P, *Psw, *VA, *GB, *TB, *TW, *TT, *d, *e, *tau, *a, *y, *part;
     float2 *Ahl, *ahl;
     long ldva;
     unsigned *bar;
@@ -1025,15 +1041,17 @@ static size_t carve(uint8_t *base, int n, int npanel, int nlev, int nmerge, Syev
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t r = o; o += (bytes + 255) & ~(size_t)255; return base ? (void *)(base + r) : nullptr; };
     const size_t NN = (size_t)n * n;
-    const long nvpad = (long)std::max(1, ceil_div(std::max(1, n - 1), NBB)) * NBB;
+    const long nvpad = (long)std::max(1, ceil_div(std::max(1, n - 1), NBW)) * NBW;
     p.ldva = nvpad;
     p.P = (double *)take(sizeof(double) * (size_t)n * LDP);
     p.Ahl = (float2 *)take(sizeof(float2) * NN);
     p.ahl = (float2 *)take(sizeof(float2) * n);
     p.Psw = (double *)take(sizeof(double) * (size_t)n * LDP);
     p.VA = (double *)take(sizeof(double) * (size_t)n * nvpad);          // every reflector, column j = v_j
-    p.GB = (double *)take(sizeof(double) * (size_t)nvpad * nvpad);      // diagonal NBB blocks of VA^T VA
+    p.GB = (double *)take(sizeof(double) * (size_t)nvpad * nvpad);      // diagonal NBW blocks of VA^T VA
     p.TB = (double *)take(sizeof(double) * (size_t)(nvpad / NBB) * NBB * NBB);
+    p.TW = (double *)take(sizeof(double) * (size_t)(nvpad / NBW) * NBW * NBW);
+    p.TT = (double *)take(sizeof(double) * (size_t)NBB * NBB);
     p.d = (double *)take(sizeof(double) * n);
     p.e = (double *)take(sizeof(double) * n);
     p.tau = (double *)take(sizeof(double) * n);
@@ -1262,37 +1280,50 @@ static modal_status dc_run(modal_ctx *ctx, int n, SyevState &st, SyevPtrs &p)
 // the Gram matrix VA^T VA (tensor-core products), then dlarft per block.
 static modal_status wy_blocks(modal_ctx *ctx, int n, SyevPtrs &p)
 {
-    const int nv = n - 1, nbig = ceil_div(nv, NBB);
+    const int nv = n - 1, nbig = ceil_div(nv, NBB), nbw = ceil_div(nv, NBW);
     OzOpts o;
     o.slices = OZ_SLICES;
-    o.diag_tiles = NBB / 128;
+    o.diag_tiles = NBW / 128;
     o.check = false;
     MODAL_TRY(oz_gemm_ex(ctx, nv, nv, n, 1.0, p.VA, p.ldva, true, p.VA, p.ldva, false, 0.0, p.GB, p.ldva, o));
     k_larft<<<nbig, 256, 0, ctx->stream>>>(nv, p.GB, p.ldva, p.tau, p.TB);
-    return launched(ctx, "larft");
+    MODAL_TRY(launched(ctx, "larft"));
+    k_tw_assemble<<<dim3(NBW * NBW / 256, nbw), 256, 0, ctx->stream>>>(nv, p.TB, p.TW);
+    MODAL_TRY(launched(ctx, "tw_assemble"));
+    // T12 = -T1 (V1^T V2) T2 for the blocks with two halves (FP64 products, 2 x 256^3 each)
+    for (int k = 0; k < nbw; k++) {
+        const int j0 = k * NBW, w = std::min(NBW, nv - j0), w2 = w - NBB;
+        if (w2 <= 0) continue;
+        const double *G12 = p.GB + (size_t)j0 * p.ldva + j0 + NBB;
+        const double *T1 = p.TB + (size_t)(2 * k) * NBB * NBB, *T2 = p.TB + (size_t)(2 * k + 1) * NBB * NBB;
+        double *T12 = p.TW + (size_t)k * NBW * NBW + NBB;
+        MODAL_TRY(dgemm(ctx, NBB, w2, w2, 1.0, G12, (int)p.ldva, false, T2, NBB, false, 0.0, p.TT, NBB, 0));
+        MODAL_TRY(dgemm(ctx, NBB, w2, NBB, -1.0, T1, NBB, false, p.TT, NBB, false, 0.0, T12, NBW, 0));
+    }
+    return MODAL_OK;
 }
 
 // X[m][n] (rows = vectors in the tridiagonal basis) := X Q^T, Q = H_0 ... H_{n-2}.
-// Per block of NBB reflectors, last block first (block = I - V T V^T):
+// Per block of NBW reflectors, last block first (block = I - V T V^T):
 //   X[:, r:] -= ((X[:, r:] V) T^T) V^T,  r = first row where the block's V is nonzero.
 static modal_status backtransform(modal_ctx *ctx, int n, int m, double *X, int ldx, SyevPtrs &p)
 {
     if (m <= 0 || n < 2) return MODAL_OK;
     MODAL_TRY(wy_blocks(ctx, n, p));
-    MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)m * NBB * 2));
-    double *XV = ctx->scratch2.as<double>(), *XT = XV + (size_t)m * NBB;
-    const int nv = n - 1, nbig = ceil_div(nv, NBB);
+    MODAL_TRY(ensure(ctx->scratch2, sizeof(double) * (size_t)m * NBW * 2));
+    double *XV = ctx->scratch2.as<double>(), *XT = XV + (size_t)m * NBW;
+    const int nv = n - 1, nbw = ceil_div(nv, NBW);
     OzOpts o;
     o.slices = OZ_SLICES;
     o.check = false;
-    for (int bb = nbig - 1; bb >= 0; bb--) {
-        const int j0 = bb * NBB, w = std::min(NBB, nv - j0);
+    for (int bb = nbw - 1; bb >= 0; bb--) {
+        const int j0 = bb * NBW, w = std::min(NBW, nv - j0);
         const int r = j0 + 1, K = n - r;
         const double *V = p.VA + (size_t)r * p.ldva + j0;
-        const double *T = p.TB + (size_t)bb * NBB * NBB;
-        MODAL_TRY(oz_gemm_ex(ctx, m, w, K, 1.0, X + r, ldx, false, V, p.ldva, false, 0.0, XV, NBB, o));
-        MODAL_TRY(oz_gemm_ex(ctx, m, w, w, 1.0, XV, NBB, false, T, NBB, true, 0.0, XT, NBB, o));
-        MODAL_TRY(oz_gemm_ex(ctx, m, K, w, -1.0, XT, NBB, false, V, p.ldva, true, 1.0, X + r, ldx, o));
+        const double *T = p.TW + (size_t)bb * NBW * NBW;
+        MODAL_TRY(oz_gemm_ex(ctx, m, w, K, 1.0, X + r, ldx, false, V, p.ldva, false, 0.0, XV, NBW, o));
+        MODAL_TRY(oz_gemm_ex(ctx, m, w, w, 1.0, XV, NBW, false, T, NBW, true, 0.0, XT, NBW, o));
+        MODAL_TRY(oz_gemm_ex(ctx, m, K, w, -1.0, XT, NBW, false, V, p.ldva, true, 1.0, X + r, ldx, o));
     }
     return oz_check(ctx);
 }

@@ -367,15 +367,24 @@ __global__ void __launch_bounds__(192, 1) k_oz_gemm(const __grid_constant__ CUte
                 __syncwarp();
                 const int n = n0 + c0 + lane;
                 const double cs = (n < a.N) ? ldexp(1.0, a.eb[n]) : 0.0;
-                for (int rr = 0; rr < 32; rr++) {
-                    const int mm = mrow + rr;
-                    if (mm >= a.M || n >= a.N || (a.lower && n > mm)) continue;
-                    const double v = st[rr * 33 + lane] * cs;
-                    if (split) {
-                        a.part[((size_t)tile.z * a.M + mm) * a.N + n] = v;
-                    } else {
-                        double *cp = a.C + (size_t)mm * a.ldc + n;
-                        *cp = (a.beta == 0.0) ? a.alpha * v : fma(a.beta, *cp, a.alpha * v);
+                // the C values of 16 rows are loaded together before any store (one round
+                // trip per 16 rows instead of one per row)
+#pragma unroll 1
+                for (int r0 = 0; r0 < 32; r0 += 16) {
+                    double cv[16];
+#pragma unroll
+                    for (int rr = 0; rr < 16; rr++) {
+                        const int mm = mrow + r0 + rr;
+                        const bool ok = !split && a.beta != 0.0 && mm < a.M && n < a.N && !(a.lower && n > mm);
+                        cv[rr] = ok ? a.C[(size_t)mm * a.ldc + n] : 0.0;
+                    }
+#pragma unroll
+                    for (int rr = 0; rr < 16; rr++) {
+                        const int mm = mrow + r0 + rr;
+                        if (mm >= a.M || n >= a.N || (a.lower && n > mm)) continue;
+                        const double v = st[(r0 + rr) * 33 + lane] * cs;
+                        if (split) a.part[((size_t)tile.z * a.M + mm) * a.N + n] = v;
+                        else a.C[(size_t)mm * a.ldc + n] = (a.beta == 0.0) ? a.alpha * v : fma(a.beta, cv[rr], a.alpha * v);
                     }
                 }
                 __syncwarp();

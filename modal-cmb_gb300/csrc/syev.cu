@@ -138,10 +138,15 @@ struct TrdArgs {
 // Sum over the grid of component `comp` of the partials, by one warp (fixed order).
 __device__ __forceinline__ double grid_total(const double *part, int comp, int lane)
 {
-    double s = 0.0;
+    double s0 = 0.0, s1 = 0.0;
     const double *p = part + (size_t)comp * gridDim.x;
-    for (int b = lane; b < (int)gridDim.x; b += 32) s += p[b];
-    return warp_sum(s);
+    int b = lane;
+    for (; b + 32 < (int)gridDim.x; b += 64) {
+        s0 += p[b];
+        s1 += p[b + 32];
+    }
+    if (b < (int)gridDim.x) s0 += p[b];
+    return warp_sum(s0 + s1);
 }
 
 // Panel of the tridiagonalisation (dlatrd, lower) as one cooperative launch.
@@ -200,8 +205,16 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 if (ci < ncomp) {
                     const int comp = ci < cp ? ci : (ci < 2 * cp ? TRD_NB + (ci - cp) : 2 * TRD_NB);
                     const double *pp = g.part + (size_t)comp * G;
-#pragma unroll 4
-                    for (int bb = sub; bb < G; bb += 8) s += pp[bb];
+                    // four independent chains (GB300's FP64 additions have a long latency)
+                    double s4[4] = {0.0, 0.0, 0.0, 0.0};
+                    int bb = sub;
+                    for (; bb + 24 < G; bb += 32)
+#pragma unroll
+                        for (int u = 0; u < 4; u++) s4[u] += pp[bb + 8 * u];
+                    if (bb < G) s4[0] += pp[bb];
+                    if (bb + 8 < G) s4[1] += pp[bb + 8];
+                    if (bb + 16 < G) s4[2] += pp[bb + 16];
+                    s = (s4[0] + s4[1]) + (s4[2] + s4[3]);
                 }
                 s += __shfl_xor_sync(0xffffffffu, s, 1);
                 s += __shfl_xor_sync(0xffffffffu, s, 2);
@@ -288,9 +301,11 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
         if (lane == 0) s_red[warp] = nrm;
         __syncthreads();
         if (tid == 0) {
-            double s = 0.0;
-            for (int w = 0; w < TRD_WARPS; w++) s += s_red[w];
-            g.part[(size_t)(2 * TRD_NB + 1) * G + b] = s;
+            double s4[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                s4[u] = (s_red[u] + s_red[u + 4]) + (s_red[u + 8] + s_red[u + 12]);
+            g.part[(size_t)(2 * TRD_NB + 1) * G + b] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
         }
         if (!grid_barrier(g.bar, g.err)) return;
 
@@ -405,7 +420,17 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
                 hh = t + e;
                 hl = e - (hh - t);
             }
-            const double ssum = warp_sum((double)hh + (double)hl);
+            // the warp's sum in double-FP32 as well (short FP32 dependency chains instead of
+            // FP64 ones), converted once
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, hh, o), ol = __shfl_xor_sync(0xffffffffu, hl, o);
+                const float t = hh + oh, bp = t - hh;
+                const float e = ((hh - (t - bp)) + (oh - bp)) + (hl + ol);
+                hh = t + e;
+                hl = e - (hh - t);
+            }
+            const double ssum = (double)hh + (double)hl;
             if (lane == 0) {
                 const float2 a0 = Ar[0];
                 const double s = fma(scale, ssum, (double)a0.x + (double)a0.y);
@@ -606,12 +631,14 @@ __device__ void dc_deflate_serial(DcWork &w, MergeInfo &M, int a, int k, double 
         for (int nj = 0; nj < k; nj++) {
             if (rho * fabs(z[nj]) <= tol) { w.dl[a + nd++] = a + nj; continue; }
             if (pj < 0) { pj = nj; continue; }
-            double s = z[pj], c = z[nj];
-            const double tau = hypot(c, s);
-            const double t = D[nj] - D[pj];
-            c /= tau;
-            s = -s / tau;
-            if (fabs(t * c * s) <= tol) {
+            // |t c s| <= tol with c = z_nj / tau, s = -z_pj / tau, tau^2 = z_pj^2 + z_nj^2,
+            // tested without the square root and divisions (on GB300's slow FP64 pipe);
+            // the rotation is formed only for the pairs that deflate
+            const double zp = z[pj], zn = z[nj], t = D[nj] - D[pj];
+            const double r2 = zp * zp + zn * zn;
+            if (fabs(t) * fabs(zp * zn) <= tol * r2) {
+                const double tau = sqrt(r2);
+                const double c = zn / tau, s = -zp / tau;
                 fl[nj] |= fl[pj];  // the rotated vector has support on both halves
                 z[nj] = tau;
                 z[pj] = 0.0;
@@ -777,9 +804,10 @@ __global__ void __launch_bounds__(256) k_dc_secular(DcWork w)
         double psi = 0.0, phi = 0.0, dpsi = 0.0, dphi = 0.0;
         for (int i = lane; i < kk; i += 32) {
             const double dlt = (dl[i] - dorg) - tau;
-            const double t = z[i] * z[i] / dlt;
-            if (i <= j) { psi += t; dpsi += t / dlt; }
-            else { phi += t; dphi += t / dlt; }
+            const double rd = 1.0 / dlt;  // one FP64 division per term (GB300's FP64 pipe is slow)
+            const double t = z[i] * z[i] * rd;
+            if (i <= j) { psi += t; dpsi += t * rd; }
+            else { phi += t; dphi += t * rd; }
         }
         psi = rho * warp_sum(psi);
         phi = rho * warp_sum(phi);

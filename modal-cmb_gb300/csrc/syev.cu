@@ -1318,15 +1318,19 @@ static modal_status wy_blocks(modal_ctx *ctx, int n, SyevPtrs &p)
     MODAL_TRY(launched(ctx, "larft"));
     k_tw_assemble<<<dim3(NBW * NBW / 256, nbw), 256, 0, ctx->stream>>>(nv, p.TB, p.TW);
     MODAL_TRY(launched(ctx, "tw_assemble"));
-    // T12 = -T1 (V1^T V2) T2 for the blocks with two halves (FP64 products, 2 x 256^3 each)
+    // T12 = -T1 (V1^T V2) T2 for the blocks with two halves (FP64-accurate tensor-core products,
+    // 2 x 256^3 each: the FP64 tiled kernel would run them on 16 CTAs at GB300's FP64 rate)
+    OzOpts oj;
+    oj.slices = OZ_SLICES;
+    oj.check = false;
     for (int k = 0; k < nbw; k++) {
         const int j0 = k * NBW, w = std::min(NBW, nv - j0), w2 = w - NBB;
         if (w2 <= 0) continue;
         const double *G12 = p.GB + (size_t)j0 * p.ldva + j0 + NBB;
         const double *T1 = p.TB + (size_t)(2 * k) * NBB * NBB, *T2 = p.TB + (size_t)(2 * k + 1) * NBB * NBB;
         double *T12 = p.TW + (size_t)k * NBW * NBW + NBB;
-        MODAL_TRY(dgemm(ctx, NBB, w2, w2, 1.0, G12, (int)p.ldva, false, T2, NBB, false, 0.0, p.TT, NBB, 0));
-        MODAL_TRY(dgemm(ctx, NBB, w2, NBB, -1.0, T1, NBB, false, p.TT, NBB, false, 0.0, T12, NBW, 0));
+        MODAL_TRY(oz_gemm_ex(ctx, NBB, w2, w2, 1.0, G12, p.ldva, false, T2, NBB, false, 0.0, p.TT, NBB, oj));
+        MODAL_TRY(oz_gemm_ex(ctx, NBB, w2, NBB, -1.0, T1, NBB, false, p.TT, NBB, false, 0.0, T12, NBW, oj));
     }
     return MODAL_OK;
 }

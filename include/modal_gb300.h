@@ -475,12 +475,15 @@ modal_status modal_lambda_min(modal_ctx *ctx, double *lambda_min, double *eigvec
  * (MODAL_NOALLOC_SCRATCH_BYTES); every GPU that loads the library holds it
  * until exit.  Problems needing more (about lmax <= 500 with P <= 10, or
  * lmax <= 600 with P <= 6, fit) are rejected with MODAL_ERR_ARG and a
- * message giving the size needed; no device memory is ever allocated.  The
- * first call on a device looks up the array's device address and should
- * come before any stream capture; that address is kept for the life of the
- * process, so do not reset the device while the library is loaded.  Every
- * call reads a status word back and waits for `stream` before returning.  All calls share the array: calls that
- * overlap on the GPU (different streams or threads) race, so serialise them.
+ * message giving the size needed; no device memory is ever allocated.
+ * Every call reads a status word back into host memory and waits for
+ * `stream` before returning, so NO call may be made while a stream is being
+ * captured into a CUDA graph (the copy and the synchronisation are illegal
+ * during capture and would invalidate the caller's capture).  The first call
+ * on a device looks up the array's device address; that address is kept for
+ * the life of the process, so do not reset the device while the library is
+ * loaded.  All calls share the array: calls that overlap on the GPU
+ * (different streams or threads) race, so serialise them.
  * Out-of-range triples give MODAL_ERR_ARG. */
 #define MODAL_NOALLOC_SCRATCH_BYTES (8u << 20)
 modal_status modal_gamma_fp64_noalloc(int lmin, int lmax, int P, const double *d_q, int N,

@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <vector>
 #include "common.cuh"
+#include "dfbits.cuh"
 
 namespace modal {
 
@@ -52,12 +53,25 @@ __global__ void k_wgt48(int nmu, int Kpad, const double *__restrict__ w, double 
     if (k < Kpad) wk[k] = (k < nmu) ? w[k] / (48e0 * 3.14159265358979323846) : 0.0;
 }
 
-// Digits of the rows Y_vt(k) = wk[k] X_v(k) X_t(k) (FP64 product), one warp per
-// row: the row's exponent from its maximum, then s balanced 7-bit digits of
-// y 2^{6 - e + 7(s-1)} rounded to an integer (the ozgemm.cu layout:
-// out[p][r][k], FP16).  Rows >= UV are zero.
+// Z[v][k] = wk[k] X_v(k) for k < K, 0 beyond: the first factor of every Y row
+// of pair v (the product (wk X_v) X_t rounds as wk X_v X_t evaluated left to right).
+__global__ void k_weight_rows(int U, int K, int Kpad, const double *__restrict__ X, const double *__restrict__ wk,
+                              double *__restrict__ Z)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)U * Kpad) return;
+    const int k = (int)(e % Kpad);
+    Z[e] = (k < K) ? wk[k] * X[e] : 0.0;
+}
+
+// Digits of the rows Y_vt(k) = (wk[k] X_v(k)) X_t(k) = Z_v(k) X_t(k) (one FP64
+// product), one warp per row: the row's exponent from its maximum, then s
+// balanced 7-bit digits of y 2^{6 - e + 7(s-1)} rounded to an integer (the
+// ozgemm.cu layout: out[p][r][k], FP16).  Rows >= UV are zero.  The maximum
+// and the scaled rounding run on the bit patterns (integer instructions), so
+// the FP64 pipe sees one multiply per element and pass.
 __global__ void __launch_bounds__(256) k_slice_y(int UV, int UVpad, int K, int Kpad, const int2 *__restrict__ vt,
-                                                 const double *__restrict__ X, long ldx, const double *__restrict__ wk,
+                                                 const double *__restrict__ X, const double *__restrict__ Z, long ldx,
                                                  int s, __half *__restrict__ out, int *__restrict__ ey)
 {
     const long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -72,17 +86,22 @@ __global__ void __launch_bounds__(256) k_slice_y(int UV, int UVpad, int K, int K
         return;
     }
     const int2 p2 = vt[r];
-    const double *xv = X + (size_t)p2.x * ldx, *xt = X + (size_t)p2.y * ldx;
-    double m = 0.0;
-    for (int k = lane; k < K; k += 32) m = fmax(m, fabs(wk[k] * xv[k] * xt[k]));
+    const double *zv = Z + (size_t)p2.x * ldx, *xt = X + (size_t)p2.y * ldx;
+    unsigned long long mb = 0ull;
+    for (int k = lane; k < K; k += 32) mb = dfb::absmax_bits(mb, zv[k] * xt[k]);
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
+    for (int off = 16; off > 0; off >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, off));
+    const double m = __longlong_as_double((long long)mb);
     const int e = (m > 0.0 && isfinite(m)) ? ilogb(m) + 1 : 0;
     if (lane == 0) ey[r] = e;
     const int sh = 6 - e + 7 * (s - 1);
     for (int k = lane; k < Kpad; k += 32) {
-        const double y = (k < K) ? ldexp(wk[k] * xv[k] * xt[k], sh) : 0.0;
-        long long F = isfinite(y) ? __double2ll_rn(y) : 0ll;
+        const double y = (k < K) ? zv[k] * xt[k] : 0.0;
+        long long F;
+        if (!dfb::scaled_rint(y, sh, &F)) {
+            const double ys = ldexp(y, sh);
+            F = isfinite(ys) ? __double2ll_rn(ys) : 0ll;
+        }
         for (int p = s - 1; p > 0; p--) {
             const long long d = ((F + 64) & 127) - 64;
             o[p * plane + k] = __int2half_rn((int)d);
@@ -182,6 +201,7 @@ modal_status gamma_split_dev(modal_ctx *ctx, int mu0, int nmu)
     const size_t o_ys = o; o += al((size_t)SP_SLICES_G * UVpad * Kpad * 2);
     const size_t o_ey = o; o += al((size_t)UVpad * 4);
     const size_t o_T = o; o += al((size_t)U * UV * 8);
+    const size_t o_z = o; o += al((size_t)U * Kpad * 8);
     MODAL_TRY(ensure(ctx->split, o));
     uint8_t *b = ctx->split.as<uint8_t>();
     double *Qp = reinterpret_cast<double *>(b + o_qp), *X = reinterpret_cast<double *>(b + o_x);
@@ -216,8 +236,11 @@ modal_status gamma_split_dev(modal_ctx *ctx, int mu0, int nmu)
     OzOperand xs{reinterpret_cast<__half *>(b + o_xs), reinterpret_cast<int *>(b + o_ex), U, Upad};
     OzOperand ys{reinterpret_cast<__half *>(b + o_ys), reinterpret_cast<int *>(b + o_ey), (int)UV, (int)UVpad};
     MODAL_TRY(oz_slice(ctx, U, nmu, X, Kpad, false, SP_SLICES_G, Upad, Kpad, xs.slices, xs.ex));
+    double *Z = reinterpret_cast<double *>(b + o_z);
+    k_weight_rows<<<ceil_div((long)U * Kpad, 256), 256, 0, ctx->stream>>>(U, nmu, Kpad, X, wk, Z);
+    MODAL_TRY(launched(ctx, "weight_rows"));
     k_slice_y<<<ceil_div(UVpad * 32, 256), 256, 0, ctx->stream>>>((int)UV, (int)UVpad, nmu, Kpad,
-                                                                   reinterpret_cast<const int2 *>(b + o_vtp), X, Kpad, wk,
+                                                                   reinterpret_cast<const int2 *>(b + o_vtp), X, Z, Kpad,
                                                                    SP_SLICES_G, ys.slices, ys.ex);
     MODAL_TRY(launched(ctx, "slice_y"));
     oz.slices = SP_SLICES_G;

@@ -15,11 +15,11 @@
 // is only a host-side stand-in, not a device address, so on the first call
 // on each device (with that device current) the entry point asks the runtime
 // for the real address with cudaGetSymbolAddress and remembers it; later
-// calls on that device reuse it.  That first call should therefore come
-// before any stream capture.  The address is kept for the life of the
+// calls on that device reuse it.  The address is kept for the life of the
 // process, so the device must not be reset (cudaDeviceReset) while the
-// library is loaded.  Every call reads a status word back and waits for its
-// stream before returning.
+// library is loaded.  Every call reads a status word back into a host
+// variable and waits for its stream before returning, so no call (first or
+// later) can be made while a stream is being captured into a CUDA graph.
 //
 // Every call shares the one array and overwrites it; the kernels fully
 // rewrite every region they read, so nothing needs clearing between calls.

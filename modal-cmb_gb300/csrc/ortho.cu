@@ -468,7 +468,10 @@ modal_status cholesky_dev(modal_ctx *ctx, int *fail_row)
             MODAL_TRY(launched(ctx, "trsm_panel"));
             double *A21 = A + (size_t)(kb + nb) * N + kb;
             double *A22 = A + (size_t)(kb + nb) * N + kb + nb;
-            MODAL_TRY(dgemm(ctx, rest, rest, nb, -1.0, A21, N, false, A21, N, true, 1.0, A22, N, 1));
+            // large trailing blocks on the tensor cores (FP64-accurate slices): the
+            // FP64 tiled kernel runs at the FP64 rate, about 1.2 ms per update at 4900 rows
+            if (rest >= 1024) MODAL_TRY(oz_gemm(ctx, rest, rest, nb, -1.0, A21, N, false, A21, N, true, 1.0, A22, N, 1, 8));
+            else MODAL_TRY(dgemm(ctx, rest, rest, nb, -1.0, A21, N, false, A21, N, true, 1.0, A22, N, 1));
         }
     }
     MODAL_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

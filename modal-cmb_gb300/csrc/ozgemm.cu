@@ -40,6 +40,7 @@
 #include <mutex>
 #include <vector>
 #include "common.cuh"
+#include "dfbits.cuh"
 #include "tc_ptx.cuh"
 
 namespace modal {
@@ -89,19 +90,21 @@ __global__ void __launch_bounds__(256) k_oz_rowexp(int R, int K, int kchunk, con
     __shared__ double tile[32][33];
     const int r0 = blockIdx.x * 32, kb = blockIdx.y * kchunk, ke = min(K, kb + kchunk);
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    double mx[4] = {0.0, 0.0, 0.0, 0.0};
+    // the maxima on the bit patterns (integer instructions, not the FP64 pipe)
+    unsigned long long mx[4] = {0ull, 0ull, 0ull, 0ull};
     for (int k0 = kb; k0 < ke; k0 += 32) {
         oz_load_tile(tile, X, ld, trans, R, ke, r0, k0);
         __syncthreads();
 #pragma unroll
-        for (int j = 0; j < 4; j++) mx[j] = fmax(mx[j], fabs(tile[ty + 8 * j][tx]));
+        for (int j = 0; j < 4; j++) mx[j] = dfb::absmax_bits(mx[j], tile[ty + 8 * j][tx]);
         __syncthreads();
     }
 #pragma unroll
     for (int j = 0; j < 4; j++) {
-        double v = mx[j];
+        unsigned long long b = mx[j];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_xor_sync(0xffffffffu, b, o));
+        const double v = __longlong_as_double((long long)b);
         const int r = r0 + ty + 8 * j;
         if (tx == 0 && r < R && v > 0.0 && isfinite(v)) atomicMax(ex + r, ilogb(v) + 1);
     }
@@ -131,10 +134,16 @@ __global__ void __launch_bounds__(256) k_oz_slice(int R, int K, int Rpad, int Kp
         __syncthreads();
         for (int rr = ty; rr < 32; rr += 8) {
             const int r = r0 + rr, k = k0 + tx;
-            // F = x 2^{6 - e + 7(s-1)} rounded to an integer, |F| < 2^55; its balanced
+            // F = x 2^{6 - e + 7(s-1)} rounded to an integer, |F| < 2^55 (from the bits
+            // of x; FP64 instructions only outside that route's range); its balanced
             // base-128 digits, least significant first, are exact integer operations
-            const double y = (k0 < K) ? ldexp(tile[rr][tx], 6 - sexp[rr] + 7 * (s - 1)) : 0.0;
-            long long F = isfinite(y) ? __double2ll_rn(y) : 0ll;
+            const double x = (k0 < K) ? tile[rr][tx] : 0.0;
+            const int sh = 6 - sexp[rr] + 7 * (s - 1);
+            long long F;
+            if (!dfb::scaled_rint(x, sh, &F)) {
+                const double y = ldexp(x, sh);
+                F = isfinite(y) ? __double2ll_rn(y) : 0ll;
+            }
             __half *o = out + (size_t)r * Kpad + k;
             for (int p = s - 1; p > 0; p--) {
                 const long long d = ((F + 64) & 127) - 64;

@@ -33,6 +33,7 @@
 #include <cmath>
 #include <vector>
 #include "common.cuh"
+#include "dfbits.cuh"
 
 namespace modal {
 
@@ -155,8 +156,12 @@ __device__ __forceinline__ double grid_total(const double *part, int comp, int l
 // reductions over all rows and the head row of each reflector go through
 // global memory.  Shared memory: v (n doubles) | V rows | W rows (R x NB each) | y | a.
 // x = head + tail with |x - head - tail| <= 2^-48 |x|
+// (head, tail) floats of x: the bits of (RN(x), RN(x - RN(x))), by integer
+// arithmetic where it covers x (dfbits.cuh), else by FP64 conversions
 __device__ __forceinline__ float2 df_split(double x)
 {
+    uint32_t hb, lb;
+    if (dfb::split(x, &hb, &lb)) return make_float2(__uint_as_float(hb), __uint_as_float(lb));
     const float h = __double2float_rn(x);
     return make_float2(h, __double2float_rn(x - (double)h));
 }
@@ -482,7 +487,9 @@ __global__ void __launch_bounds__(TRD_THREADS, 1) k_trd_panel(TrdArgs g)
 
 // The trailing block [s, n) x [s, n) as double-float pairs, both triangles,
 // from the FP64 lower triangle: one CTA per lower 32 x 32 tile writes the
-// tile and its transpose (the diagonal tile reflects within itself).
+// tile and its transpose (the diagonal tile reflects within itself).  The
+// pairs come from the integer split (one pass of integer instructions per
+// element instead of four FP64 conversions and subtractions).
 __global__ void k_trail_hilo(const double *__restrict__ A, int n, int s, float2 *__restrict__ Ahl)
 {
     __shared__ double tile[32][33];
@@ -1209,6 +1216,7 @@ static modal_status trd_run(modal_ctx *ctx, int n, double *A, SyevPtrs &p, int n
         const int s = j0 + nbp, rest = n - s;
         if (rest > 0) {
             // A22 -= V W^T + W V^T = [V W] [W V]^T on the lower triangle (tensor cores, FP64 accuracy)
+            // the same epilogue refreshes the block's (head, tail) float copy, both triangles
             double *A22 = A + (size_t)s * n + s;
             MODAL_TRY(oz_gemm_ex(ctx, rest, rest, LDP, -1.0, p.P + (size_t)s * LDP, LDP, false, p.Psw + (size_t)s * LDP,
                                  LDP, true, 1.0, A22, n, oz));

@@ -443,7 +443,8 @@ modal_status modal_adjoint_residual(modal_ctx *ctx, int S, const modal_shape *sh
  * prints it (:326-343).  Both arrays are host [N - nfail].  gamma: host
  * [N][N] (the master Gamma the reference reads, :90-109) or NULL for the
  * device Gamma of modal_gamma (N must match).  Every leave-one-out smallest
- * eigenvalue comes from one eigendecomposition per step (FP64, cuSOLVER) and
+ * eigenvalue comes from one eigendecomposition per step (FP64, the library's
+ * own eigensolver) and
  * the secular equation of the minor (see prune.cu), not one eigensolve per
  * candidate.  Repeated or out-of-range fail-list entries give MODAL_ERR_ARG
  * (the reference would mis-size its active list). */
